@@ -1,0 +1,348 @@
+"""Benchmark: candidate poses scored per second, box 128 / 5,000 particles.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Workload (seeded synthetic data of the reference's published shapes): a
+3,000-atom moving chain over a 20,000-atom fixed context, box 128 at
+1.1 A/px, 5,000 particles (CTF, SNR 0.05), HEALPix order 3 directions
+(768) searched +-10 deg, psi step 7.5 deg, translations +-5 px (crop 12),
+logistic FSC. One step scores one candidate pose (a 3 deg / 1.5 A rigid
+perturbation of the moving chain) end to end: splat, 3-D FFT, templates of
+every needed direction, correlation of every particle, records, score.
+
+The GB300 arm times K steps with CUDA events on the launching stream (job
+tables and particle spectra resident in HBM, the 1.0 GB particle stack is
+read every step, so inputs exceed L2), then the same K poses through the
+public API with the pose copied host->device and the score plus the
+per-particle peaks copied back each step (``e2e``). The reference arm
+(``--impl reference``) times the CPU oracle, the numpy restatement of the
+reference's CPU path, on a bounded sample of the same workload per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+METRIC = "candidates scored/s @box128·5k ptcl vs plain FP32 GPU; p50/p99 latency"
+UNIT = "candidates/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
+    ap.add_argument("--workload", default="box128_5kp")
+    ap.add_argument("--particles", type=int, default=0, help="override the particle count (tests only)")
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=48, help="particles and templates in the CPU sample")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+
+def make_workload(name: str, seed: int, device: str, particles: int = 0):
+    from gisapr_gb300 import synthetic as syn
+    spec = syn.WORKLOADS[name]
+    job = syn.make_job(spec, seed=seed, device=device, n_particles=particles or None)
+    return spec, job
+
+
+def job_records(job):
+    from gisapr_gb300.tables import ParticleRecord
+    r = job.records
+    return [ParticleRecord(int(r.line_index[i]), f"{i + 1}@particles.mrcs", float(r.rot[i]), float(r.tilt[i]),
+                           float(r.psi[i]), float(r.defocus_u[i]), float(r.defocus_v[i]),
+                           float(r.defocus_angle[i])) for i in range(len(r.rot))]
+
+
+def cpu_baseline(spec, job, pose, sample: int):
+    from oracle.cpu_baseline import time_candidate
+    r = job.records
+    out = time_candidate(job.model.pdb_text, pose, spec.box, spec.apix, spec.res, job.model_rot, job.model_tilt,
+                         job.images, r, job.fsc, spec.mask_radius, spec.mask_edge, spec.psi_step,
+                         spec.local_range, spec.crop, kk=spec.kk, n_template_sample=sample,
+                         n_particle_sample=sample)
+    return out
+
+
+def correlation_flops(n: int, maps: int) -> float:
+    """Algorithmic flops of the plain correlation: M * (6K + 2.5 n^2 log2 n^2)."""
+    K = n * (n // 2 + 1)
+    return maps * (6.0 * K + 2.5 * n * n * math.log2(n * n))
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+def profiled_traffic(kernel: str, workload: str):
+    """DRAM bytes per launch of ``kernel`` from the committed ncu summary."""
+    p = ROOT / "profiles" / "traffic.json"
+    if not p.exists():
+        return None
+    try:
+        d = json.loads(p.read_text())
+        return d.get(workload, {}).get(kernel)
+    except (ValueError, OSError):
+        return None
+
+
+# ---------------------------------------------------------------------------
+# arms
+# ---------------------------------------------------------------------------
+
+def run_reference(args):
+    from gisapr_gb300 import synthetic as syn
+    n_sample = max(8, args.cpu_sample)
+    spec = syn.WORKLOADS[args.workload]
+    # the sample needs only the particles it times; the model, box and
+    # direction set are the full workload's
+    spec_s, job = make_workload(args.workload, args.seed, "cpu", particles=max(n_sample, 64))
+    poses = syn.candidate_poses(args.steps + args.warmup, args.seed + 100, spec.pose_rotation_deg,
+                                spec.pose_translation, exact=True)
+    per = []
+    info = None
+    for k in range(args.warmup + args.steps):
+        info = cpu_baseline(spec, job, poses[k], n_sample)
+        # scale the per-particle cost to the full particle count of the workload
+        secs = (info["density_s"] + info["volume_fft_s"] + info["template_s"] * info["n_templates"]
+                + info["particle_s"] * spec.n_particles)
+        if k >= args.warmup:
+            per.append(secs)
+    sec = statistics.mean(per)
+    value = 1.0 / sec
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{args.workload}: box {spec.box}, {spec.n_particles} particles, "
+                               f"{spec.n_moving_atoms}+{spec.n_fixed_atoms} atoms, HEALPix order "
+                               f"{spec.healpix_order}, +-{spec.local_range} deg, crop {spec.crop}",
+                   "candidates_per_step": 1},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": int(info["threads"]), "kind": "port",
+                         "sample": f"per step: full moving-chain splat and 3-D FFT, {int(info['sample_templates'])}"
+                                   f" of {int(info['n_templates'])} templates and {int(info['sample_particles'])}"
+                                   f" of {spec.n_particles} particles (prepare + correlate), extrapolated"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args, rank: int, world: int, local_rank: int):
+    import numpy as np
+    import torch
+    import __graft_entry__ as g
+    from gisapr_gb300 import synthetic as syn
+    from gisapr_gb300.engine import JobConfig, ScoringJob
+    from gisapr_gb300.tables import model_angles_from_lists
+
+    g.build()
+    device = torch.device("cuda", local_rank)
+    torch.cuda.set_device(device)
+    t_setup = time.perf_counter()
+    spec, data = make_workload(args.workload, args.seed + rank, str(device), args.particles)
+    t_data = time.perf_counter() - t_setup
+    cfg = JobConfig(box=spec.box, apix=spec.apix, crop=spec.crop, psi_step=spec.psi_step,
+                    local_range=spec.local_range, mask_edge=spec.mask_edge, kk=spec.kk)
+    job = ScoringJob(cfg, data.model.pdb_text, model_angles_from_lists(data.model_rot, data.model_tilt),
+                     job_records(data), data.images, fsc_values=data.fsc, device=device)
+    K, W = args.steps, args.warmup
+    poses = syn.candidate_poses(K + W, args.seed + 100 + rank, spec.pose_rotation_deg, spec.pose_translation,
+                                exact=True)
+    pose_dev = torch.stack([job.density.pose_tensor(p) for p in poses]).to(device)
+    for k in range(W):
+        job.enqueue(pose_dev[k])
+    torch.cuda.synchronize(device)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # ---- device-timed region: poses resident in HBM
+    stage_events = {}
+    step_ev = []
+    clocks = ClockSampler(local_rank)
+    barrier()
+    torch.cuda.synchronize(device)
+    clocks.start()
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    start.record()
+    for k in range(K):
+        e = torch.cuda.Event(enable_timing=True)
+        e.record()
+        step_ev.append(e)
+        job.enqueue(pose_dev[W + k], stage_events=stage_events)
+    end.record()
+    torch.cuda.synchronize(device)
+    barrier()
+    clk = clocks.stop()
+    elapsed = start.elapsed_time(end) / 1e3
+    step_ev.append(end)
+    lat = sorted(step_ev[i].elapsed_time(step_ev[i + 1]) for i in range(K))
+    stage_ms = {s: statistics.mean(a.elapsed_time(b) for a, b in v) for s, v in stage_events.items()}
+
+    # ---- end to end through the public API, host buffers each step
+    peaks_host = torch.empty(len(job.records), dtype=torch.float32).pin_memory()
+    barrier()
+    torch.cuda.synchronize(device)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    scores = []
+    for k in range(K):
+        scores.append(job.score(poses[W + k]))
+        peaks_host.copy_(job.peak, non_blocking=True)
+    e1.record()
+    torch.cuda.synchronize(device)
+    barrier()
+    e2e_elapsed = e0.elapsed_time(e1) / 1e3
+
+    times = torch.tensor([elapsed, e2e_elapsed], dtype=torch.float64, device=device)
+    if world > 1:
+        torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
+    elapsed, e2e_elapsed = float(times[0]), float(times[1])
+    if rank != 0:
+        return
+    value = world * K / elapsed
+    e2e_value = world * K / e2e_elapsed
+    hbm_peak, bf16_peak, peak_kind = load_peaks()
+    maps = job.nnz * job.n_psi
+    flops = correlation_flops(cfg.new_box, maps)
+    corr_s = stage_ms["correlate"] / 1e3
+    dominant = max(stage_ms, key=stage_ms.get)
+    achieved = flops / corr_s / 1e12
+    roofline = {
+        "kernel": "correlate_plain", "bound": "tensor", "achieved": achieved, "peak": bf16_peak,
+        "unit": "TFLOP/s", "frac": achieved / bf16_peak, "traffic": profiled_traffic("correlate_plain", args.workload),
+        "peak_source": f"{peak_kind} bf16 dense (MEASURED_PEAKS.json)" if peak_kind == "measured" else "fallback",
+        "algorithmic": f"{flops:.4g} flop per launch = {maps} maps x (6K + 2.5 n^2 log2 n^2), n={cfg.new_box}",
+        "note": "plain FP32 correlation runs on CUDA cores; its fraction is against the bf16 tensor peak",
+        "dominant_stage": dominant, "stage_ms": stage_ms,
+    }
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": elapsed / K * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{args.workload}: plain FP32, one candidate per step",
+                   "box": spec.box, "apix": spec.apix, "particles": len(job.records),
+                   "moving_atoms": job.density.n_moving, "fixed_atoms": job.density.fixed_atom_count,
+                   "directions": len(data.model_rot), "needed_directions": len(job.needed),
+                   "maps_per_candidate": maps, "local_range_deg": spec.local_range, "psi_step_deg": spec.psi_step,
+                   "crop": spec.crop, "candidates_per_step": 1, "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2: the 1.0 GB particle stack is read every step"},
+        "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(math.ceil(0.99 * len(lat))) - 1)]},
+        "roofline": roofline,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 12 * 8,
+                "d2h_bytes_per_step": 8 + 4 * len(job.records)},
+        "gpu_launches": ScoringJob.KERNELS_PER_CANDIDATE * K,
+        "clocks": clk,
+        "setup_s": {"synthetic_data": t_data, "job": job.setup_s},
+        "score_sample": scores[0],
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        cb = cpu_baseline(spec, data, poses[W], args.cpu_sample)
+        line["cpu_baseline"] = {
+            "value": 1.0 / cb["seconds_per_candidate"], "unit": UNIT, "cores": int(cb["threads"]), "kind": "port",
+            "sample": f"one pose: full moving-chain splat and 3-D FFT, {int(cb['sample_templates'])} of "
+                      f"{int(cb['n_templates'])} templates, {int(cb['sample_particles'])} of {len(job.records)} "
+                      f"particles (prepare + correlate), extrapolated ({cb['sample_wall_s']:.1f} s of CPU work)"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        run_reference(args)
+        return
+    if world > 1:
+        import torch
+        torch.cuda.set_device(local_rank)
+        torch.distributed.init_process_group("nccl")
+    try:
+        run_gb300(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch
+            torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,472 @@
+// C ABI entry points (include/gisapr_gb300.h): argument checks, per-device
+// context (twiddle and radial-bin tables, cuFFT plans, scratch) and launches.
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/gisapr_gb300.h"
+#include "common.cuh"
+
+// ---- launchers defined in the other translation units
+cudaError_t launch_atoms_prepare(cudaStream_t, const float*, const float*, int, int, const float*,
+                                 const double*, const double*, int, int, double, double, void*);
+size_t atom_record_bytes();
+cudaError_t launch_splat_bricks(cudaStream_t, const void*, int, const float*, float*, float*, int,
+                                double);
+cudaError_t launch_pad_sinc_shift(cudaStream_t, const float*, float*, int);
+size_t project_scratch_elems(int N, int nb);
+size_t project_smem_bytes(int N, int n_bins);
+cudaError_t launch_project_templates(cudaStream_t, const float2*, const float*, const int*, int,
+                                     const int*, const float*, const float*, const int*, const int*,
+                                     const float*, int, const float2*, float2*, float2*, int, int,
+                                     int);
+cudaError_t launch_packed_ctf(cudaStream_t, const float*, const float*, const float*, int,
+                              const float*, const float*, const float*, const float*, int, float,
+                              float, float, float, float, float*);
+size_t prepare_scratch_elems(int N, int nb);
+cudaError_t launch_prepare_particles(cudaStream_t, const float*, int, int, const int*, const void*,
+                                     const float*, const float*, float2*, float2*, int,
+                                     const float2*, int, int);
+int correlate_cluster_size(int n);
+size_t correlate_smem_bytes(int n, int n_psi, int crop);
+cudaError_t launch_correlate_plain(cudaStream_t, const float2*, const float2*, const int*,
+                                   const int*, int, int, int, int, const float2*, const float2*,
+                                   float*, int*, int*);
+cudaError_t launch_particle_results(cudaStream_t, const int*, const float*, const int*, const int*,
+                                    int, int, int*, int*, float*, int*, int*, float*);
+cudaError_t launch_score_sum(cudaStream_t, const int*, const float*, int, double*);
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* where) {
+  return fail(GISAPR_ERR_CUDA, std::string(where) + ": " + cudaGetErrorName(e) + " (" +
+                                   cudaGetErrorString(e) + ")");
+}
+
+#define GISAPR_CHECK_CUDA(expr, where)          \
+  do {                                          \
+    cudaError_t _e = (expr);                    \
+    if (_e != cudaSuccess) return cuda_fail(_e, where); \
+  } while (0)
+
+bool is_pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
+
+struct DeviceBuffer {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+};
+
+struct BinTable {
+  int* list = nullptr;
+  int* ptr = nullptr;
+  float* count = nullptr;
+  int n_bins = 0;
+};
+
+struct CorrTables {
+  float2* outer = nullptr;  // [M][C]
+  float2* col = nullptr;    // [H][C]
+};
+
+}  // namespace
+
+struct gisapr_context {
+  int device = 0;
+  float2* tw = nullptr;  // exp(-2 pi i t / kMaxFftLen), t < kMaxFftLen/2
+  std::map<int, std::pair<cufftHandle, float*>> fft;  // box -> (R2C plan, padded input)
+  std::map<int, BinTable> bins;                        // N -> radial bins
+  std::map<std::pair<int, int>, CorrTables> corr;      // (n, crop) -> twiddles
+  DeviceBuffer atoms, proj_scratch, prep_scratch;
+  int sm_count = 152;
+};
+
+namespace {
+
+int set_device(gisapr_ctx ctx) {
+  GISAPR_CHECK_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  return GISAPR_OK;
+}
+
+int ensure(DeviceBuffer& b, size_t bytes, const char* what) {
+  if (b.bytes >= bytes) return GISAPR_OK;
+  if (b.ptr) cudaFree(b.ptr);
+  b.ptr = nullptr;
+  b.bytes = 0;
+  cudaError_t e = cudaMalloc(&b.ptr, bytes);
+  if (e != cudaSuccess) return cuda_fail(e, what);
+  b.bytes = bytes;
+  return GISAPR_OK;
+}
+
+int get_fft(gisapr_ctx ctx, int box, cufftHandle* plan, float** padded) {
+  auto it = ctx->fft.find(box);
+  if (it != ctx->fft.end()) {
+    *plan = it->second.first;
+    *padded = it->second.second;
+    return GISAPR_OK;
+  }
+  const int m = 2 * box;
+  float* buf = nullptr;
+  const size_t bytes = (size_t)m * m * m * sizeof(float);
+  cudaError_t e = cudaMalloc(&buf, bytes);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(FFT input)");
+  // The zero padding outside the centred box is written once and never
+  // touched again: the splat and pad kernels only write the box region and
+  // an out-of-place R2C leaves its input unchanged.
+  e = cudaMemset(buf, 0, bytes);
+  if (e != cudaSuccess) { cudaFree(buf); return cuda_fail(e, "cudaMemset(FFT input)"); }
+  cufftHandle h;
+  cufftResult r = cufftPlan3d(&h, m, m, m, CUFFT_R2C);
+  if (r != CUFFT_SUCCESS) {
+    cudaFree(buf);
+    return fail(GISAPR_ERR_CUFFT, "cufftPlan3d failed with code " + std::to_string((int)r));
+  }
+  ctx->fft[box] = {h, buf};
+  *plan = h;
+  *padded = buf;
+  return GISAPR_OK;
+}
+
+int get_bins(gisapr_ctx ctx, int N, BinTable* out) {
+  auto it = ctx->bins.find(N);
+  if (it != ctx->bins.end()) { *out = it->second; return GISAPR_OK; }
+  const int HC = N / 2 + 1;
+  std::vector<int> bin_of(N * HC);
+  int max_bin = 0;
+  for (int r = 0; r < N; ++r)
+    for (int kx = 0; kx < HC; ++kx) {
+      const int ky = r < N / 2 ? r : r - N;
+      const int b = (int)std::nearbyint(std::sqrt((float)(ky * ky + kx * kx)));
+      bin_of[r * HC + kx] = b;
+      if (b > max_bin) max_bin = b;
+    }
+  const int nb = max_bin + 1;
+  // full-grid counts, radius of the fftshifted N x N grid (v606:901-913)
+  std::vector<float> cnt(nb, 0.f);
+  for (int y = 0; y < N; ++y)
+    for (int x = 0; x < N; ++x) {
+      const int dy = y - N / 2, dx = x - N / 2;
+      const int b = (int)std::nearbyint(std::sqrt((float)(dy * dy + dx * dx)));
+      if (b < nb) cnt[b] += 1.f;
+    }
+  std::vector<int> ptr(nb + 1, 0), list(N * HC);
+  for (int i = 0; i < N * HC; ++i) ptr[bin_of[i] + 1]++;
+  for (int b = 0; b < nb; ++b) ptr[b + 1] += ptr[b];
+  std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+  for (int i = 0; i < N * HC; ++i) list[fill[bin_of[i]]++] = i;
+  BinTable t;
+  t.n_bins = nb;
+  GISAPR_CHECK_CUDA(cudaMalloc(&t.list, list.size() * sizeof(int)), "cudaMalloc(bins)");
+  GISAPR_CHECK_CUDA(cudaMalloc(&t.ptr, ptr.size() * sizeof(int)), "cudaMalloc(bins)");
+  GISAPR_CHECK_CUDA(cudaMalloc(&t.count, cnt.size() * sizeof(float)), "cudaMalloc(bins)");
+  GISAPR_CHECK_CUDA(cudaMemcpy(t.list, list.data(), list.size() * sizeof(int), cudaMemcpyHostToDevice),
+                    "cudaMemcpy(bins)");
+  GISAPR_CHECK_CUDA(cudaMemcpy(t.ptr, ptr.data(), ptr.size() * sizeof(int), cudaMemcpyHostToDevice),
+                    "cudaMemcpy(bins)");
+  GISAPR_CHECK_CUDA(cudaMemcpy(t.count, cnt.data(), cnt.size() * sizeof(float), cudaMemcpyHostToDevice),
+                    "cudaMemcpy(bins)");
+  ctx->bins[N] = t;
+  *out = t;
+  return GISAPR_OK;
+}
+
+int get_corr_tables(gisapr_ctx ctx, int n, int crop, CorrTables* out) {
+  auto key = std::make_pair(n, crop);
+  auto it = ctx->corr.find(key);
+  if (it != ctx->corr.end()) { *out = it->second; return GISAPR_OK; }
+  const int M = n / 16, H = n / 2 + 1, h = crop / 2;
+  const double two_pi = 6.283185307179586476925286766559;
+  std::vector<float2> outer((size_t)M * crop), col((size_t)H * crop);
+  for (int q = 0; q < M; ++q)
+    for (int yi = 0; yi < crop; ++yi) {
+      const double a = two_pi * (double)q * (double)(yi - h) / (double)n;
+      outer[(size_t)q * crop + yi] = make_float2((float)std::cos(a), (float)std::sin(a));
+    }
+  for (int c = 0; c < H; ++c) {
+    const double w = (c == 0 || c == n / 2) ? 1.0 : 2.0;
+    for (int xi = 0; xi < crop; ++xi) {
+      const double a = two_pi * (double)c * (double)(xi - h) / (double)n;
+      col[(size_t)c * crop + xi] = make_float2((float)(w * std::cos(a)), (float)(w * std::sin(a)));
+    }
+  }
+  CorrTables t;
+  GISAPR_CHECK_CUDA(cudaMalloc(&t.outer, outer.size() * sizeof(float2)), "cudaMalloc(corr)");
+  GISAPR_CHECK_CUDA(cudaMalloc(&t.col, col.size() * sizeof(float2)), "cudaMalloc(corr)");
+  GISAPR_CHECK_CUDA(cudaMemcpy(t.outer, outer.data(), outer.size() * sizeof(float2), cudaMemcpyHostToDevice),
+                    "cudaMemcpy(corr)");
+  GISAPR_CHECK_CUDA(cudaMemcpy(t.col, col.data(), col.size() * sizeof(float2), cudaMemcpyHostToDevice),
+                    "cudaMemcpy(corr)");
+  ctx->corr[key] = t;
+  *out = t;
+  return GISAPR_OK;
+}
+
+int check_box(int box) {
+  if (!is_pow2(box) || box < 32 || box > 256)
+    return fail(GISAPR_ERR_UNSUPPORTED, "box must be a power of two in [32, 256], got " + std::to_string(box));
+  return GISAPR_OK;
+}
+
+int check_newbox(int box, int nb) {
+  if (nb <= 0 || nb % 16 != 0 || nb > box)
+    return fail(GISAPR_ERR_ARGUMENT, "newbox must be a positive multiple of 16 not above box, got " +
+                                         std::to_string(nb));
+  return GISAPR_OK;
+}
+
+int grid_for(gisapr_ctx ctx, int work, int per_sm) {
+  int g = ctx->sm_count * per_sm;
+  return work < g ? work : g;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gisapr_abi_version(void) { return 100; }
+
+const char* gisapr_last_error(void) { return g_last_error.c_str(); }
+
+int gisapr_context_create(int device, gisapr_ctx* out) {
+  if (!out) return fail(GISAPR_ERR_ARGUMENT, "out is NULL");
+  *out = nullptr;
+  int n_dev = 0;
+  GISAPR_CHECK_CUDA(cudaGetDeviceCount(&n_dev), "cudaGetDeviceCount");
+  if (device < 0 || device >= n_dev)
+    return fail(GISAPR_ERR_ARGUMENT, "device index out of range: " + std::to_string(device));
+  GISAPR_CHECK_CUDA(cudaSetDevice(device), "cudaSetDevice");
+  gisapr_context* ctx = new gisapr_context();
+  ctx->device = device;
+  cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+  std::vector<float2> tw(kMaxFftLen / 2);
+  const double two_pi = 6.283185307179586476925286766559;
+  for (int t = 0; t < kMaxFftLen / 2; ++t) {
+    const double a = -two_pi * (double)t / (double)kMaxFftLen;
+    tw[t] = make_float2((float)std::cos(a), (float)std::sin(a));
+  }
+  cudaError_t e = cudaMalloc(&ctx->tw, tw.size() * sizeof(float2));
+  if (e == cudaSuccess) e = cudaMemcpy(ctx->tw, tw.data(), tw.size() * sizeof(float2), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    delete ctx;
+    return cuda_fail(e, "context tables");
+  }
+  *out = ctx;
+  return GISAPR_OK;
+}
+
+int gisapr_context_destroy(gisapr_ctx ctx) {
+  if (!ctx) return GISAPR_OK;
+  cudaSetDevice(ctx->device);
+  cudaDeviceSynchronize();
+  for (auto& kv : ctx->fft) { cufftDestroy(kv.second.first); cudaFree(kv.second.second); }
+  for (auto& kv : ctx->bins) { cudaFree(kv.second.list); cudaFree(kv.second.ptr); cudaFree(kv.second.count); }
+  for (auto& kv : ctx->corr) { cudaFree(kv.second.outer); cudaFree(kv.second.col); }
+  cudaFree(ctx->atoms.ptr);
+  cudaFree(ctx->proj_scratch.ptr);
+  cudaFree(ctx->prep_scratch.ptr);
+  cudaFree(ctx->tw);
+  delete ctx;
+  return GISAPR_OK;
+}
+
+static int deposit_common(gisapr_ctx ctx, void* stream, const float* xyz, const float* numbers, int n,
+                          int transform, const float* pivot, const double* rot, const double* shift,
+                          const float* initial, float* out, float* padded, int box, int width,
+                          double apix, double rp, double kn) {
+  if (!ctx) return fail(GISAPR_ERR_ARGUMENT, "context is NULL");
+  if (n < 0 || (n > 0 && (!xyz || !numbers)))
+    return fail(GISAPR_ERR_ARGUMENT, "atom arrays are NULL or n_atoms < 0");
+  if (box < 1 || box > 1024) return fail(GISAPR_ERR_ARGUMENT, "box out of range");
+  if (width < 3) return fail(GISAPR_ERR_ARGUMENT, "width must be >= 3 (insufficient sampling)");
+  if (!(apix > 0.0) || !std::isfinite(apix) || !std::isfinite(rp) || !std::isfinite(kn))
+    return fail(GISAPR_ERR_ARGUMENT, "apix, rp and kn must be positive and finite");
+  if (transform && (!pivot || !rot || !shift)) return fail(GISAPR_ERR_ARGUMENT, "pose arrays are NULL");
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  rc = ensure(ctx->atoms, (size_t)(n > 0 ? n : 1) * atom_record_bytes(), "cudaMalloc(atoms)");
+  if (rc) return rc;
+  GISAPR_CHECK_CUDA(launch_atoms_prepare(st, xyz, numbers, n, transform, pivot, rot, shift, box, width,
+                                         apix, kn, ctx->atoms.ptr),
+                    "atoms_prepare");
+  GISAPR_CHECK_CUDA(launch_splat_bricks(st, ctx->atoms.ptr, n, initial, out, padded, box, rp),
+                    "splat_bricks");
+  return GISAPR_OK;
+}
+
+int gisapr_deposit(gisapr_ctx ctx, void* stream, const float* xyz, const float* numbers, int n_atoms,
+                   float* volume, int box, int width, double apix, double rp, double kn) {
+  if (!volume) return fail(GISAPR_ERR_ARGUMENT, "volume is NULL");
+  return deposit_common(ctx, stream, xyz, numbers, n_atoms, 0, nullptr, nullptr, nullptr, volume, volume,
+                        nullptr, box, width, apix, rp, kn);
+}
+
+int gisapr_deposit_moved(gisapr_ctx ctx, void* stream, const float* xyz, const float* numbers,
+                         int n_atoms, const float* pivot, const double* rot, const double* shift,
+                         const float* fixed, float* out, int write_padded, int box, int width,
+                         double apix, double rp, double kn) {
+  if (!ctx) return fail(GISAPR_ERR_ARGUMENT, "context is NULL");
+  if (!out && !write_padded) return fail(GISAPR_ERR_ARGUMENT, "nothing to write: out is NULL and write_padded is 0");
+  float* padded = nullptr;
+  if (write_padded) {
+    int rc = check_box(box);
+    if (rc) return rc;
+    rc = set_device(ctx);
+    if (rc) return rc;
+    cufftHandle plan;
+    rc = get_fft(ctx, box, &plan, &padded);
+    if (rc) return rc;
+  }
+  return deposit_common(ctx, stream, xyz, numbers, n_atoms, 1, pivot, rot, shift, fixed, out, padded, box,
+                        width, apix, rp, kn);
+}
+
+int gisapr_volume_spectrum(gisapr_ctx ctx, void* stream, const float* volume, int box, float* spectrum) {
+  if (!ctx || !spectrum) return fail(GISAPR_ERR_ARGUMENT, "context or spectrum is NULL");
+  int rc = check_box(box);
+  if (rc) return rc;
+  rc = set_device(ctx);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  cufftHandle plan;
+  float* padded = nullptr;
+  rc = get_fft(ctx, box, &plan, &padded);
+  if (rc) return rc;
+  if (volume) GISAPR_CHECK_CUDA(launch_pad_sinc_shift(st, volume, padded, box), "pad_sinc_shift");
+  cufftResult r = cufftSetStream(plan, st);
+  if (r != CUFFT_SUCCESS) return fail(GISAPR_ERR_CUFFT, "cufftSetStream failed");
+  r = cufftExecR2C(plan, (cufftReal*)padded, (cufftComplex*)spectrum);
+  if (r != CUFFT_SUCCESS) return fail(GISAPR_ERR_CUFFT, "cufftExecR2C failed with code " + std::to_string((int)r));
+  return GISAPR_OK;
+}
+
+int gisapr_project_templates(gisapr_ctx ctx, void* stream, const float* spectrum, int box,
+                             const float* rot, const int* dirs, int n_build, const int* out_slot,
+                             const float* mask, const float* fsc, int newbox, float* bank) {
+  if (!ctx || !spectrum || !rot || !dirs || !fsc || !bank)
+    return fail(GISAPR_ERR_ARGUMENT, "a required pointer is NULL");
+  int rc = check_box(box);
+  if (rc) return rc;
+  rc = check_newbox(box, newbox);
+  if (rc) return rc;
+  if (n_build < 0) return fail(GISAPR_ERR_ARGUMENT, "n_build < 0");
+  if (n_build == 0) return GISAPR_OK;
+  rc = set_device(ctx);
+  if (rc) return rc;
+  BinTable bt;
+  rc = get_bins(ctx, box, &bt);
+  if (rc) return rc;
+  const int grid = grid_for(ctx, n_build, 2);
+  rc = ensure(ctx->proj_scratch, (size_t)grid * project_scratch_elems(box, newbox) * sizeof(float2),
+              "cudaMalloc(projector scratch)");
+  if (rc) return rc;
+  GISAPR_CHECK_CUDA(launch_project_templates((cudaStream_t)stream, (const float2*)spectrum, rot, dirs, n_build,
+                                             out_slot, mask, fsc, bt.list, bt.ptr, bt.count, bt.n_bins,
+                                             ctx->tw, (float2*)bank, (float2*)ctx->proj_scratch.ptr, grid,
+                                             box, newbox),
+                    "project_templates");
+  return GISAPR_OK;
+}
+
+int gisapr_packed_ctf(void* stream, const float* dfu, const float* dfv, const float* dfa, int n,
+                      const float* tx, const float* ty, const float* tu4, const float* tnc, int K,
+                      float k1, float k2, float k3, float k5, float kk, float* out) {
+  if (n < 0 || K <= 0) return fail(GISAPR_ERR_ARGUMENT, "n < 0 or K <= 0");
+  if (n > 0 && (!dfu || !dfv || !dfa || !tx || !ty || !tu4 || !tnc || !out))
+    return fail(GISAPR_ERR_ARGUMENT, "a required pointer is NULL");
+  if (n > 65535) return fail(GISAPR_ERR_ARGUMENT, "at most 65535 particles per CTF call");
+  GISAPR_CHECK_CUDA(launch_packed_ctf((cudaStream_t)stream, dfu, dfv, dfa, n, tx, ty, tu4, tnc, K, k1, k2,
+                                      k3, k5, kk, out),
+                    "packed_ctf");
+  return GISAPR_OK;
+}
+
+int gisapr_prepare_particles(gisapr_ctx ctx, void* stream, const float* images, int n, int n_psi,
+                             const int* psi_index, const float* psi_table, const float* mask,
+                             const float* ctf, int box, int newbox, float* out) {
+  if (!ctx) return fail(GISAPR_ERR_ARGUMENT, "context is NULL");
+  if (n < 0 || n_psi <= 0) return fail(GISAPR_ERR_ARGUMENT, "n < 0 or n_psi <= 0");
+  if (n > 0 && (!images || !psi_index || !psi_table || !ctf || !out))
+    return fail(GISAPR_ERR_ARGUMENT, "a required pointer is NULL");
+  int rc = check_box(box);
+  if (rc) return rc;
+  rc = check_newbox(box, newbox);
+  if (rc) return rc;
+  if (n == 0) return GISAPR_OK;
+  rc = set_device(ctx);
+  if (rc) return rc;
+  const int grid = grid_for(ctx, n * n_psi, 4);
+  rc = ensure(ctx->prep_scratch, (size_t)grid * prepare_scratch_elems(box, newbox) * sizeof(float2),
+              "cudaMalloc(particle scratch)");
+  if (rc) return rc;
+  GISAPR_CHECK_CUDA(launch_prepare_particles((cudaStream_t)stream, images, n, n_psi, psi_index, psi_table, mask,
+                                             ctf, (float2*)out, (float2*)ctx->prep_scratch.ptr, grid, ctx->tw,
+                                             box, newbox),
+                    "prepare_particles");
+  return GISAPR_OK;
+}
+
+int gisapr_correlate(gisapr_ctx ctx, void* stream, const float* bank, const float* stack,
+                     const int* local_ptr, const int* local_idx, int n_particles, int n_psi, int n,
+                     int crop, float* out_score, int* out_y, int* out_x) {
+  if (!ctx) return fail(GISAPR_ERR_ARGUMENT, "context is NULL");
+  if (n_particles < 0 || n_psi <= 0) return fail(GISAPR_ERR_ARGUMENT, "n_particles < 0 or n_psi <= 0");
+  if (n_particles == 0) return GISAPR_OK;
+  if (!bank || !stack || !local_ptr || !local_idx || !out_score || !out_y || !out_x)
+    return fail(GISAPR_ERR_ARGUMENT, "a required pointer is NULL");
+  if (n < 32 || n > 256 || n % 16 != 0)
+    return fail(GISAPR_ERR_UNSUPPORTED, "correlation size must be a multiple of 16 in [32, 256]");
+  if (crop < 2 || crop > 16 || crop % 2 != 0 || crop > n)
+    return fail(GISAPR_ERR_UNSUPPORTED, "crop must be even, 2..16 and <= n");
+  const size_t smem = correlate_smem_bytes(n, n_psi, crop);
+  if (smem > 227 * 1024)
+    return fail(GISAPR_ERR_UNSUPPORTED, "too many psi angles for the shared-memory particle slice");
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  CorrTables t;
+  rc = get_corr_tables(ctx, n, crop, &t);
+  if (rc) return rc;
+  GISAPR_CHECK_CUDA(launch_correlate_plain((cudaStream_t)stream, (const float2*)bank, (const float2*)stack,
+                                           local_ptr, local_idx, n_particles, n_psi, n, crop, t.outer, t.col,
+                                           out_score, out_y, out_x),
+                    "correlate");
+  return GISAPR_OK;
+}
+
+int gisapr_particle_results(void* stream, const int* local_ptr, const float* score, const int* ys,
+                            const int* xs, int n_particles, int n_psi, int* best_entry, int* best_psi,
+                            float* peak, int* peak_y, int* peak_x, float* zscore) {
+  if (n_particles < 0 || n_psi <= 0) return fail(GISAPR_ERR_ARGUMENT, "n_particles < 0 or n_psi <= 0");
+  if (n_particles == 0) return GISAPR_OK;
+  if (!local_ptr || !score || !ys || !xs || !best_entry || !best_psi || !peak || !peak_y || !peak_x ||
+      !zscore)
+    return fail(GISAPR_ERR_ARGUMENT, "a required pointer is NULL");
+  GISAPR_CHECK_CUDA(launch_particle_results((cudaStream_t)stream, local_ptr, score, ys, xs, n_particles, n_psi,
+                                            best_entry, best_psi, peak, peak_y, peak_x, zscore),
+                    "particle_results");
+  return GISAPR_OK;
+}
+
+int gisapr_score_sum(void* stream, const int* local_ptr, const float* peak, int n_particles, double* out) {
+  if (n_particles < 0 || !out) return fail(GISAPR_ERR_ARGUMENT, "bad arguments");
+  if (n_particles > 0 && (!local_ptr || !peak)) return fail(GISAPR_ERR_ARGUMENT, "a required pointer is NULL");
+  GISAPR_CHECK_CUDA(launch_score_sum((cudaStream_t)stream, local_ptr, peak, n_particles, out), "score_sum");
+  return GISAPR_OK;
+}
+
+}  // extern "C"

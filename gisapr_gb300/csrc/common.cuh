@@ -1,0 +1,152 @@
+// Shared device helpers for the GisAPR scoring kernels (sm_103a).
+//
+// Complex numbers are float2 (x = real, y = imaginary) in HBM and shared
+// memory, matching torch.complex64 storage. Twiddle tables are computed on
+// the host in double precision from the definition exp(-2*pi*i*k/L) and
+// rounded once to float; no library trigonometry is reproduced here.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define GISAPR_DEV __device__ __forceinline__
+
+// Largest 1-D transform length any kernel stages in shared memory.
+constexpr int kMaxFftLen = 512;
+
+GISAPR_DEV float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+GISAPR_DEV float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+GISAPR_DEV float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+GISAPR_DEV float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+GISAPR_DEV float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+// a * conj(b) and conj(a) are folded into the twiddle sign by the callers.
+GISAPR_DEV float2 cmul_sign(float2 a, float2 w, float sign) {
+  // multiply by (w.x + i*sign*w.y)
+  float wy = sign * w.y;
+  return make_float2(a.x * w.x - a.y * wy, a.x * wy + a.y * w.x);
+}
+
+GISAPR_DEV int ilog2_pow2(int n) { return 31 - __clz(n); }
+GISAPR_DEV int bitrev(int i, int logn) { return (int)(__brev((unsigned)i) >> (32 - logn)); }
+
+// ---------------------------------------------------------------------------
+// In-place radix-2 decimation-in-time FFT over many lines in shared memory.
+//
+// Line l, element k lives at buf[l * line_stride + k * elem_stride]. The data
+// must already be in bit-reversed order along each line; the result is in
+// natural order. sign = -1 for the forward transform exp(-2 pi i k n / L),
+// +1 for the unnormalised inverse. ``tw`` holds exp(-2 pi i t / kMaxFftLen)
+// for t < kMaxFftLen / 2. All threads of the block must call this.
+// ---------------------------------------------------------------------------
+GISAPR_DEV void smem_fft_dit(float2* buf, int L, int lines, int line_stride, int elem_stride,
+                             float sign, const float2* __restrict__ tw) {
+  const int half_total = L >> 1;
+  const int work = lines * half_total;
+  for (int half = 1; half < L; half <<= 1) {
+    const int twstep = kMaxFftLen / (half << 1);
+    for (int t = threadIdx.x; t < work; t += blockDim.x) {
+      const int line = t / half_total;
+      const int b = t - line * half_total;
+      const int group = b / half;
+      const int k = b - group * half;
+      const int i = group * (half << 1) + k;
+      float2* base = buf + line * line_stride;
+      float2 u = base[i * elem_stride];
+      float2 v = base[(i + half) * elem_stride];
+      float2 w = tw[k * twstep];
+      float2 vt = cmul_sign(v, w, -sign);  // tw is exp(-..): sign=-1 keeps it, +1 conjugates
+      base[i * elem_stride] = cadd(u, vt);
+      base[(i + half) * elem_stride] = csub(u, vt);
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 16-point inverse DFT in registers: X[r] = sum_j x[j] exp(+2 pi i j r / 16),
+// as a radix-4 x radix-4 decomposition (j = 4 j1 + j2, r = r1 + 4 r2).
+// The constants are cos/sin of multiples of pi/8.
+// ---------------------------------------------------------------------------
+GISAPR_DEV void idft4(float2& a, float2& b, float2& c, float2& d) {
+  // X0 = a+b+c+d, X1 = a + i b - c - i d, X2 = a - b + c - d, X3 = a - i b - c + i d
+  float2 s0 = cadd(a, c), s1 = csub(a, c), s2 = cadd(b, d), s3 = csub(b, d);
+  float2 x0 = cadd(s0, s2);
+  float2 x2 = csub(s0, s2);
+  float2 ib = make_float2(-s3.y, s3.x);  // i * (b - d)
+  float2 x1 = cadd(s1, ib);
+  float2 x3 = csub(s1, ib);
+  a = x0; b = x1; c = x2; d = x3;
+}
+
+GISAPR_DEV void idft16(float2 (&x)[16]) {
+  constexpr float C1 = 0.92387953251128675613f;  // cos(pi/8)
+  constexpr float S1 = 0.38268343236508977173f;  // sin(pi/8)
+  constexpr float R2 = 0.70710678118654752440f;  // cos(pi/4)
+  // Step 1: for each j2, a 4-point inverse DFT over j1 (elements j2, j2+4, ...).
+#pragma unroll
+  for (int j2 = 0; j2 < 4; ++j2) idft4(x[j2], x[j2 + 4], x[j2 + 8], x[j2 + 12]);
+  // Now x[j2 + 4*r1] = A[j2][r1]. Twiddle by exp(+2 pi i j2 r1 / 16).
+  // (j2, r1) products 1..9: angles k*pi/8.
+  const float2 w1 = make_float2(C1, S1), w2 = make_float2(R2, R2), w3 = make_float2(S1, C1);
+  const float2 w4 = make_float2(0.f, 1.f), w6 = make_float2(-R2, R2), w9 = make_float2(-C1, -S1);
+  x[1 + 4] = cmul(x[1 + 4], w1);   // j2=1, r1=1
+  x[1 + 8] = cmul(x[1 + 8], w2);   // j2=1, r1=2
+  x[1 + 12] = cmul(x[1 + 12], w3); // j2=1, r1=3
+  x[2 + 4] = cmul(x[2 + 4], w2);   // j2=2, r1=1
+  x[2 + 8] = cmul(x[2 + 8], w4);   // j2=2, r1=2
+  x[2 + 12] = cmul(x[2 + 12], w6); // j2=2, r1=3
+  x[3 + 4] = cmul(x[3 + 4], w3);   // j2=3, r1=1
+  x[3 + 8] = cmul(x[3 + 8], w6);   // j2=3, r1=2
+  x[3 + 12] = cmul(x[3 + 12], w9); // j2=3, r1=3
+  // Step 2: for each r1, a 4-point inverse DFT over j2: X[r1 + 4 r2].
+#pragma unroll
+  for (int r1 = 0; r1 < 4; ++r1)
+    idft4(x[4 * r1 + 0], x[4 * r1 + 1], x[4 * r1 + 2], x[4 * r1 + 3]);
+  // Now x[4*r1 + r2] holds X[r1 + 4*r2]; callers index through idft16_slot().
+}
+
+// Register slot that holds output r of idft16.
+GISAPR_DEV constexpr int idft16_slot(int r) { return 4 * (r & 3) + (r >> 2); }
+
+// ---------------------------------------------------------------------------
+// Reductions
+// ---------------------------------------------------------------------------
+GISAPR_DEV float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+GISAPR_DEV double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Deterministic block sum of one double per thread (fixed tree order).
+// ``scratch`` needs blockDim.x/32 doubles. Result is returned to every thread.
+GISAPR_DEV double block_sum_d(double v, double* scratch) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  v = warp_sum_d(v);
+  __syncthreads();
+  if (lane == 0) scratch[warp] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (warp == 0) {
+    t = lane < nw ? scratch[lane] : 0.0;
+    t = warp_sum_d(t);
+    if (lane == 0) scratch[0] = t;
+  }
+  __syncthreads();
+  t = scratch[0];
+  __syncthreads();
+  return t;
+}
+
+// Status word written by kernels that detect bad input on the device.
+enum GisaprDeviceStatus : int {
+  kDevOk = 0,
+  kDevBadIndex = 1,
+  kDevTooManyLocal = 2,
+};

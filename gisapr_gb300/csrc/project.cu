@@ -1,0 +1,436 @@
+// Central-slice projector and template tail (v606:856-1147) for sm_103a.
+//
+// One CTA builds one template at a time (grid-stride over directions). Every
+// 2-D array of a template lives in an L2-resident scratch area owned by the
+// CTA; each pass stages a batch of rows or columns in shared memory, runs
+// radix-2 FFTs there and writes the batch back. The passes are:
+//
+//   A  slice gather + inverse along rows: trilinear samples of the half
+//      volume (border clamp, conjugate where the rotated x < 0) feed two
+//      N-point inverse FFTs per column (even/odd rows of the 2N grid); the
+//      pair combines into exactly the N centred output rows of the 2N-point
+//      inverse that the crop keeps (v606:1099-1130).
+//   B  C2R along columns (2N-point real output from N+1 coefficients, via an
+//      N-point complex inverse), keep the N centred columns, scale 1/(2N)^2;
+//      then the forward row FFT that starts the whitening.
+//   C  forward column FFT; radial |F| sums per bin (deterministic warp
+//      reductions over a host-built bin list).
+//   D  divide by the radial mean amplitude (DC bin untouched), inverse
+//      column FFT.
+//   E  inverse row transform (real part), plane-fit sums in FP64.
+//   F  plane removal, mean/population-sigma normalisation, soft mask,
+//      forward row FFT.
+//   G  forward column FFT, Fourier crop and packing, FSC weight, L2 norm
+//      over the packed half plane, pre-shift (fftshift both dims) into the
+//      template bank (v606:1132-1147, 531-537).
+//
+// The slice coordinates repeat the reference's float32 operations, including
+// the rounding of R00*x + R01*y without fused multiply-add: points where that
+// sum cancels sit on the conjugation boundary (v606:881-885), and any other
+// rounding there picks the mirrored sample.
+#include "common.cuh"
+
+namespace {
+
+struct ProjParams {
+  const float2* spectrum;   // cuFFT R2C output [2N][2N][N+1], unshifted
+  const float* rot;         // [n_dir][9] float32 rotation matrices (stored transposed)
+  const int* dirs;          // directions to build (indices into rot), n_build
+  int n_build;
+  const float* mask;        // [N][N] or null
+  const float* fsc;         // [nb][H] packed FSC
+  const int* bin_list;      // [N*(N/2+1)] half-plane indices sorted by radial bin
+  const int* bin_ptr;       // [n_bins+1]
+  const float* bin_count;   // [n_bins] full-grid counts per bin
+  int n_bins;
+  const float2* tw;         // twiddles exp(-2 pi i t / kMaxFftLen)
+  float2* bank;             // [n_dir_out][nb][H] output templates
+  const int* out_slot;      // output row in bank for each build index (null => dirs[i])
+  float2* scratch;          // per-CTA scratch
+  size_t scratch_stride;    // complex elements per CTA
+  int N;
+  int nb;
+};
+
+constexpr int kThreads = 256;
+constexpr int kLineCols = 8;   // columns per batch in pass A
+constexpr int kRowBatch = 8;   // rows per batch in passes B/E/F
+constexpr int kColBatch = 16;  // columns per batch in passes C/D/G
+
+__device__ __forceinline__ float2 tw_pos(const float2* tw, int num, int den) {
+  // exp(+2 pi i num/den) for |num| <= den/2, from the exp(-...) table.
+  int t = abs(num) * (kMaxFftLen / den);
+  float2 w = tw[t];
+  return num >= 0 ? make_float2(w.x, -w.y) : w;
+}
+
+// Trilinear sample of the half volume at clamped voxel coordinates, in the
+// corner and weight order of grid_sample's 3-D kernel.
+__device__ __forceinline__ float2 sample_trilinear(const float2* __restrict__ vol, int m, int w,
+                                                   float iz, float iy, float ix) {
+  const float fz = floorf(iz), fy = floorf(iy), fx = floorf(ix);
+  const int z0 = (int)fz, y0 = (int)fy, x0 = (int)fx;
+  const float wz1 = __fsub_rn(iz, fz), wy1 = __fsub_rn(iy, fy), wx1 = __fsub_rn(ix, fx);
+  const float wz0 = __fsub_rn(fz + 1.0f, iz), wy0 = __fsub_rn(fy + 1.0f, iy), wx0 = __fsub_rn(fx + 1.0f, ix);
+  float2 acc = make_float2(0.f, 0.f);
+  // Half-volume storage is unshifted along z and y: stored index = (i + N) mod 2N.
+  const int half = m / 2;
+#pragma unroll
+  for (int dz = 0; dz < 2; ++dz) {
+    const int zz = z0 + dz;
+    if (zz >= m) continue;
+    const float wz = dz ? wz1 : wz0;
+    const int zs = (zz + half) % m;
+#pragma unroll
+    for (int dy = 0; dy < 2; ++dy) {
+      const int yy = y0 + dy;
+      if (yy >= m) continue;
+      const float wy = dy ? wy1 : wy0;
+      const int ys = (yy + half) % m;
+      const float2* row = vol + ((size_t)zs * m + ys) * w;
+#pragma unroll
+      for (int dx = 0; dx < 2; ++dx) {
+        const int xx = x0 + dx;
+        if (xx >= w) continue;
+        const float wx = dx ? wx1 : wx0;
+        const float wt = __fmul_rn(__fmul_rn(wx, wy), wz);
+        const float2 v = __ldg(row + xx);
+        acc.x = __fadd_rn(acc.x, __fmul_rn(v.x, wt));
+        acc.y = __fadd_rn(acc.y, __fmul_rn(v.y, wt));
+      }
+    }
+  }
+  return acc;
+}
+
+// Coordinate of a slice point along one axis, through grid_sample's
+// normalise (align_corners=True) and un-normalise, clamped for border mode.
+__device__ __forceinline__ float grid_pixel(float c, int size) {
+  const float denom = __fsub_rn(__fmul_rn(0.5f, (float)size), 0.5f);
+  const float nrm = __fsub_rn(__fdiv_rn(c, denom), 1.0f);
+  float pix = __fmul_rn(__fdiv_rn(__fadd_rn(nrm, 1.0f), 2.0f), (float)(size - 1));
+  pix = fminf((float)(size - 1), fmaxf(pix, 0.0f));
+  return pix;
+}
+
+__device__ void build_one(const ProjParams& P, int dir, int slot, float2* S, float2* Pk,
+                          float2* sm, double* red, float* s_div, double* s_coef) {
+  const int N = P.N, m = 2 * N, W = N + 1, nb = P.nb, H = nb / 2 + 1;
+  const int logN = ilog2_pow2(N);
+  const int LDS = N + 1;  // scratch row stride (complex)
+  const float* R = P.rot + (size_t)dir * 9;
+  const float R00 = R[0], R01 = R[1], R10 = R[3], R11 = R[4], R20 = R[6], R21 = R[7];
+  const float inv_m = (float)(1.0 / (double)m);
+
+  // ---- pass A: gather + row inverse (pruned to the N centred rows)
+  for (int c0 = 0; c0 < W; c0 += kLineCols) {
+    const int nc = min(kLineCols, W - c0);
+    const int total = nc * m;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+      const int cl = t / m, r = t - cl * m;  // r: standard-order row of the 2N grid
+      const int c = c0 + cl;
+      const int kys = (r + N) % m;            // row in the shifted base grid
+      const float gy = __fmul_rn((float)(kys - N), inv_m);
+      const float gx = __fmul_rn((float)c, inv_m);
+      float rx = __fadd_rn(__fmul_rn(R00, gx), __fmul_rn(R01, gy));
+      float ry = __fadd_rn(__fmul_rn(R10, gx), __fmul_rn(R11, gy));
+      float rz = __fadd_rn(__fmul_rn(R20, gx), __fmul_rn(R21, gy));
+      const bool conj = rx < 0.0f;
+      if (conj) { rx = -rx; ry = -ry; rz = -rz; }
+      const float cz = __fadd_rn(__fmul_rn(rz, (float)m), (float)(m / 2));
+      const float cy = __fadd_rn(__fmul_rn(ry, (float)m), (float)(m / 2));
+      const float cx = __fmul_rn(rx, (float)m);
+      float2 v = sample_trilinear(P.spectrum, m, W, grid_pixel(cz, m), grid_pixel(cy, m),
+                                  grid_pixel(cx, W));
+      if (conj) v.y = -v.y;
+      const int e = r & 1, q = r >> 1;
+      sm[(cl * 2 + e) * N + bitrev(q, logN)] = v;
+    }
+    __syncthreads();
+    smem_fft_dit(sm, N, 2 * nc, N, 1, +1.0f, P.tw);
+    for (int t = threadIdx.x; t < nc * N; t += blockDim.x) {
+      const int cl = t / N, i = t - cl * N;
+      const int u = i - N / 2;               // signed output row of the 2N-point inverse
+      const int k = (u + N) % N;
+      const float2 a0 = sm[(cl * 2) * N + k];
+      const float2 a1 = sm[(cl * 2 + 1) * N + k];
+      const float2 z = cadd(a0, cmul(tw_pos(P.tw, u, m), a1));
+      S[(size_t)i * LDS + c0 + cl] = z;
+    }
+    __syncthreads();
+  }
+
+  // ---- pass B: C2R along columns, keep centred N, then forward row FFT
+  const float scale_b = (float)(1.0 / ((double)m * (double)m));
+  float2* sm2 = sm + kRowBatch * N;
+  for (int i0 = 0; i0 < N; i0 += kRowBatch) {
+    const int nr = min(kRowBatch, N - i0);
+    for (int t = threadIdx.x; t < nr * N; t += blockDim.x) {
+      const int rl = t / N, k = t - rl * N;
+      const float2* Z = S + (size_t)(i0 + rl) * LDS;
+      float2 ye, yo;
+      if (k == 0) {
+        const float a = Z[0].x, b = Z[N].x;
+        ye = make_float2(a + b, 0.f);
+        yo = make_float2(a - b, 0.f);
+      } else {
+        const float2 zk = Z[k], zc = cconj(Z[N - k]);
+        ye = cadd(zk, zc);
+        yo = cmul(csub(zk, zc), tw_pos(P.tw, k, m));
+      }
+      // W = Ye + i*Yo
+      sm[rl * N + bitrev(k, logN)] = make_float2(ye.x - yo.y, ye.y + yo.x);
+    }
+    __syncthreads();
+    smem_fft_dit(sm, N, nr, N, 1, +1.0f, P.tw);
+    // p(2n) = Re z(n), p(2n+1) = Im z(n); keep v = (j - N/2) mod 2N.
+    for (int t = threadIdx.x; t < nr * N; t += blockDim.x) {
+      const int rl = t / N, j = t - rl * N;
+      const int v = (j - N / 2 + m) % m;
+      const float2 zz = sm[rl * N + (v >> 1)];
+      const float p = ((v & 1) ? zz.y : zz.x) * scale_b;
+      sm2[rl * N + bitrev(j, logN)] = make_float2(p, 0.f);
+    }
+    __syncthreads();
+    smem_fft_dit(sm2, N, nr, N, 1, -1.0f, P.tw);
+    for (int t = threadIdx.x; t < nr * (N / 2 + 1); t += blockDim.x) {
+      const int rl = t / (N / 2 + 1), k = t - rl * (N / 2 + 1);
+      S[(size_t)(i0 + rl) * LDS + k] = sm2[rl * N + k];
+    }
+    __syncthreads();
+  }
+
+  // ---- pass C: forward column FFT (kx in [0, N/2])
+  const int HC = N / 2 + 1;
+  for (int c0 = 0; c0 < HC; c0 += kColBatch) {
+    const int nc = min(kColBatch, HC - c0);
+    for (int t = threadIdx.x; t < nc * N; t += blockDim.x) {
+      const int r = t / nc, cl = t - r * nc;
+      sm[cl * N + bitrev(r, logN)] = S[(size_t)r * LDS + c0 + cl];
+    }
+    __syncthreads();
+    smem_fft_dit(sm, N, nc, N, 1, -1.0f, P.tw);
+    for (int t = threadIdx.x; t < nc * N; t += blockDim.x) {
+      const int r = t / nc, cl = t - r * nc;
+      S[(size_t)r * LDS + c0 + cl] = sm[cl * N + r];
+    }
+    __syncthreads();
+  }
+  // radial sums of |F| over the full grid: columns 1..N/2-1 stand for two bins
+  {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int b = warp; b < P.n_bins; b += nw) {
+      double acc = 0.0;
+      for (int e = P.bin_ptr[b] + lane; e < P.bin_ptr[b + 1]; e += 32) {
+        const int idx = P.bin_list[e];
+        const int r = idx / HC, kx = idx - r * HC;
+        const float2 f = S[(size_t)r * LDS + kx];
+        const double a = (double)hypotf(f.x, f.y);
+        acc += (kx == 0 || kx == N / 2) ? a : 2.0 * a;
+      }
+      acc = warp_sum_d(acc);
+      if (lane == 0) s_div[b] = (b == 0) ? 1.0f : (float)((double)P.bin_count[b] / acc);
+    }
+  }
+  __syncthreads();
+
+  // ---- pass D: scale by the radial divisor, inverse column FFT
+  for (int c0 = 0; c0 < HC; c0 += kColBatch) {
+    const int nc = min(kColBatch, HC - c0);
+    for (int t = threadIdx.x; t < nc * N; t += blockDim.x) {
+      const int r = t / nc, cl = t - r * nc;
+      const int kx = c0 + cl;
+      const int ky = r < N / 2 ? r : r - N;
+      const int bin = (int)rintf(sqrtf((float)(ky * ky + kx * kx)));
+      sm[cl * N + bitrev(r, logN)] = cscale(S[(size_t)r * LDS + kx], s_div[bin]);
+    }
+    __syncthreads();
+    smem_fft_dit(sm, N, nc, N, 1, +1.0f, P.tw);
+    for (int t = threadIdx.x; t < nc * N; t += blockDim.x) {
+      const int r = t / nc, cl = t - r * nc;
+      S[(size_t)r * LDS + c0 + cl] = sm[cl * N + r];
+    }
+    __syncthreads();
+  }
+
+  // ---- pass E: inverse row transform (real part), plane-fit sums
+  const float scale_e = (float)(1.0 / ((double)N * (double)N));
+  double sz = 0.0, sxz = 0.0, syz = 0.0;
+  for (int i0 = 0; i0 < N; i0 += kRowBatch) {
+    const int nr = min(kRowBatch, N - i0);
+    for (int t = threadIdx.x; t < nr * N; t += blockDim.x) {
+      const int rl = t / N, k = t - rl * N;
+      const float2* G = S + (size_t)(i0 + rl) * LDS;
+      float2 y;
+      if (k == 0 || k == N / 2) y = make_float2(G[k].x, 0.f);
+      else if (k < N / 2) y = G[k];
+      else y = cconj(G[N - k]);
+      sm[rl * N + bitrev(k, logN)] = y;
+    }
+    __syncthreads();
+    smem_fft_dit(sm, N, nr, N, 1, +1.0f, P.tw);
+    for (int t = threadIdx.x; t < nr * N; t += blockDim.x) {
+      const int rl = t / N, j = t - rl * N;
+      const int i = i0 + rl;
+      const float w = sm[rl * N + j].x * scale_e;
+      S[(size_t)i * LDS + j] = make_float2(w, 0.f);
+      sz += (double)w;
+      sxz += (double)i * (double)w;
+      syz += (double)j * (double)w;
+    }
+    __syncthreads();
+  }
+  sz = block_sum_d(sz, red);
+  sxz = block_sum_d(sxz, red);
+  syz = block_sum_d(syz, red);
+  if (threadIdx.x == 0) {
+    // Normal equations of z = c0*row + c1*col + c2 over the N x N grid.
+    const double n = (double)N, n2 = n * n;
+    const double s1 = n * (n - 1.0) / 2.0 * n;           // sum of row (or col) indices
+    const double s2 = (n - 1.0) * n * (2.0 * n - 1.0) / 6.0 * n;  // sum of squares
+    const double sxy = (n * (n - 1.0) / 2.0) * (n * (n - 1.0) / 2.0);
+    double A[3][4] = {{s2, sxy, s1, sxz}, {sxy, s2, s1, syz}, {s1, s1, n2, sz}};
+    for (int c = 0; c < 3; ++c) {  // Gauss-Jordan with partial pivoting
+      int p = c;
+      for (int r2 = c + 1; r2 < 3; ++r2) if (fabs(A[r2][c]) > fabs(A[p][c])) p = r2;
+      if (p != c) for (int k = 0; k < 4; ++k) { double tmp = A[c][k]; A[c][k] = A[p][k]; A[p][k] = tmp; }
+      for (int r2 = 0; r2 < 3; ++r2) {
+        if (r2 == c) continue;
+        const double f = A[r2][c] / A[c][c];
+        for (int k = c; k < 4; ++k) A[r2][k] -= f * A[c][k];
+      }
+    }
+    const double c0 = A[0][3] / A[0][0], c1 = A[1][3] / A[1][1], c2 = A[2][3] / A[2][2];
+    s_coef[0] = c0; s_coef[1] = c1; s_coef[2] = c2;
+    s_coef[3] = (sz - c0 * s1 - c1 * s1 - c2 * n2) / n2;  // mean after plane removal
+  }
+  __syncthreads();
+  const double pc0 = s_coef[0], pc1 = s_coef[1], pc2 = s_coef[2], mean = s_coef[3];
+  // ---- pass F1: population variance after plane removal
+  double sv = 0.0;
+  for (int t = threadIdx.x; t < N * N; t += blockDim.x) {
+    const int i = t / N, j = t - i * N;
+    const double v = (double)S[(size_t)i * LDS + j].x - (pc0 * i + pc1 * j + pc2) - mean;
+    sv += v * v;
+  }
+  sv = block_sum_d(sv, red);
+  const double sd = sqrt(sv / ((double)N * (double)N));
+  const double inv_sd = sd > 1e-12 ? 1.0 / sd : 1.0;
+
+  // ---- pass F2: normalise, mask, forward row FFT
+  for (int i0 = 0; i0 < N; i0 += kRowBatch) {
+    const int nr = min(kRowBatch, N - i0);
+    for (int t = threadIdx.x; t < nr * N; t += blockDim.x) {
+      const int rl = t / N, j = t - rl * N;
+      const int i = i0 + rl;
+      double v = ((double)S[(size_t)i * LDS + j].x - (pc0 * i + pc1 * j + pc2) - mean) * inv_sd;
+      float f = (float)v;
+      if (P.mask != nullptr) f *= P.mask[(size_t)i * N + j];
+      sm[rl * N + bitrev(j, logN)] = make_float2(f, 0.f);
+    }
+    __syncthreads();
+    smem_fft_dit(sm, N, nr, N, 1, -1.0f, P.tw);
+    for (int t = threadIdx.x; t < nr * HC; t += blockDim.x) {
+      const int rl = t / HC, k = t - rl * HC;
+      S[(size_t)(i0 + rl) * LDS + k] = sm[rl * N + k];
+    }
+    __syncthreads();
+  }
+  // ---- pass G: forward column FFT
+  for (int c0 = 0; c0 < HC; c0 += kColBatch) {
+    const int nc = min(kColBatch, HC - c0);
+    for (int t = threadIdx.x; t < nc * N; t += blockDim.x) {
+      const int r = t / nc, cl = t - r * nc;
+      sm[cl * N + bitrev(r, logN)] = S[(size_t)r * LDS + c0 + cl];
+    }
+    __syncthreads();
+    smem_fft_dit(sm, N, nc, N, 1, -1.0f, P.tw);
+    for (int t = threadIdx.x; t < nc * N; t += blockDim.x) {
+      const int r = t / nc, cl = t - r * nc;
+      S[(size_t)r * LDS + c0 + cl] = sm[cl * N + r];
+    }
+    __syncthreads();
+  }
+  // crop + pack + FSC, L2 norm
+  double ss = 0.0;
+  for (int t = threadIdx.x; t < nb * H; t += blockDim.x) {
+    const int r = t / H, c = t - r * H;
+    const int ky = r < nb / 2 ? r : r - nb;
+    float2 f;
+    if (c < nb / 2) {
+      f = S[(size_t)((ky + N) % N) * LDS + c];
+    } else if (nb == N) {
+      f = S[(size_t)((ky + N) % N) * LDS + N / 2];
+    } else {
+      f = cconj(S[(size_t)((-ky + N) % N) * LDS + nb / 2]);
+    }
+    f = cscale(f, P.fsc[t]);
+    Pk[t] = f;
+    ss += (double)f.x * f.x + (double)f.y * f.y;
+  }
+  ss = block_sum_d(ss, red);
+  const float inv_norm = (float)(1.0 / sqrt(ss));
+  float2* out = P.bank + (size_t)slot * nb * H;
+  for (int t = threadIdx.x; t < nb * H; t += blockDim.x) {
+    const int r = t / H, c = t - r * H;
+    const int rs = (r + nb / 2) % nb, cs = (c + H / 2) % H;
+    out[(size_t)rs * H + cs] = cscale(Pk[t], inv_norm);
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kThreads) project_templates(ProjParams P) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* sm = reinterpret_cast<float2*>(smem_raw);
+  const int N = P.N;
+  const int line_elems = max(2 * kLineCols * N, 2 * kRowBatch * N);
+  const int lines = max(line_elems, kColBatch * N);
+  float2* s_tw = sm + lines;
+  double* red = reinterpret_cast<double*>(s_tw + kMaxFftLen / 2);
+  double* s_coef = red + 32;
+  float* s_div = reinterpret_cast<float*>(s_coef + 8);
+  for (int t = threadIdx.x; t < kMaxFftLen / 2; t += blockDim.x) s_tw[t] = P.tw[t];
+  __syncthreads();
+  ProjParams Q = P;
+  Q.tw = s_tw;
+  float2* S = P.scratch + (size_t)blockIdx.x * P.scratch_stride;
+  float2* Pk = S + (size_t)N * (N + 1);
+  for (int b = blockIdx.x; b < P.n_build; b += gridDim.x) {
+    const int dir = P.dirs[b];
+    const int slot = P.out_slot ? P.out_slot[b] : dir;
+    build_one(Q, dir, slot, S, Pk, sm, red, s_div, s_coef);
+  }
+}
+
+}  // namespace
+
+size_t project_scratch_elems(int N, int nb) {
+  return (size_t)N * (N + 1) + (size_t)nb * (nb / 2 + 1);
+}
+
+size_t project_smem_bytes(int N, int n_bins) {
+  const int line_elems = max(2 * kLineCols * N, 2 * kRowBatch * N);
+  const int lines = max(line_elems, kColBatch * N);
+  return (size_t)lines * sizeof(float2) + (kMaxFftLen / 2) * sizeof(float2) + 40 * sizeof(double) +
+         (size_t)(n_bins + 4) * sizeof(float);
+}
+
+cudaError_t launch_project_templates(cudaStream_t st, const float2* spectrum, const float* rot,
+                                     const int* dirs, int n_build, const int* out_slot,
+                                     const float* mask, const float* fsc, const int* bin_list,
+                                     const int* bin_ptr, const float* bin_count, int n_bins,
+                                     const float2* tw, float2* bank, float2* scratch, int grid,
+                                     int N, int nb) {
+  if (n_build <= 0) return cudaSuccess;
+  ProjParams P;
+  P.spectrum = spectrum; P.rot = rot; P.dirs = dirs; P.n_build = n_build; P.mask = mask;
+  P.fsc = fsc; P.bin_list = bin_list; P.bin_ptr = bin_ptr; P.bin_count = bin_count;
+  P.n_bins = n_bins; P.tw = tw; P.bank = bank; P.out_slot = out_slot; P.scratch = scratch;
+  P.scratch_stride = project_scratch_elems(N, nb); P.N = N; P.nb = nb;
+  const size_t smem = project_smem_bytes(N, n_bins);
+  cudaError_t e = cudaFuncSetAttribute(project_templates, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  project_templates<<<grid, kThreads, smem, st>>>(P);
+  return cudaGetLastError();
+}

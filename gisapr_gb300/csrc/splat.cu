@@ -1,0 +1,298 @@
+// Gaussian atom splat (pdb2mrc density) for sm_103a.
+//
+// Two launches:
+//   1. atoms_prepare: one thread per atom. Optional rigid-body pose in FP64
+//      ((c - pivot) @ R + pivot + t), the PDB 8.3 write/reread, the voxel
+//      position f32(f64(q)/apix + box/2) and the clipped integer bounds
+//      (pdb_text.py:123-142, ZL pdb_text.py:33-58, pdb2mrc_gpu_ver_fp32_v3.py:
+//      71-87).
+//   2. splat_bricks: one CTA per 16^3 brick of the box. Each thread owns one
+//      (x, y) column of 16 voxels in registers and walks the atoms in input
+//      order, so every voxel sums its contributions in the reference's atom
+//      order with no atomics: the result is deterministic, and a cached
+//      fixed-context brick is read once and written once (no clone pass).
+//      The epilogue optionally writes the sinc^2-weighted value into the
+//      zero-padded, fftshifted (2N)^3 input of the volume FFT (v606:837-853,
+//      1063-1072), so the padded volume is never materialised separately.
+//
+// Per voxel the arithmetic follows the reference's float32/float64 mix
+// (pdb2mrc:88-95): r = sqrtf((dx*dx + dy*dy) + dz*dz) with every product and
+// sum rounded to float; exponent = f32(-r * rp) and value = f32(Z*kn *
+// expf(exponent)) where rp and Z*kn are doubles. The float64 products are
+// formed in float32 pairs (hi + lo) with an exact product error term, which
+// gives the same float result as the double product except at exact ties.
+#include "common.cuh"
+
+namespace {
+
+constexpr int kBrick = 16;
+
+struct AtomRec {
+  float px, py, pz;   // voxel-space position (float32)
+  int lx, ly, lz;     // clipped lower bounds (inclusive)
+  int ux, uy, uz;     // clipped upper bounds (exclusive)
+  float zk_hi, zk_lo; // Z*kn as a float pair (0 => atom skipped)
+  int pad;
+};
+static_assert(sizeof(AtomRec) == 48, "AtomRec layout");
+
+__device__ __forceinline__ int round_away_f64(double v) {
+  double a = floor(fabs(v) + 0.5);
+  return (int)(v < 0.0 ? -a : a);
+}
+
+// Round v*1000 to the nearest integer, ties to even, using the exact
+// product v*1000 = hi + lo (fma residual). This is what Python's "%8.3f"
+// does with the exact binary value of v.
+__device__ __forceinline__ double pdb_8_3(double v) {
+  double hi = v * 1000.0;
+  double lo = fma(v, 1000.0, -hi);
+  double f = floor(hi);
+  double d = (hi - f) - 0.5;  // exact for |hi| < 2^52
+  d += lo;
+  double r;
+  if (d > 0.0) r = f + 1.0;
+  else if (d < 0.0) r = f;
+  else r = (fmod(f, 2.0) == 0.0) ? f : f + 1.0;
+  // hi may itself sit on an integer with lo carrying the sign of the error.
+  if (hi == f && lo < 0.0) {
+    // exact value slightly below the integer hi: nearest is still hi unless
+    // the distance reaches a half (impossible for |lo| < 0.5).
+    r = f;
+  }
+  return r / 1000.0;
+}
+
+__global__ void atoms_prepare(const float* __restrict__ xyz, const float* __restrict__ numbers,
+                              int n, int transform, const float* __restrict__ pivot,
+                              const double* __restrict__ rot, const double* __restrict__ shift,
+                              int box, int width, double apix, double kn,
+                              AtomRec* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float c[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
+  float q[3];
+  if (transform) {
+    // (c - pivot) is float32, as numpy evaluates float32 arrays; the matrix
+    // product and the additions are float64 (pdb_text.py:141).
+    double d[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) d[k] = (double)__fsub_rn(c[k], pivot[k]);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      double m = d[0] * rot[0 * 3 + k];
+      m = fma(d[1], rot[1 * 3 + k], m);
+      m = fma(d[2], rot[2 * 3 + k], m);
+      double v = m + (double)pivot[k] + shift[k];
+      q[k] = (float)pdb_8_3(v);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) q[k] = c[k];
+  }
+  AtomRec r;
+  float p[3];
+  int lo[3], hi[3];
+  bool inside = true;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    p[k] = (float)((double)q[k] / apix + (double)(box / 2));
+    lo[k] = round_away_f64((double)__fsub_rn(p[k], (float)width));
+    hi[k] = round_away_f64((double)__fadd_rn(p[k], (float)width));
+    inside = inside && (lo[k] < box) && (hi[k] >= 0);
+    lo[k] = max(lo[k], 0);
+    hi[k] = min(hi[k], box - 1);
+  }
+  const float z = numbers[i];
+  double zk = (double)z * kn;
+  float zk_hi = (float)zk;
+  float zk_lo = (float)(zk - (double)zk_hi);
+  if (!inside || z == 0.0f || !(isfinite(p[0]) && isfinite(p[1]) && isfinite(p[2]))) {
+    zk_hi = 0.0f;
+    zk_lo = 0.0f;
+  }
+  r.px = p[0]; r.py = p[1]; r.pz = p[2];
+  r.lx = lo[0]; r.ly = lo[1]; r.lz = lo[2];
+  r.ux = hi[0]; r.uy = hi[1]; r.uz = hi[2];
+  r.zk_hi = zk_hi; r.zk_lo = zk_lo; r.pad = 0;
+  out[i] = r;
+}
+
+// float32 sinc(r)^2 in the operation order of the reference filter
+// (v606:841-853 with torch.sinc: sin(pi*r)/(pi*r), 1 at r == 0).
+__device__ __forceinline__ float sinc2_f32(float fz2, float fy2, float fx2) {
+  float r = sqrtf(__fadd_rn(__fadd_rn(fz2, fy2), fx2));
+  float s;
+  if (r == 0.0f) {
+    s = 1.0f;
+  } else {
+    float prod = __fmul_rn(3.14159274101257324219f, r);
+    s = __fdiv_rn(sinf(prod), prod);
+  }
+  return __fmul_rn(s, s);
+}
+
+__device__ __forceinline__ float fftfreq_shifted_f32(int i, int m) {
+  // fftshift(fftfreq(m))[i] = (i - m/2) * float(1/m)
+  return __fmul_rn((float)(i - m / 2), (float)(1.0 / (double)m));
+}
+
+__global__ void __launch_bounds__(256)
+splat_bricks(const AtomRec* __restrict__ atoms, int n_atoms, const float* __restrict__ initial,
+             float* __restrict__ out, float* __restrict__ padded, int box, float rp_hi,
+             float rp_lo) {
+  __shared__ AtomRec s_atoms[256];
+  __shared__ int s_list[256];
+  __shared__ int s_count;
+  const int nbx = (box + kBrick - 1) / kBrick;
+  const int bz = blockIdx.x / (nbx * nbx);
+  const int by = (blockIdx.x / nbx) % nbx;
+  const int bx = blockIdx.x % nbx;
+  const int x = bx * kBrick + (threadIdx.x & 15);
+  const int y = by * kBrick + (threadIdx.x >> 4);
+  const int z0 = bz * kBrick;
+  const bool col_ok = (x < box) && (y < box);
+  const size_t plane = (size_t)box * box;
+
+  float acc[kBrick];
+#pragma unroll
+  for (int k = 0; k < kBrick; ++k) {
+    const int z = z0 + k;
+    acc[k] = (initial != nullptr && col_ok && z < box) ? initial[(size_t)z * plane + (size_t)y * box + x]
+                                                       : 0.0f;
+  }
+  const int bx0 = bx * kBrick, by0 = by * kBrick;
+  const float fx = (float)x, fy = (float)y;
+  for (int base = 0; base < n_atoms; base += 256) {
+    const int ai = base + threadIdx.x;
+    __syncthreads();
+    if (threadIdx.x == 0) s_count = 0;
+    bool hit = false;
+    AtomRec r;
+    if (ai < n_atoms) {
+      r = atoms[ai];
+      hit = (r.zk_hi != 0.0f || r.zk_lo != 0.0f) && r.ux > bx0 && r.lx < bx0 + kBrick &&
+            r.uy > by0 && r.ly < by0 + kBrick && r.uz > z0 && r.lz < z0 + kBrick;
+    }
+    // Order-preserving compaction of the atoms that touch this brick.
+    const unsigned mask = __ballot_sync(0xffffffffu, hit);
+    __syncthreads();
+    __shared__ int s_warp_base[8];
+    if ((threadIdx.x & 31) == 0) s_warp_base[threadIdx.x >> 5] = __popc(mask);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int run = 0;
+      for (int w = 0; w < 8; ++w) {
+        int c = s_warp_base[w];
+        s_warp_base[w] = run;
+        run += c;
+      }
+      s_count = run;
+    }
+    __syncthreads();
+    if (hit) {
+      const int pos = s_warp_base[threadIdx.x >> 5] + __popc(mask & ((1u << (threadIdx.x & 31)) - 1u));
+      s_atoms[pos] = r;
+      s_list[pos] = ai;
+    }
+    __syncthreads();
+    const int cnt = s_count;
+    for (int t = 0; t < cnt; ++t) {
+      const AtomRec a = s_atoms[t];
+      if (!col_ok || x < a.lx || x >= a.ux || y < a.ly || y >= a.uy) continue;
+      const float dx = __fsub_rn(fx, a.px), dy = __fsub_rn(fy, a.py);
+      const float sxy = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+#pragma unroll
+      for (int k = 0; k < kBrick; ++k) {
+        const int z = z0 + k;
+        if (z >= a.lz && z < a.uz) {
+          const float dz = __fsub_rn((float)z, a.pz);
+          const float rr = sqrtf(__fadd_rn(sxy, __fmul_rn(dz, dz)));
+          // f32(r * rp) with rp = rp_hi + rp_lo
+          const float ph = __fmul_rn(rr, rp_hi);
+          const float pe = __fmaf_rn(rr, rp_hi, -ph);
+          const float expo = -__fadd_rn(ph, __fmaf_rn(rr, rp_lo, pe));
+          const float e = expf(expo);
+          // f32(zk * e) with zk = zk_hi + zk_lo
+          const float vh = __fmul_rn(a.zk_hi, e);
+          const float ve = __fmaf_rn(a.zk_hi, e, -vh);
+          const float v = __fadd_rn(vh, __fmaf_rn(a.zk_lo, e, ve));
+          acc[k] = __fadd_rn(acc[k], v);
+        }
+      }
+    }
+  }
+  (void)s_list;
+  if (!col_ok) return;
+  const int m = 2 * box;
+  const int half = box / 2;
+  const float fyv = fftfreq_shifted_f32(y + half, m);
+  const float fxv = fftfreq_shifted_f32(x + half, m);
+  const float fy2 = __fmul_rn(fyv, fyv), fx2 = __fmul_rn(fxv, fxv);
+  const size_t mm = (size_t)m * m;
+  const int ys = (y + 3 * half) % m, xs = (x + 3 * half) % m;
+#pragma unroll
+  for (int k = 0; k < kBrick; ++k) {
+    const int z = z0 + k;
+    if (z >= box) break;
+    if (out != nullptr) out[(size_t)z * plane + (size_t)y * box + x] = acc[k];
+    if (padded != nullptr) {
+      const float fzv = fftfreq_shifted_f32(z + half, m);
+      const float w = sinc2_f32(__fmul_rn(fzv, fzv), fy2, fx2);
+      const int zs = (z + 3 * half) % m;
+      padded[(size_t)zs * mm + (size_t)ys * m + xs] = __fmul_rn(acc[k], w);
+    }
+  }
+}
+
+}  // namespace
+
+// Host-side launchers (called from abi.cu).
+cudaError_t launch_atoms_prepare(cudaStream_t st, const float* xyz, const float* numbers, int n,
+                                 int transform, const float* pivot, const double* rot,
+                                 const double* shift, int box, int width, double apix, double kn,
+                                 void* atom_recs) {
+  if (n <= 0) return cudaSuccess;
+  atoms_prepare<<<(n + 255) / 256, 256, 0, st>>>(xyz, numbers, n, transform, pivot, rot, shift, box,
+                                                  width, apix, kn, (AtomRec*)atom_recs);
+  return cudaGetLastError();
+}
+
+size_t atom_record_bytes() { return sizeof(AtomRec); }
+
+cudaError_t launch_splat_bricks(cudaStream_t st, const void* atom_recs, int n, const float* initial,
+                                float* out, float* padded, int box, double rp) {
+  const int nb = (box + kBrick - 1) / kBrick;
+  const float rp_hi = (float)rp;
+  const float rp_lo = (float)(rp - (double)rp_hi);
+  splat_bricks<<<nb * nb * nb, 256, 0, st>>>((const AtomRec*)atom_recs, n, initial, out, padded, box,
+                                             rp_hi, rp_lo);
+  return cudaGetLastError();
+}
+
+namespace {
+// Standalone sinc^2 / pad / fftshift of an existing box^3 density into the
+// (2*box)^3 FFT input (the splat epilogue does the same for fresh densities).
+__global__ void pad_sinc_shift(const float* __restrict__ vol, float* __restrict__ padded, int box) {
+  const size_t total = (size_t)box * box * box;
+  const int m = 2 * box, half = box / 2;
+  const size_t mm = (size_t)m * m;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const int x = (int)(t % box), y = (int)((t / box) % box), z = (int)(t / ((size_t)box * box));
+    const float fz = fftfreq_shifted_f32(z + half, m), fy = fftfreq_shifted_f32(y + half, m),
+                fx = fftfreq_shifted_f32(x + half, m);
+    const float w = sinc2_f32(__fmul_rn(fz, fz), __fmul_rn(fy, fy), __fmul_rn(fx, fx));
+    const int zs = (z + 3 * half) % m, ys = (y + 3 * half) % m, xs = (x + 3 * half) % m;
+    padded[(size_t)zs * mm + (size_t)ys * m + xs] = __fmul_rn(vol[t], w);
+  }
+}
+}  // namespace
+
+cudaError_t launch_pad_sinc_shift(cudaStream_t st, const float* vol, float* padded, int box) {
+  const size_t total = (size_t)box * box * box;
+  int grid = (int)((total + 255) / 256);
+  if (grid > 152 * 32) grid = 152 * 32;
+  pad_sinc_shift<<<grid, 256, 0, st>>>(vol, padded, box);
+  return cudaGetLastError();
+}

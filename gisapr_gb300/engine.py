@@ -1,0 +1,229 @@
+"""Job-resident candidate scoring on one GPU.
+
+A ScoringJob holds everything that does not depend on the candidate pose on
+the device: the particle spectra (CTF * ISSPA weighted, conjugated,
+normalised, pre-shifted), the local direction lists as CSR arrays, the
+fixed-context density and the output buffers. Scoring a pose then enqueues
+six launches on the current stream (splat with fused FFT input, 3-D R2C,
+projector, correlation, per-particle records, score sum) and reads back one
+float64. This is the in-process form of the reference's worker request
+``search_from_pdb`` / ``search_batch_from_pdb`` (Z3 gisapr_worker.py,
+Lite gisapr_batch_search.py:142-364) with the Python per-particle loop of
+run_search (v606:1749-1810) replaced by batched kernels.
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass
+from typing import Dict, List, Optional, Sequence
+
+import numpy as np
+import torch
+
+from . import _native as nat
+from .pdb2mrc import MovedChainDensity
+from .search import (IntegratedProjector, PackedCTFTorch, PackedFourierLayout, ParticleFourierPreparer,
+                     PsiGridBank, format_records)
+from .tables import (ModelAngles, ParticleRecord, build_local_orientation_entries, centered_to_packed_np,
+                     expand_radial_values, generate_soft_mask, psi_sampling_for_record)
+
+
+@dataclass
+class JobConfig:
+    box: int
+    apix: float
+    crop: int
+    psi_step: float
+    local_range: float
+    do_local_search: bool = True
+    newbox: Optional[int] = None
+    res: Optional[float] = None
+    mask_radius: Optional[int] = None
+    mask_edge: int = 6
+    discard_mask: bool = False
+    kk: float = 3.0
+    voltage: float = 300.0
+    cs: float = 2.7
+    chain_id: str = "A"
+    include_hetatm: bool = False
+
+    @property
+    def new_box(self) -> int:
+        return int(self.newbox or self.box)
+
+    @property
+    def resolution(self) -> float:
+        return float(self.res) if self.res is not None else 2.0 * float(self.apix)
+
+
+class ScoringJob:
+    """One refinement job (model + particles) resident on one CUDA device."""
+
+    def __init__(self, cfg: JobConfig, pdb_text: str, angles: ModelAngles,
+                 records: Sequence[ParticleRecord], images, fsc_values=None, has_ctf: bool = True,
+                 device="cuda"):
+        t0 = time.perf_counter()
+        self.cfg = cfg
+        self.device = torch.device(device)
+        if self.device.type != "cuda":
+            raise ValueError("ScoringJob needs a CUDA device")
+        if self.device.index is None:
+            self.device = torch.device("cuda", torch.cuda.current_device())
+        dev = self.device
+        n, nb = int(cfg.box), cfg.new_box
+        self.angles = angles
+        self.records = list(records)
+        self.layout = PackedFourierLayout(nb, cfg.crop, dev)
+        new_apix = n / nb * cfg.apix
+        self.trans_scale = cfg.apix / new_apix
+        # local direction lists -> compact template bank + CSR
+        if cfg.do_local_search:
+            entries = build_local_orientation_entries(self.records, angles.rot, angles.tilt, cfg.local_range)
+            local = [e[1:] for e in entries]
+        else:
+            local = [list(range(len(angles.rot))) for _ in self.records]
+        self.local = local
+        needed = sorted({k for l in local for k in l})
+        self.needed = needed
+        slot = {d: i for i, d in enumerate(needed)}
+        ptr = np.zeros(len(local) + 1, dtype=np.int32)
+        ptr[1:] = np.cumsum([len(l) for l in local])
+        idx = np.asarray([slot[k] for l in local for k in l], dtype=np.int32)
+        self.local_ptr = torch.from_numpy(ptr).to(dev)
+        self.local_idx = torch.from_numpy(idx if len(idx) else np.zeros(1, np.int32)).to(dev)
+        self.nnz = int(ptr[-1])
+        self.needed_dirs = torch.tensor(needed if needed else [0], dtype=torch.int32, device=dev)
+        self.needed_slots = torch.arange(max(1, len(needed)), dtype=torch.int32, device=dev)
+        # mask and FSC
+        mask_radius = cfg.mask_radius if cfg.mask_radius is not None else int(round(0.43 * n))
+        mask_np = generate_soft_mask((n, n), mask_radius, cfg.mask_edge)
+        self.mask = None if cfg.discard_mask else torch.from_numpy(mask_np).to(dev)
+        fsc = np.ones(n, np.float32) if fsc_values is None else np.asarray(fsc_values, np.float32)
+        self.packed_fsc = torch.from_numpy(np.ascontiguousarray(
+            centered_to_packed_np(expand_radial_values(fsc, nb)))).to(dev)
+        # psi sampling
+        self.psi_meta = [psi_sampling_for_record(r.psi, cfg.psi_step, cfg.do_local_search, cfg.local_range)
+                         for r in self.records]
+        self.n_psi = len(self.psi_meta[0][1]) if self.psi_meta else 1
+        uniq = list(dict.fromkeys(float(np.round(a, 6)) for _, eff in self.psi_meta for a in eff))
+        self.psi_bank = PsiGridBank(n, dev, uniq)
+        psi_index = np.asarray([[self.psi_bank.angle_to_index[float(np.round(a, 6))] for a in eff]
+                                for _, eff in self.psi_meta], dtype=np.int32).reshape(-1, self.n_psi)
+        # particle spectra, once per job
+        ctfgen = PackedCTFTorch(nb, new_apix, cfg.cs, cfg.voltage, cfg.kk, dev)
+        ctf = ctfgen.batch(self.records, has_ctf)
+        imgs = torch.as_tensor(np.asarray(images, dtype=np.float32)) if not torch.is_tensor(images) else images
+        imgs = imgs.to(dev, torch.float32).contiguous()
+        preparer = ParticleFourierPreparer(n, nb, dev, self.layout, self.mask, self.psi_bank)
+        self.stack = preparer.prepare_batch(imgs, torch.from_numpy(psi_index), ctf)
+        del imgs, ctf
+        # model
+        self.density = MovedChainDensity(pdb_text, cfg.chain_id, n, cfg.apix, cfg.resolution, dev,
+                                         include_hetatm=cfg.include_hetatm, from_text=True)
+        self.projector = IntegratedProjector(dev, n, nb, self.layout, self.mask, self.packed_fsc)
+        self.bank = torch.empty((max(1, len(needed)), nb, nb // 2 + 1), dtype=torch.complex64, device=dev)
+        m = max(1, self.nnz) * self.n_psi
+        self.score_buf = torch.empty(m, dtype=torch.float32, device=dev)
+        self.y_buf = torch.empty(m, dtype=torch.int32, device=dev)
+        self.x_buf = torch.empty(m, dtype=torch.int32, device=dev)
+        np_ = len(self.records)
+        self.best_entry = torch.empty(np_, dtype=torch.int32, device=dev)
+        self.best_psi = torch.empty(np_, dtype=torch.int32, device=dev)
+        self.peak = torch.empty(np_, dtype=torch.float32, device=dev)
+        self.peak_y = torch.empty(np_, dtype=torch.int32, device=dev)
+        self.peak_x = torch.empty(np_, dtype=torch.int32, device=dev)
+        self.zscore = torch.empty(np_, dtype=torch.float32, device=dev)
+        self.total = torch.zeros(1, dtype=torch.float64, device=dev)
+        self.pose_dev = torch.zeros(12, dtype=torch.float64, device=dev)
+        self.pose_host = torch.zeros(12, dtype=torch.float64).pin_memory()
+        self.total_host = torch.zeros(1, dtype=torch.float64).pin_memory()
+        torch.cuda.synchronize(dev)
+        self.setup_s = time.perf_counter() - t0
+
+    # ------------------------------------------------------------------
+    # launches of this engine per scored candidate (cuFFT's own kernels not counted)
+    KERNELS_PER_CANDIDATE = 6
+    STAGES = ("density", "volume_fft", "templates", "correlate", "records")
+
+    def enqueue(self, pose_device: torch.Tensor, write_volume: Optional[torch.Tensor] = None,
+                stage_events: Optional[Dict[str, list]] = None) -> None:
+        """Enqueue one candidate on the current stream; pose_device is
+        [rot(9), shift(3)] float64 on the device. The score lands in
+        self.total. ``stage_events`` (stage -> list) collects a pair of CUDA
+        events around each stage when given."""
+        dev = self.device
+        ctx = nat.Context.for_device(dev).handle
+        st = nat.stream_of(dev)
+
+        def mark(stage, end):
+            if stage_events is None:
+                return
+            ev = torch.cuda.Event(enable_timing=True)
+            ev.record()
+            if end:
+                stage_events[stage][-1].append(ev)
+            else:
+                stage_events.setdefault(stage, []).append([ev])
+
+        mark("density", False)
+        self.density.generate(None, out=write_volume, write_padded=True, pose_device=pose_device)
+        mark("density", True)
+        mark("volume_fft", False)
+        self.projector.volume_spectrum(None)
+        mark("volume_fft", True)
+        mark("templates", False)
+        if self.needed:
+            self.projector.project(self.angles, self.needed_dirs, self.bank, self.needed_slots)
+        mark("templates", True)
+        mark("correlate", False)
+        nat.call("gisapr_correlate", ctx, st, nat.ptr(self.bank), nat.ptr(self.stack), nat.ptr(self.local_ptr),
+                 nat.ptr(self.local_idx), len(self.records), self.n_psi, self.cfg.new_box, self.cfg.crop,
+                 nat.ptr(self.score_buf), nat.ptr(self.y_buf), nat.ptr(self.x_buf))
+        mark("correlate", True)
+        mark("records", False)
+        nat.call("gisapr_particle_results", st, nat.ptr(self.local_ptr), nat.ptr(self.score_buf),
+                 nat.ptr(self.y_buf), nat.ptr(self.x_buf), len(self.records), self.n_psi,
+                 nat.ptr(self.best_entry), nat.ptr(self.best_psi), nat.ptr(self.peak), nat.ptr(self.peak_y),
+                 nat.ptr(self.peak_x), nat.ptr(self.zscore))
+        nat.call("gisapr_score_sum", st, nat.ptr(self.local_ptr), nat.ptr(self.peak), len(self.records),
+                 nat.ptr(self.total))
+        mark("records", True)
+
+    def score(self, pose) -> float:
+        """sum_i exp(rawCC_i / 1024) of one pose (degrees, Angstrom)."""
+        self.pose_host.copy_(self.density.pose_tensor(pose))
+        self.pose_dev.copy_(self.pose_host, non_blocking=True)
+        self.enqueue(self.pose_dev)
+        self.total_host.copy_(self.total, non_blocking=True)
+        torch.cuda.current_stream(self.device).synchronize()
+        return float(self.total_host[0])
+
+    def score_many(self, poses) -> np.ndarray:
+        return np.asarray([self.score(p) for p in poses], dtype=np.float64)
+
+    # ------------------------------------------------------------------
+    def particle_results(self) -> Dict[str, np.ndarray]:
+        """Per-particle arrays of the last scored pose."""
+        out = dict(best_entry=self.best_entry, best_psi=self.best_psi, peak=self.peak,
+                   peak_y=self.peak_y, peak_x=self.peak_x, zscore=self.zscore)
+        return {k: v.cpu().numpy() for k, v in out.items()}
+
+    def result_records(self) -> List[List[object]]:
+        """The search text records of the last scored pose, in particle order
+        (v606:1494-1516), skipping particles without directions."""
+        r = self.particle_results()
+        rows = []
+        ptr = self.local_ptr.cpu().numpy()
+        for i, rec in enumerate(self.records):
+            if ptr[i + 1] <= ptr[i]:
+                continue
+            fake, _ = self.psi_meta[i]
+            local_index = int(r["best_entry"][i] - ptr[i])
+            rows.extend(format_records(rec, fake, self.angles.rot, self.angles.tilt, self.local[i], local_index,
+                                       int(r["best_psi"][i]), float(r["peak"][i]), int(r["peak_y"][i]),
+                                       int(r["peak_x"][i]), float(r["zscore"][i]), self.cfg.crop,
+                                       self.trans_scale))
+        return rows
+
+    def search_text(self) -> str:
+        return "".join(str(row) + "\n" for row in self.result_records())

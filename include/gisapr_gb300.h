@@ -1,0 +1,167 @@
+/*
+ * gisapr_gb300.h -- C ABI of the GB300 (sm_103a) candidate-scoring engine.
+ *
+ * Every pointer argument is a device pointer unless noted, every size is in
+ * elements, arrays are dense C order, complex values are interleaved float
+ * pairs (torch.complex64 layout). Work is enqueued on ``stream`` (a
+ * cudaStream_t passed as void*; NULL is the legacy default stream) and the
+ * calls return before it finishes. Each call returns GISAPR_OK or an error
+ * code; gisapr_last_error() gives the message of the calling thread's last
+ * failure. A context owns cuFFT plans, lookup tables and scratch buffers for
+ * one device; it is not thread-safe, so use one context per host thread.
+ * Scratch grows on first use of a size, so warm a size up once before
+ * capturing a call into a CUDA graph.
+ *
+ * Each entry point names the reference interface it replaces. File paths are
+ * those of GisAPR's sources: "v606" is
+ * test1_with_isspa_weight_varingKK_search_translation_also_v606_torch_
+ * optimized_standalone.py; "ZL/" is the GisAPR-Lite-v1.3.2 tree.
+ */
+#ifndef GISAPR_GB300_H
+#define GISAPR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  GISAPR_OK = 0,
+  GISAPR_ERR_ARGUMENT = 1,    /* bad size, shape or null pointer (Python: ValueError) */
+  GISAPR_ERR_CUDA = 2,        /* CUDA runtime / launch failure (Python: RuntimeError) */
+  GISAPR_ERR_CUFFT = 3,       /* cuFFT failure */
+  GISAPR_ERR_UNSUPPORTED = 4  /* a size this build does not implement */
+};
+
+typedef struct gisapr_context* gisapr_ctx;
+
+/* ABI version of this header (major * 100 + minor). */
+int gisapr_abi_version(void);
+
+/* Message of the calling thread's last failed call ("" if none). */
+const char* gisapr_last_error(void);
+
+/* Create / destroy a context bound to CUDA device ``device``. */
+int gisapr_context_create(int device, gisapr_ctx* out);
+int gisapr_context_destroy(gisapr_ctx ctx);
+
+/*
+ * Add Gaussian atoms to ``volume`` [box][box][box] in place.
+ * Replaces the NVRTC kernel ``deposit(xyz, numbers, volume, n, box, width,
+ * apix, rp, kn)`` of ZL/gisapr_cuda_density.py:21-55 (launched by
+ * accumulate, :177-200) and the index_add_ loop of
+ * pdb2mrc_gpu_ver_fp32_v3.py:71-97. xyz [n][3] float32 Angstrom, numbers [n]
+ * float32 atomic numbers (0 = no density). Atoms are summed per voxel in
+ * input order.
+ */
+int gisapr_deposit(gisapr_ctx ctx, void* stream, const float* xyz, const float* numbers, int n_atoms,
+                   float* volume, int box, int width, double apix, double rp, double kn);
+
+/*
+ * Density of a rigidly moved chain on top of a fixed context:
+ * out = fixed + splat(q), q = pdb_8.3((xyz - pivot) @ rot + pivot + shift).
+ * Replaces RigidDensityCache.generate (ZL/gisapr_batch_density.py:57-117)
+ * with transformed_density_atoms / quantize_coordinates
+ * (ZL/pdb_text.py:33-58, 204-223). pivot [3] float32 (the float32 mean of
+ * the chain's first-model atoms), rot [3][3] float64 row-major (applied as a
+ * row vector times rot), shift [3] float64 Angstrom. ``fixed`` may be NULL
+ * (zeros); ``out`` may be NULL when only the FFT input is wanted.
+ * ``write_padded`` != 0 also writes the sinc^2-weighted, zero-padded,
+ * fftshifted (2*box)^3 volume into the context's FFT input for
+ * gisapr_volume_spectrum(ctx, stream, NULL, ...).
+ */
+int gisapr_deposit_moved(gisapr_ctx ctx, void* stream, const float* xyz, const float* numbers,
+                         int n_atoms, const float* pivot, const double* rot, const double* shift,
+                         const float* fixed, float* out, int write_padded, int box, int width,
+                         double apix, double rp, double kn);
+
+/*
+ * Half-volume spectrum of a box^3 density: pad box/2 per side, multiply by
+ * sinc^2(|f|), fftshift, 3-D R2C (cuFFT). Replaces v606:1063-1073
+ * (IntegratedProjector.build_templates pre-amble with
+ * apply_sinc2_filter_inplace_3d, v606:837-853). ``volume`` NULL uses the
+ * FFT input last written by gisapr_deposit_moved(..., write_padded=1).
+ * spectrum: [2*box][2*box][box+1] complex, NOT fftshifted (the projector
+ * applies the reference's (z, y) shift when it samples).
+ */
+int gisapr_volume_spectrum(gisapr_ctx ctx, void* stream, const float* volume, int box,
+                           float* spectrum);
+
+/*
+ * Templates of ``n_build`` directions. Replaces the slice gather and the
+ * per-orientation tail of IntegratedProjector.build_templates
+ * (v606:1075-1147) with ProjectionWhitening (v606:899-992).
+ * rot [n_dir][3][3] float32 (rotation_matrices_t), dirs [n_build] int32
+ * direction indices, out_slot [n_build] int32 rows of ``bank`` to write (NULL:
+ * row = dirs[i]), mask [box][box] float32 or NULL, fsc [newbox][newbox/2+1]
+ * float32 packed FSC, bank [..][newbox][newbox/2+1] complex pre-shifted
+ * packed templates. box: power of two, 32..256; newbox: even, <= box,
+ * multiple of 16.
+ */
+int gisapr_project_templates(gisapr_ctx ctx, void* stream, const float* spectrum, int box,
+                             const float* rot, const int* dirs, int n_build, const int* out_slot,
+                             const float* mask, const float* fsc, int newbox, float* bank);
+
+/*
+ * CTF * ISSPA weight per particle in the packed layout. Replaces
+ * PackedCTFTorch.batch (v606:781-829). dfu/dfv/dfa [n] float32 (Angstrom,
+ * degrees); tx, ty, tu4, tnc [K] float32 static tables (packed frequency x,
+ * y, u^4 and the ISSPA noise curve, v606:745-777); out [n][K] float32.
+ */
+int gisapr_packed_ctf(void* stream, const float* dfu, const float* dfv, const float* dfa, int n,
+                      const float* tx, const float* ty, const float* tu4, const float* tnc, int K,
+                      float k1, float k2, float k3, float k5, float kk, float* out);
+
+/*
+ * Particle spectra for n particles x n_psi in-plane angles. Replaces
+ * ParticleFourierPreparer.prepare (v606:1340-1374) with PsiGridBank
+ * (v606:1193-1256). images [n][box][box] float32; psi_index [n][n_psi] int32
+ * rows of psi_table [n_angles][4] float32 (cos, sin, offset_row, offset_col
+ * of each effective psi, as PsiGridBank builds them); mask [box][box] or
+ * NULL; ctf [n][newbox][newbox/2+1]; out [n][n_psi][newbox][newbox/2+1]
+ * complex, conjugated, L2-normalised and pre-shifted.
+ */
+int gisapr_prepare_particles(gisapr_ctx ctx, void* stream, const float* images, int n, int n_psi,
+                             const int* psi_index, const float* psi_table, const float* mask,
+                             const float* ctf, int box, int newbox, float* out);
+
+/*
+ * For every particle b and every local direction entry e in
+ * [local_ptr[b], local_ptr[b+1]) and psi s: the maximum of 1024 * n^2 *
+ * irfft2(T[local_idx[e]] * P[b][s]) over the centred crop x crop window,
+ * with its row-major first argmax. Replaces correlate_templates_and_particle
+ * (v606:1418-1449) for a whole particle set. bank [..][n][n/2+1] and
+ * stack [n_particles][n_psi][n][n/2+1] complex pre-shifted; local_ptr
+ * [n_particles+1], local_idx [nnz] int32; out_score [nnz][n_psi] float32,
+ * out_y / out_x [nnz][n_psi] int32 crop indices. crop: even, 2..16.
+ */
+int gisapr_correlate(gisapr_ctx ctx, void* stream, const float* bank, const float* stack,
+                     const int* local_ptr, const int* local_idx, int n_particles, int n_psi, int n,
+                     int crop, float* out_score, int* out_y, int* out_x);
+
+/*
+ * Per particle: first maximum over (local entry, psi), its crop position and
+ * the z-score (peak - mean) / population sigma over all the particle's
+ * scores. Replaces the numeric part of make_result_records (v606:1466-1491).
+ * best_entry is a global entry index (-1 for a particle without directions).
+ */
+int gisapr_particle_results(void* stream, const int* local_ptr, const float* score, const int* ys,
+                            const int* xs, int n_particles, int n_psi, int* best_entry,
+                            int* best_psi, float* peak, int* peak_y, int* peak_x, float* zscore);
+
+/*
+ * Candidate score sum over particles with directions of exp(peak / 1024),
+ * float64 into out[0]. Replaces ZL/gisapr_batch_search.py:361 and the
+ * "CC + simple sum" mode of new_method_to_fit_the_2nd_Gaussian_PEAK_v4.py:
+ * 133-134.
+ */
+int gisapr_score_sum(void* stream, const int* local_ptr, const float* peak, int n_particles,
+                     double* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GISAPR_GB300_H */

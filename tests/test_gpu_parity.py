@@ -247,7 +247,17 @@ def test_scoring_job_box64_published_config(golden64):
     assert abs(score / float(g["score"]) - 1.0) < SCORE_REL
     r = job.particle_results()
     valid = r["best_entry"] >= 0
-    np.testing.assert_allclose(r["peak"][valid], g["peak"], rtol=PEAK_REL)
+    # Per particle: within 1e-4 of the FP64 oracle; against the float32
+    # reference the two error floors add (the reference's own peaks sit up to
+    # ~9e-5 from the oracle on this case), hence 2e-4.
+    rd = data.records
+    ora = O.evaluate_candidate(data.model.pdb_text, g["pose"], 64, 1.5, 3.0, data.model_rot, data.model_tilt,
+                               data.images, rd.line_index, rd.rot, rd.tilt, rd.psi, rd.defocus_u, rd.defocus_v,
+                               rd.defocus_angle, data.fsc, spec.mask_radius, spec.mask_edge, spec.psi_step,
+                               spec.local_range, spec.crop, kk=spec.kk, keep_templates=False)
+    np.testing.assert_allclose(r["peak"][valid], ora["raw"], rtol=PEAK_REL)
+    np.testing.assert_allclose(r["peak"][valid], g["peak"], rtol=2 * PEAK_REL)
+    assert abs(score / ora["score"] - 1.0) < SCORE_REL
     best_dir = np.asarray([job.needed[int(job.local_idx[e])] for e in r["best_entry"][valid]])
     agree = np.mean(best_dir == g["best_dir"])
     assert agree >= 0.99, agree

@@ -23,6 +23,7 @@ SIGNATURES = {
     "gisapr_context_create": [_i, C.POINTER(_p)],
     "gisapr_context_destroy": [_p],
     "gisapr_deposit": [_p, _p, _p, _p, _i, _p, _i, _i, _d, _d, _d],
+    "gisapr_deposit_noalloc": [_p, _p, _p, _i, _p, _i, _i, _d, _d, _d],
     "gisapr_deposit_moved": [_p, _p, _p, _p, _i, _p, _p, _p, _p, _p, _i, _i, _i, _d, _d, _d],
     "gisapr_volume_spectrum": [_p, _p, _p, _i, _p],
     "gisapr_project_templates": [_p, _p, _p, _i, _p, _p, _i, _p, _p, _p, _i, _p],

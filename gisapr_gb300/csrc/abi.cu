@@ -85,6 +85,10 @@ struct CorrTables {
 
 }  // namespace
 
+// Lets the other translation units of the library report errors through
+// gisapr_last_error().
+void gisapr_internal_set_error(const char* msg) { g_last_error = msg; }
+
 struct gisapr_context {
   int device = 0;
   float2* tw = nullptr;  // exp(-2 pi i t / kMaxFftLen), t < kMaxFftLen/2

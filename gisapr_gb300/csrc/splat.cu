@@ -296,3 +296,84 @@ cudaError_t launch_pad_sinc_shift(cudaStream_t st, const float* vol, float* padd
   pad_sinc_shift<<<grid, 256, 0, st>>>(vol, padded, box);
   return cudaGetLastError();
 }
+
+// ---------------------------------------------------------------------------
+// gisapr_deposit_noalloc: the deposit entry point for callers that cannot
+// allocate device memory.
+//
+// gisapr_deposit keeps its per-atom records (48 bytes per atom) in a buffer
+// the context grows with cudaMalloc. Some callers cannot do that: a host
+// whose device memory is handed out by another framework's pool and must not
+// change size, code running while a CUDA graph is being captured, or a
+// latency-bound loop that cannot afford the device synchronisation a
+// cudaMalloc implies. This variant keeps the records in a fixed array in the
+// library's own device memory instead, so it allocates nothing and needs no
+// context. Every GPU that loads the library holds that array (3 MiB) until
+// the process exits.
+// ---------------------------------------------------------------------------
+#include <mutex>
+#include <string>
+
+#include "../../include/gisapr_gb300.h"
+
+void gisapr_internal_set_error(const char* msg);
+
+namespace {
+
+// Largest atom count one call accepts.
+constexpr int kNoAllocMaxAtoms = 65536;
+static __device__ __align__(256) AtomRec g_noalloc_atoms[kNoAllocMaxAtoms];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+int noalloc_fail(int code, const std::string& msg) {
+  gisapr_internal_set_error(msg.c_str());
+  return code;
+}
+
+}  // namespace
+
+extern "C" int gisapr_deposit_noalloc(void* stream, const float* xyz, const float* numbers, int n_atoms,
+                                      float* volume, int box, int width, double apix, double rp, double kn) {
+  if (!volume) return noalloc_fail(GISAPR_ERR_ARGUMENT, "volume is NULL");
+  if (n_atoms < 0 || (n_atoms > 0 && (!xyz || !numbers)))
+    return noalloc_fail(GISAPR_ERR_ARGUMENT, "atom arrays are NULL or n_atoms < 0");
+  if (n_atoms > kNoAllocMaxAtoms)
+    return noalloc_fail(GISAPR_ERR_ARGUMENT,
+                        "gisapr_deposit_noalloc accepts at most " + std::to_string(kNoAllocMaxAtoms) +
+                            " atoms per call, got " + std::to_string(n_atoms) +
+                            " (split the atoms over several calls or use gisapr_deposit)");
+  if (box < 1 || box > 1024) return noalloc_fail(GISAPR_ERR_ARGUMENT, "box out of range");
+  if (width < 3) return noalloc_fail(GISAPR_ERR_ARGUMENT, "width must be >= 3 (insufficient sampling)");
+  if (!(apix > 0.0) || !isfinite(apix) || !isfinite(rp) || !isfinite(kn))
+    return noalloc_fail(GISAPR_ERR_ARGUMENT, "apix, rp and kn must be positive and finite");
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return noalloc_fail(GISAPR_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return noalloc_fail(GISAPR_ERR_UNSUPPORTED, "device index too large");
+  void* recs = nullptr;
+  {
+    // First call on a device: resolve the device address of the record array
+    // with that device current. Host code must not use the symbol itself.
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+      void* p = nullptr;
+      e = cudaGetSymbolAddress(&p, g_noalloc_atoms);
+      if (e != cudaSuccess || !p)
+        return noalloc_fail(GISAPR_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+      g_noalloc_ptr[dev] = p;
+    }
+    recs = g_noalloc_ptr[dev];
+  }
+  if (n_atoms == 0) return GISAPR_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  // Every record a call reads is written first by atoms_prepare in the same
+  // call, so nothing left from an earlier call needs clearing.
+  e = launch_atoms_prepare(st, xyz, numbers, n_atoms, 0, nullptr, nullptr, nullptr, box, width, apix, kn, recs);
+  if (e != cudaSuccess) return noalloc_fail(GISAPR_ERR_CUDA, std::string("atoms_prepare: ") + cudaGetErrorString(e));
+  e = launch_splat_bricks(st, recs, n_atoms, volume, volume, nullptr, box, rp);
+  if (e != cudaSuccess) return noalloc_fail(GISAPR_ERR_CUDA, std::string("splat_bricks: ") + cudaGetErrorString(e));
+  return GISAPR_OK;
+}

@@ -60,6 +60,24 @@ int gisapr_deposit(gisapr_ctx ctx, void* stream, const float* xyz, const float* 
                    float* volume, int box, int width, double apix, double rp, double kn);
 
 /*
+ * gisapr_deposit without any device allocation. Same inputs, result and
+ * per-voxel atom order as gisapr_deposit, for callers that cannot allocate
+ * device memory (memory owned by another framework's pool, code running
+ * while a CUDA graph is captured, loops that cannot take the device-wide
+ * synchronisation of a cudaMalloc). This entry point has no counterpart in
+ * the reference. Its per-atom scratch is a fixed array of 65,536 records
+ * (3 MiB) in the library's static device memory, held by every GPU that
+ * loads the library until the process exits; more atoms per call are
+ * rejected with GISAPR_ERR_ARGUMENT. No context is needed. The first call
+ * on a device resolves the array's device address with that device current,
+ * so make that first call before capturing a stream. All calls share the
+ * array: calls whose work overlaps on the GPU (other streams, other host
+ * threads) race on it, so serialise them.
+ */
+int gisapr_deposit_noalloc(void* stream, const float* xyz, const float* numbers, int n_atoms,
+                           float* volume, int box, int width, double apix, double rp, double kn);
+
+/*
  * Density of a rigidly moved chain on top of a fixed context:
  * out = fixed + splat(q), q = pdb_8.3((xyz - pivot) @ rot + pivot + shift).
  * Replaces RigidDensityCache.generate (ZL/gisapr_batch_density.py:57-117)

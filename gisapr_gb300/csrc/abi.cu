@@ -22,12 +22,21 @@ size_t atom_record_bytes();
 cudaError_t launch_splat_bricks(cudaStream_t, const void*, int, const float*, float*, float*, int,
                                 double);
 cudaError_t launch_pad_sinc_shift(cudaStream_t, const float*, float*, int);
+int splat_bin_cap();
+int splat_bin_count(int box);
+cudaError_t launch_splat_binned(cudaStream_t, const float*, const float*, int, int, const float*, const double*,
+                                const double*, const float*, float*, float*, int, int, double, double, double, void*,
+                                int*, int*);
 size_t project_scratch_elems(int N, int nb);
 size_t project_smem_bytes(int N, int n_bins);
 cudaError_t launch_project_templates(cudaStream_t, const float2*, const float*, const int*, int,
                                      const int*, const float*, const float*, const int*, const int*,
                                      const float*, int, const float2*, float2*, float2*, int, int,
                                      int);
+size_t project_smem_bytes_fast(int N, int n_bins);
+cudaError_t launch_project_templates_fast(cudaStream_t, const float2*, const float*, const int*, int,
+                                          const int*, const float*, const float*, const int*, const int*,
+                                          const float*, int, const float2*, float2*, int, int, int);
 cudaError_t launch_packed_ctf(cudaStream_t, const float*, const float*, const float*, int,
                               const float*, const float*, const float*, const float*, int, float,
                               float, float, float, float, float*);
@@ -95,7 +104,7 @@ struct gisapr_context {
   std::map<int, std::pair<cufftHandle, float*>> fft;  // box -> (R2C plan, padded input)
   std::map<int, BinTable> bins;                        // N -> radial bins
   std::map<std::pair<int, int>, CorrTables> corr;      // (n, crop) -> twiddles
-  DeviceBuffer atoms, proj_scratch, prep_scratch;
+  DeviceBuffer atoms, bin_counts, bin_lists, proj_scratch, prep_scratch;
   int sm_count = 152;
 };
 
@@ -281,6 +290,8 @@ int gisapr_context_destroy(gisapr_ctx ctx) {
   for (auto& kv : ctx->bins) { cudaFree(kv.second.list); cudaFree(kv.second.ptr); cudaFree(kv.second.count); }
   for (auto& kv : ctx->corr) { cudaFree(kv.second.outer); cudaFree(kv.second.col); }
   cudaFree(ctx->atoms.ptr);
+  cudaFree(ctx->bin_counts.ptr);
+  cudaFree(ctx->bin_lists.ptr);
   cudaFree(ctx->proj_scratch.ptr);
   cudaFree(ctx->prep_scratch.ptr);
   cudaFree(ctx->tw);
@@ -305,11 +316,15 @@ static int deposit_common(gisapr_ctx ctx, void* stream, const float* xyz, const 
   cudaStream_t st = (cudaStream_t)stream;
   rc = ensure(ctx->atoms, (size_t)(n > 0 ? n : 1) * atom_record_bytes(), "cudaMalloc(atoms)");
   if (rc) return rc;
-  GISAPR_CHECK_CUDA(launch_atoms_prepare(st, xyz, numbers, n, transform, pivot, rot, shift, box, width,
-                                         apix, kn, ctx->atoms.ptr),
-                    "atoms_prepare");
-  GISAPR_CHECK_CUDA(launch_splat_bricks(st, ctx->atoms.ptr, n, initial, out, padded, box, rp),
-                    "splat_bricks");
+  const size_t nbricks = (size_t)splat_bin_count(box);
+  rc = ensure(ctx->bin_counts, nbricks * sizeof(int), "cudaMalloc(brick counts)");
+  if (rc) return rc;
+  rc = ensure(ctx->bin_lists, nbricks * splat_bin_cap() * sizeof(int), "cudaMalloc(brick lists)");
+  if (rc) return rc;
+  GISAPR_CHECK_CUDA(launch_splat_binned(st, xyz, numbers, n, transform, pivot, rot, shift, initial, out, padded,
+                                        box, width, apix, rp, kn, ctx->atoms.ptr, (int*)ctx->bin_counts.ptr,
+                                        (int*)ctx->bin_lists.ptr),
+                    "splat");
   return GISAPR_OK;
 }
 
@@ -375,6 +390,15 @@ int gisapr_project_templates(gisapr_ctx ctx, void* stream, const float* spectrum
   BinTable bt;
   rc = get_bins(ctx, box, &bt);
   if (rc) return rc;
+  if (box <= 128) {
+    // whole template in shared memory, one CTA per SM
+    const int grid = grid_for(ctx, n_build, 1);
+    GISAPR_CHECK_CUDA(launch_project_templates_fast((cudaStream_t)stream, (const float2*)spectrum, rot, dirs,
+                                                    n_build, out_slot, mask, fsc, bt.list, bt.ptr, bt.count,
+                                                    bt.n_bins, ctx->tw, (float2*)bank, grid, box, newbox),
+                      "project_templates");
+    return GISAPR_OK;
+  }
   const int grid = grid_for(ctx, n_build, 2);
   rc = ensure(ctx->proj_scratch, (size_t)grid * project_scratch_elems(box, newbox) * sizeof(float2),
               "cudaMalloc(projector scratch)");

@@ -150,3 +150,127 @@ enum GisaprDeviceStatus : int {
   kDevBadIndex = 1,
   kDevTooManyLocal = 2,
 };
+
+// ---------------------------------------------------------------------------
+// Register DFT codelets, natural-order outputs.
+// dft<R, DIR>: X[k] = sum_n x[n] exp(DIR * 2 pi i n k / R), DIR = -1 forward,
+// +1 inverse (unnormalised). Constants are cos/sin of multiples of pi/8.
+// ---------------------------------------------------------------------------
+template <int DIR>
+GISAPR_DEV float2 mul_dir_i(float2 a) {  // a * (DIR * i)
+  return DIR > 0 ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+
+template <int DIR>
+GISAPR_DEV void dft2(float2& a, float2& b) {
+  float2 s = cadd(a, b), d = csub(a, b);
+  a = s; b = d;
+}
+
+template <int DIR>
+GISAPR_DEV void dft4(float2& a, float2& b, float2& c, float2& d) {
+  const float2 s0 = cadd(a, c), s1 = csub(a, c), s2 = cadd(b, d), s3 = csub(b, d);
+  const float2 t = mul_dir_i<DIR>(s3);
+  a = cadd(s0, s2);
+  c = csub(s0, s2);
+  b = cadd(s1, t);
+  d = csub(s1, t);
+}
+
+// exp(DIR * i * k * pi / 8) for k = 0..15
+template <int DIR>
+GISAPR_DEV float2 w16(int k) {
+  constexpr float C1 = 0.92387953251128675613f, S1 = 0.38268343236508977173f, R2 = 0.70710678118654752440f;
+  float c, s;
+  switch (k & 15) {
+    case 0: c = 1.f; s = 0.f; break;
+    case 1: c = C1; s = S1; break;
+    case 2: c = R2; s = R2; break;
+    case 3: c = S1; s = C1; break;
+    case 4: c = 0.f; s = 1.f; break;
+    case 5: c = -S1; s = C1; break;
+    case 6: c = -R2; s = R2; break;
+    case 7: c = -C1; s = S1; break;
+    case 8: c = -1.f; s = 0.f; break;
+    case 9: c = -C1; s = -S1; break;
+    case 10: c = -R2; s = -R2; break;
+    case 11: c = -S1; s = -C1; break;
+    case 12: c = 0.f; s = -1.f; break;
+    case 13: c = S1; s = -C1; break;
+    case 14: c = R2; s = -R2; break;
+    default: c = C1; s = -S1; break;
+  }
+  return make_float2(c, DIR > 0 ? s : -s);
+}
+
+template <int R, int DIR>
+GISAPR_DEV void dft(float2 (&x)[R]);
+
+template <>
+GISAPR_DEV void dft<2, 1>(float2 (&x)[2]) { dft2<1>(x[0], x[1]); }
+template <>
+GISAPR_DEV void dft<2, -1>(float2 (&x)[2]) { dft2<-1>(x[0], x[1]); }
+
+template <>
+GISAPR_DEV void dft<4, 1>(float2 (&x)[4]) { dft4<1>(x[0], x[1], x[2], x[3]); }
+template <>
+GISAPR_DEV void dft<4, -1>(float2 (&x)[4]) { dft4<-1>(x[0], x[1], x[2], x[3]); }
+
+// 8 = 2 x 4: n = 4 n1 + n2, k = k1 + 2 k2
+template <int DIR>
+GISAPR_DEV void dft8_impl(float2 (&x)[8]) {
+#pragma unroll
+  for (int n2 = 0; n2 < 4; ++n2) dft2<DIR>(x[n2], x[n2 + 4]);  // x[n2 + 4 k1] = A[n2][k1]
+  // twiddle A[n2][1] by exp(DIR 2 pi i n2 / 8) = w16(2 n2)
+#pragma unroll
+  for (int n2 = 1; n2 < 4; ++n2) x[n2 + 4] = cmul(x[n2 + 4], w16<DIR>(2 * n2));
+  dft4<DIR>(x[0], x[1], x[2], x[3]);  // k1 = 0 -> X[0], X[2], X[4], X[6]
+  dft4<DIR>(x[4], x[5], x[6], x[7]);  // k1 = 1 -> X[1], X[3], X[5], X[7]
+  float2 y[8];
+#pragma unroll
+  for (int k2 = 0; k2 < 4; ++k2) {
+    y[2 * k2] = x[k2];
+    y[2 * k2 + 1] = x[4 + k2];
+  }
+#pragma unroll
+  for (int k = 0; k < 8; ++k) x[k] = y[k];
+}
+template <>
+GISAPR_DEV void dft<8, 1>(float2 (&x)[8]) { dft8_impl<1>(x); }
+template <>
+GISAPR_DEV void dft<8, -1>(float2 (&x)[8]) { dft8_impl<-1>(x); }
+
+// 16 = 4 x 4: n = 4 n1 + n2, k = k1 + 4 k2
+template <int DIR>
+GISAPR_DEV void dft16_impl(float2 (&x)[16]) {
+#pragma unroll
+  for (int n2 = 0; n2 < 4; ++n2) dft4<DIR>(x[n2], x[n2 + 4], x[n2 + 8], x[n2 + 12]);
+  // x[n2 + 4 k1] = A[n2][k1]; twiddle by exp(DIR 2 pi i n2 k1 / 16) = w16(n2 k1)
+#pragma unroll
+  for (int n2 = 1; n2 < 4; ++n2)
+#pragma unroll
+    for (int k1 = 1; k1 < 4; ++k1) x[n2 + 4 * k1] = cmul(x[n2 + 4 * k1], w16<DIR>(n2 * k1));
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) dft4<DIR>(x[4 * k1 + 0], x[4 * k1 + 1], x[4 * k1 + 2], x[4 * k1 + 3]);
+  // x[4 k1 + k2] = X[k1 + 4 k2]
+  float2 y[16];
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) y[k1 + 4 * k2] = x[4 * k1 + k2];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) x[k] = y[k];
+}
+template <>
+GISAPR_DEV void dft<16, 1>(float2 (&x)[16]) { dft16_impl<1>(x); }
+template <>
+GISAPR_DEV void dft<16, -1>(float2 (&x)[16]) { dft16_impl<-1>(x); }
+
+// exp(DIR * 2 pi i * t / L) from the half table tw[t'] = exp(-2 pi i t' / kMaxFftLen),
+// t' < kMaxFftLen / 2, for any integer t (L divides kMaxFftLen).
+template <int DIR>
+GISAPR_DEV float2 tw_full(const float2* __restrict__ tw, int t, int L) {
+  int u = (t * (kMaxFftLen / L)) & (kMaxFftLen - 1);
+  float2 w = u < kMaxFftLen / 2 ? tw[u] : make_float2(-tw[u - kMaxFftLen / 2].x, -tw[u - kMaxFftLen / 2].y);
+  return DIR < 0 ? w : make_float2(w.x, -w.y);
+}

@@ -434,3 +434,397 @@ cudaError_t launch_project_templates(cudaStream_t st, const float2* spectrum, co
   project_templates<<<grid, kThreads, smem, st>>>(P);
   return cudaGetLastError();
 }
+
+// ===========================================================================
+// Shared-memory projector for box <= 128.
+//
+// The whole per-template working set (the N x (N+1) plane left by the pruned
+// inverse along rows, then the N x (N/2+1) spectra of the whitening) stays in
+// shared memory. Every 1-D transform is a four-step 16 x (N/16) FFT done by
+// one warp on whole lines: a 16-point register codelet over n1, twiddles,
+// then N/16-point codelets, with only warp barriers inside a pass and block
+// barriers between passes. The arithmetic of every pass is that of the
+// general kernel above (same float32 slice coordinates, same passes A-G).
+// ===========================================================================
+namespace {
+
+constexpr int kSmemThreads = 512;
+constexpr int kSmemWarps = kSmemThreads / 32;
+
+// In-place four-step FFT of ``nlines`` (<= 32 / (N/16)) lines starting at
+// ``buf``; line l, element k at buf[l * ls + k * es]. Natural order in and out.
+template <int N, int DIR>
+__device__ __forceinline__ void warp_fft(float2* buf, int nlines, int ls, int es, const float2* tw) {
+  constexpr int L2 = N / 16, G = 32 / L2, T = (G * 16) / 32;
+  const int lane = threadIdx.x & 31;
+  {
+    const int g = lane / L2, n2 = lane % L2;
+    if (g < nlines) {
+      float2* p = buf + g * ls;
+      float2 x[16];
+#pragma unroll
+      for (int n1 = 0; n1 < 16; ++n1) x[n1] = p[(L2 * n1 + n2) * es];
+      dft<16, DIR>(x);
+#pragma unroll
+      for (int k1 = 1; k1 < 16; ++k1)
+        if (n2) x[k1] = cmul(x[k1], tw_full<DIR>(tw, n2 * k1, N));
+#pragma unroll
+      for (int k1 = 0; k1 < 16; ++k1) p[(L2 * k1 + n2) * es] = x[k1];
+    }
+  }
+  __syncwarp();
+  float2 y[T][L2];
+#pragma unroll
+  for (int t = 0; t < T; ++t) {
+    const int task = lane + 32 * t, g = task / 16, k1 = task % 16;
+    if (g < nlines) {
+      const float2* p = buf + g * ls;
+#pragma unroll
+      for (int n2 = 0; n2 < L2; ++n2) y[t][n2] = p[(L2 * k1 + n2) * es];
+      dft<L2, DIR>(y[t]);
+    }
+  }
+  __syncwarp();
+#pragma unroll
+  for (int t = 0; t < T; ++t) {
+    const int task = lane + 32 * t, g = task / 16, k1 = task % 16;
+    if (g < nlines) {
+      float2* p = buf + g * ls;
+#pragma unroll
+      for (int k2 = 0; k2 < L2; ++k2) p[(k1 + 16 * k2) * es] = y[t][k2];
+    }
+  }
+  __syncwarp();
+}
+
+template <int N>
+__device__ void build_one_smem(const ProjParams& P, int dir, int slot, float2* Zs, float2* stage_all,
+                               const float2* tw, float* s_div, double* red, double* s_coef) {
+  constexpr int m = 2 * N, W = N + 1, LDZ = N + 1, HC = N / 2 + 1, L2 = N / 16, G = 32 / L2;
+  const int nb = P.nb, H = nb / 2 + 1;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const float* R = P.rot + (size_t)dir * 9;
+  const float R00 = R[0], R01 = R[1], R10 = R[3], R11 = R[4], R20 = R[6], R21 = R[7];
+  const float inv_m = (float)(1.0 / (double)m);
+
+  // ---- pass A: gather + pruned row inverse, 16/L2 columns per warp round
+  {
+    constexpr int CPR = 16 / L2;  // columns per warp round
+    float2* stage = stage_all + warp * (CPR * 2 * N);
+    for (int c0 = warp * CPR; c0 < W; c0 += kSmemWarps * CPR) {
+      {  // step 1: lane -> (column, parity, n2)
+        const int cl = lane / (2 * L2), e = (lane / L2) & 1, n2 = lane % L2;
+        const int c = c0 + cl;
+        if (c < W) {
+          float2 x[16];
+#pragma unroll
+          for (int n1 = 0; n1 < 16; ++n1) {
+            const int r = 2 * (L2 * n1 + n2) + e;  // standard-order row of the 2N grid
+            const int kys = (r + N) % m;
+            const float gy = __fmul_rn((float)(kys - N), inv_m);
+            const float gx = __fmul_rn((float)c, inv_m);
+            float rx = __fadd_rn(__fmul_rn(R00, gx), __fmul_rn(R01, gy));
+            float ry = __fadd_rn(__fmul_rn(R10, gx), __fmul_rn(R11, gy));
+            float rz = __fadd_rn(__fmul_rn(R20, gx), __fmul_rn(R21, gy));
+            const bool conj = rx < 0.0f;
+            if (conj) { rx = -rx; ry = -ry; rz = -rz; }
+            const float cz = __fadd_rn(__fmul_rn(rz, (float)m), (float)(m / 2));
+            const float cy = __fadd_rn(__fmul_rn(ry, (float)m), (float)(m / 2));
+            const float cx = __fmul_rn(rx, (float)m);
+            float2 v = sample_trilinear(P.spectrum, m, W, grid_pixel(cz, m), grid_pixel(cy, m),
+                                        grid_pixel(cx, W));
+            if (conj) v.y = -v.y;
+            x[n1] = v;
+          }
+          dft<16, 1>(x);
+#pragma unroll
+          for (int k1 = 1; k1 < 16; ++k1)
+            if (n2) x[k1] = cmul(x[k1], tw_full<1>(tw, n2 * k1, N));
+          float2* s = stage + (cl * 2 + e) * N;
+#pragma unroll
+          for (int k1 = 0; k1 < 16; ++k1) s[L2 * k1 + n2] = x[k1];
+        }
+      }
+      __syncwarp();
+      {  // step 2: tasks (column, k1), both parities, combine into Zs
+        constexpr int T2 = (CPR * 16) / 32;
+#pragma unroll
+        for (int t = 0; t < T2; ++t) {
+          const int task = lane + 32 * t, cl = task / 16, k1 = task % 16;
+          const int c = c0 + cl;
+          if (c < W) {
+            float2 a0[L2], a1[L2];
+            const float2* s0 = stage + (cl * 2) * N;
+            const float2* s1 = s0 + N;
+#pragma unroll
+            for (int n2 = 0; n2 < L2; ++n2) { a0[n2] = s0[L2 * k1 + n2]; a1[n2] = s1[L2 * k1 + n2]; }
+            dft<L2, 1>(a0);
+            dft<L2, 1>(a1);
+#pragma unroll
+            for (int k2 = 0; k2 < L2; ++k2) {
+              const int k = k1 + 16 * k2;
+              const int u = k < N / 2 ? k : k - N;
+              const float2 z = cadd(a0[k2], cmul(tw_pos(tw, u, m), a1[k2]));
+              Zs[(u + N / 2) * LDZ + c] = z;
+            }
+          }
+        }
+      }
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+
+  // ---- pass B: C2R along columns, keep centred N, then forward row FFT
+  const float scale_b = (float)(1.0 / ((double)m * (double)m));
+  for (int r0 = warp * G; r0 < N; r0 += kSmemWarps * G) {
+    float2* rows = Zs + r0 * LDZ;
+    {  // W = Ye + i Yo, read all then write (k and N-k cross)
+      float2 wv[16];
+#pragma unroll
+      for (int t = 0; t < 16; ++t) {
+        const int idx = lane + 32 * t, g = idx / N, k = idx % N;
+        const float2* Z = rows + g * LDZ;
+        float2 ye, yo;
+        if (k == 0) {
+          const float a = Z[0].x, b = Z[N].x;
+          ye = make_float2(a + b, 0.f);
+          yo = make_float2(a - b, 0.f);
+        } else {
+          const float2 zk = Z[k], zc = cconj(Z[N - k]);
+          ye = cadd(zk, zc);
+          yo = cmul(csub(zk, zc), tw_pos(tw, k, m));
+        }
+        wv[t] = make_float2(ye.x - yo.y, ye.y + yo.x);
+      }
+      __syncwarp();
+#pragma unroll
+      for (int t = 0; t < 16; ++t) {
+        const int idx = lane + 32 * t, g = idx / N, k = idx % N;
+        rows[g * LDZ + k] = wv[t];
+      }
+      __syncwarp();
+    }
+    warp_fft<N, 1>(rows, G, LDZ, 1, tw);
+    {  // p(2n) = Re z(n), p(2n+1) = Im z(n); keep v = (j - N/2) mod 2N
+      float pv[16];
+#pragma unroll
+      for (int t = 0; t < 16; ++t) {
+        const int idx = lane + 32 * t, g = idx / N, j = idx % N;
+        const int v = (j - N / 2 + m) % m;
+        const float2 zz = rows[g * LDZ + (v >> 1)];
+        pv[t] = ((v & 1) ? zz.y : zz.x) * scale_b;
+      }
+      __syncwarp();
+#pragma unroll
+      for (int t = 0; t < 16; ++t) {
+        const int idx = lane + 32 * t, g = idx / N, j = idx % N;
+        rows[g * LDZ + j] = make_float2(pv[t], 0.f);
+      }
+      __syncwarp();
+    }
+    warp_fft<N, -1>(rows, G, LDZ, 1, tw);
+  }
+  __syncthreads();
+
+  // ---- pass C: forward column FFT over kx in [0, N/2]
+  for (int c0 = warp * G; c0 < HC; c0 += kSmemWarps * G)
+    warp_fft<N, -1>(Zs + c0, min(G, HC - c0), 1, LDZ, tw);
+  __syncthreads();
+  for (int b = warp; b < P.n_bins; b += kSmemWarps) {
+    double acc = 0.0;
+    for (int e = P.bin_ptr[b] + lane; e < P.bin_ptr[b + 1]; e += 32) {
+      const int idx = P.bin_list[e];
+      const int r = idx / HC, kx = idx - r * HC;
+      const float2 f = Zs[r * LDZ + kx];
+      const double a = (double)hypotf(f.x, f.y);
+      acc += (kx == 0 || kx == N / 2) ? a : 2.0 * a;
+    }
+    acc = warp_sum_d(acc);
+    if (lane == 0) s_div[b] = (b == 0) ? 1.0f : (float)((double)P.bin_count[b] / acc);
+  }
+  __syncthreads();
+
+  // ---- pass D: radial divisor, inverse column FFT
+  for (int c0 = warp * G; c0 < HC; c0 += kSmemWarps * G) {
+    const int nc = min(G, HC - c0);
+    for (int idx = lane; idx < nc * N; idx += 32) {
+      const int cl = idx / N, r = idx % N, kx = c0 + cl;
+      const int ky = r < N / 2 ? r : r - N;
+      const int bin = (int)rintf(sqrtf((float)(ky * ky + kx * kx)));
+      Zs[r * LDZ + kx] = cscale(Zs[r * LDZ + kx], s_div[bin]);
+    }
+    __syncwarp();
+    warp_fft<N, 1>(Zs + c0, nc, 1, LDZ, tw);
+  }
+  __syncthreads();
+
+  // ---- pass E: inverse row transform (real part), plane-fit sums
+  const float scale_e = (float)(1.0 / ((double)N * (double)N));
+  double sz = 0.0, sxz = 0.0, syz = 0.0;
+  for (int r0 = warp * G; r0 < N; r0 += kSmemWarps * G) {
+    float2* rows = Zs + r0 * LDZ;
+    float2 hv[16];
+#pragma unroll
+    for (int t = 0; t < 16; ++t) {
+      const int idx = lane + 32 * t, g = idx / N, k = idx % N;
+      const float2* Gr = rows + g * LDZ;
+      hv[t] = (k == 0 || k == N / 2) ? make_float2(Gr[k].x, 0.f) : (k < N / 2 ? Gr[k] : cconj(Gr[N - k]));
+    }
+    __syncwarp();
+#pragma unroll
+    for (int t = 0; t < 16; ++t) {
+      const int idx = lane + 32 * t, g = idx / N, k = idx % N;
+      rows[g * LDZ + k] = hv[t];
+    }
+    __syncwarp();
+    warp_fft<N, 1>(rows, G, LDZ, 1, tw);
+#pragma unroll
+    for (int t = 0; t < 16; ++t) {
+      const int idx = lane + 32 * t, g = idx / N, j = idx % N;
+      const int i = r0 + g;
+      const float w = rows[g * LDZ + j].x * scale_e;
+      rows[g * LDZ + j] = make_float2(w, 0.f);
+      sz += (double)w;
+      sxz += (double)i * (double)w;
+      syz += (double)j * (double)w;
+    }
+  }
+  sz = block_sum_d(sz, red);
+  sxz = block_sum_d(sxz, red);
+  syz = block_sum_d(syz, red);
+  if (threadIdx.x == 0) {
+    const double n = (double)N, n2 = n * n;
+    const double s1 = n * (n - 1.0) / 2.0 * n;
+    const double s2 = (n - 1.0) * n * (2.0 * n - 1.0) / 6.0 * n;
+    const double sxy = (n * (n - 1.0) / 2.0) * (n * (n - 1.0) / 2.0);
+    double A[3][4] = {{s2, sxy, s1, sxz}, {sxy, s2, s1, syz}, {s1, s1, n2, sz}};
+    for (int c = 0; c < 3; ++c) {
+      int p = c;
+      for (int r2 = c + 1; r2 < 3; ++r2) if (fabs(A[r2][c]) > fabs(A[p][c])) p = r2;
+      if (p != c) for (int k = 0; k < 4; ++k) { double tmp = A[c][k]; A[c][k] = A[p][k]; A[p][k] = tmp; }
+      for (int r2 = 0; r2 < 3; ++r2) {
+        if (r2 == c) continue;
+        const double f = A[r2][c] / A[c][c];
+        for (int k = c; k < 4; ++k) A[r2][k] -= f * A[c][k];
+      }
+    }
+    const double c0 = A[0][3] / A[0][0], c1 = A[1][3] / A[1][1], c2 = A[2][3] / A[2][2];
+    s_coef[0] = c0; s_coef[1] = c1; s_coef[2] = c2;
+    s_coef[3] = (sz - c0 * s1 - c1 * s1 - c2 * n2) / n2;
+  }
+  __syncthreads();
+  const double pc0 = s_coef[0], pc1 = s_coef[1], pc2 = s_coef[2], mean = s_coef[3];
+  double sv = 0.0;
+  for (int t = threadIdx.x; t < N * N; t += blockDim.x) {
+    const int i = t / N, j = t - i * N;
+    const double v = (double)Zs[i * LDZ + j].x - (pc0 * i + pc1 * j + pc2) - mean;
+    sv += v * v;
+  }
+  sv = block_sum_d(sv, red);
+  const double sd = sqrt(sv / ((double)N * (double)N));
+  const double inv_sd = sd > 1e-12 ? 1.0 / sd : 1.0;
+
+  // ---- pass F: normalise, mask, forward row FFT
+  for (int r0 = warp * G; r0 < N; r0 += kSmemWarps * G) {
+    float2* rows = Zs + r0 * LDZ;
+#pragma unroll
+    for (int t = 0; t < 16; ++t) {
+      const int idx = lane + 32 * t, g = idx / N, j = idx % N;
+      const int i = r0 + g;
+      float f = (float)(((double)rows[g * LDZ + j].x - (pc0 * i + pc1 * j + pc2) - mean) * inv_sd);
+      if (P.mask != nullptr) f *= P.mask[i * N + j];
+      rows[g * LDZ + j] = make_float2(f, 0.f);
+    }
+    __syncwarp();
+    warp_fft<N, -1>(rows, G, LDZ, 1, tw);
+  }
+  __syncthreads();
+  // ---- pass G: forward column FFT
+  for (int c0 = warp * G; c0 < HC; c0 += kSmemWarps * G)
+    warp_fft<N, -1>(Zs + c0, min(G, HC - c0), 1, LDZ, tw);
+  __syncthreads();
+  // crop + pack + FSC, L2 norm, pre-shifted write
+  double ss = 0.0;
+  for (int t = threadIdx.x; t < nb * H; t += blockDim.x) {
+    const int r = t / H, c = t - r * H;
+    const int ky = r < nb / 2 ? r : r - nb;
+    float2 f;
+    if (c < nb / 2) f = Zs[((ky + N) % N) * LDZ + c];
+    else if (nb == N) f = Zs[((ky + N) % N) * LDZ + N / 2];
+    else f = cconj(Zs[((-ky + N) % N) * LDZ + nb / 2]);
+    f = cscale(f, P.fsc[t]);
+    ss += (double)f.x * f.x + (double)f.y * f.y;
+  }
+  ss = block_sum_d(ss, red);
+  const float inv_norm = (float)(1.0 / sqrt(ss));
+  float2* out = P.bank + (size_t)slot * nb * H;
+  for (int t = threadIdx.x; t < nb * H; t += blockDim.x) {
+    const int r = t / H, c = t - r * H;
+    const int ky = r < nb / 2 ? r : r - nb;
+    float2 f;
+    if (c < nb / 2) f = Zs[((ky + N) % N) * LDZ + c];
+    else if (nb == N) f = Zs[((ky + N) % N) * LDZ + N / 2];
+    else f = cconj(Zs[((-ky + N) % N) * LDZ + nb / 2]);
+    f = cscale(f, P.fsc[t]);
+    const int rs = (r + nb / 2) % nb, cs = (c + H / 2) % H;
+    out[(size_t)rs * H + cs] = cscale(f, inv_norm);
+  }
+  __syncthreads();
+}
+
+template <int N>
+__global__ void __launch_bounds__(kSmemThreads, 1) project_templates_smem(ProjParams P) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int LDZ = N + 1, L2 = N / 16, CPR = 16 / L2;
+  float2* Zs = reinterpret_cast<float2*>(smem_raw);
+  float2* stage = Zs + N * LDZ;
+  float2* s_tw = stage + kSmemWarps * CPR * 2 * N;
+  double* red = reinterpret_cast<double*>(s_tw + kMaxFftLen / 2);
+  double* s_coef = red + 32;
+  float* s_div = reinterpret_cast<float*>(s_coef + 8);
+  for (int t = threadIdx.x; t < kMaxFftLen / 2; t += blockDim.x) s_tw[t] = P.tw[t];
+  __syncthreads();
+  for (int b = blockIdx.x; b < P.n_build; b += gridDim.x) {
+    const int dir = P.dirs[b];
+    const int slot = P.out_slot ? P.out_slot[b] : dir;
+    build_one_smem<N>(P, dir, slot, Zs, stage, s_tw, s_div, red, s_coef);
+  }
+}
+
+}  // namespace
+
+size_t project_smem_bytes_fast(int N, int n_bins) {
+  const int L2 = N / 16, CPR = 16 / L2;
+  return (size_t)N * (N + 1) * sizeof(float2) + (size_t)kSmemWarps * CPR * 2 * N * sizeof(float2) +
+         (kMaxFftLen / 2) * sizeof(float2) + 40 * sizeof(double) + (size_t)(n_bins + 4) * sizeof(float);
+}
+
+template <int N>
+static cudaError_t launch_fast(const ProjParams& P, int grid, cudaStream_t st) {
+  const size_t smem = project_smem_bytes_fast(N, P.n_bins);
+  cudaError_t e = cudaFuncSetAttribute(project_templates_smem<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  project_templates_smem<N><<<grid, kSmemThreads, smem, st>>>(P);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_project_templates_fast(cudaStream_t st, const float2* spectrum, const float* rot,
+                                          const int* dirs, int n_build, const int* out_slot,
+                                          const float* mask, const float* fsc, const int* bin_list,
+                                          const int* bin_ptr, const float* bin_count, int n_bins,
+                                          const float2* tw, float2* bank, int grid, int N, int nb) {
+  if (n_build <= 0) return cudaSuccess;
+  ProjParams P;
+  P.spectrum = spectrum; P.rot = rot; P.dirs = dirs; P.n_build = n_build; P.mask = mask;
+  P.fsc = fsc; P.bin_list = bin_list; P.bin_ptr = bin_ptr; P.bin_count = bin_count;
+  P.n_bins = n_bins; P.tw = tw; P.bank = bank; P.out_slot = out_slot; P.scratch = nullptr;
+  P.scratch_stride = 0; P.N = N; P.nb = nb;
+  switch (N) {
+    case 32: return launch_fast<32>(P, grid, st);
+    case 64: return launch_fast<64>(P, grid, st);
+    case 128: return launch_fast<128>(P, grid, st);
+    default: return cudaErrorInvalidValue;
+  }
+}

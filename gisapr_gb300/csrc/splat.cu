@@ -21,6 +21,8 @@
 // expf(exponent)) where rp and Z*kn are doubles. The float64 products are
 // formed in float32 pairs (hi + lo) with an exact product error term, which
 // gives the same float result as the double product except at exact ties.
+#include <climits>
+
 #include "common.cuh"
 
 namespace {
@@ -376,4 +378,180 @@ extern "C" int gisapr_deposit_noalloc(void* stream, const float* xyz, const floa
   e = launch_splat_bricks(st, recs, n_atoms, volume, volume, nullptr, box, rp);
   if (e != cudaSuccess) return noalloc_fail(GISAPR_ERR_CUDA, std::string("splat_bricks: ") + cudaGetErrorString(e));
   return GISAPR_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Binned splat (the context entry points): 8^3 bricks, one thread per voxel.
+//
+// atoms_prepare_binned computes each atom's record as atoms_prepare does and
+// appends the atom's index to every 8^3 brick its clipped cube touches
+// (fixed capacity per brick; a brick whose list overflows walks every atom in
+// input order instead). The
+// splat CTA of a brick sorts its list by atom index, so every voxel still
+// sums its atoms in input order, and each thread adds the atoms covering its
+// voxel. Work is spread over box^3 threads instead of one thread per 16-voxel
+// column, which matters because atoms crowd the centre of the box.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int kBin = 8;
+
+__global__ void atoms_prepare_binned(const float* __restrict__ xyz, const float* __restrict__ numbers, int n,
+                                     int transform, const float* __restrict__ pivot,
+                                     const double* __restrict__ rot, const double* __restrict__ shift, int box,
+                                     int width, double apix, double kn, AtomRec* __restrict__ out,
+                                     int* __restrict__ counts, int* __restrict__ lists, int cap) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  // same record as atoms_prepare
+  float c[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
+  float q[3];
+  if (transform) {
+    double d[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) d[k] = (double)__fsub_rn(c[k], pivot[k]);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      double mm = d[0] * rot[0 * 3 + k];
+      mm = fma(d[1], rot[1 * 3 + k], mm);
+      mm = fma(d[2], rot[2 * 3 + k], mm);
+      q[k] = (float)pdb_8_3(mm + (double)pivot[k] + shift[k]);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) q[k] = c[k];
+  }
+  float p[3];
+  int lo[3], hi[3];
+  bool inside = true;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    p[k] = (float)((double)q[k] / apix + (double)(box / 2));
+    lo[k] = round_away_f64((double)__fsub_rn(p[k], (float)width));
+    hi[k] = round_away_f64((double)__fadd_rn(p[k], (float)width));
+    inside = inside && (lo[k] < box) && (hi[k] >= 0);
+    lo[k] = max(lo[k], 0);
+    hi[k] = min(hi[k], box - 1);
+  }
+  const float z = numbers[i];
+  const double zk = (double)z * kn;
+  float zk_hi = (float)zk, zk_lo = (float)(zk - (double)zk_hi);
+  const bool live = inside && z != 0.0f && isfinite(p[0]) && isfinite(p[1]) && isfinite(p[2]) &&
+                    hi[0] > lo[0] && hi[1] > lo[1] && hi[2] > lo[2];
+  if (!live) { zk_hi = 0.0f; zk_lo = 0.0f; }
+  AtomRec r;
+  r.px = p[0]; r.py = p[1]; r.pz = p[2];
+  r.lx = lo[0]; r.ly = lo[1]; r.lz = lo[2];
+  r.ux = hi[0]; r.uy = hi[1]; r.uz = hi[2];
+  r.zk_hi = zk_hi; r.zk_lo = zk_lo; r.pad = 0;
+  out[i] = r;
+  if (!live) return;
+  const int nb = (box + kBin - 1) / kBin;
+  for (int bz = lo[2] / kBin; bz <= (hi[2] - 1) / kBin; ++bz)
+    for (int by = lo[1] / kBin; by <= (hi[1] - 1) / kBin; ++by)
+      for (int bx = lo[0] / kBin; bx <= (hi[0] - 1) / kBin; ++bx) {
+        const int b = (bz * nb + by) * nb + bx;
+        const int slot = atomicAdd(counts + b, 1);
+        if (slot < cap) lists[(size_t)b * cap + slot] = i;
+      }
+}
+
+__global__ void __launch_bounds__(512)
+splat_binned(const AtomRec* __restrict__ atoms, int n_atoms, const int* __restrict__ counts,
+             const int* __restrict__ lists, int cap, const float* __restrict__ initial, float* __restrict__ out,
+             float* __restrict__ padded, int box, float rp_hi, float rp_lo) {
+  extern __shared__ int s_ids[];  // cap entries (power of two >= count for the sort)
+  __shared__ AtomRec s_rec[64];
+  const int nb = (box + kBin - 1) / kBin;
+  const int b = blockIdx.x;
+  const int bz = b / (nb * nb), by = (b / nb) % nb, bx = b % nb;
+  const int x = bx * kBin + (threadIdx.x & 7), y = by * kBin + ((threadIdx.x >> 3) & 7),
+            z = bz * kBin + (threadIdx.x >> 6);
+  const bool ok = x < box && y < box && z < box;
+  const size_t vi = ((size_t)z * box + y) * box + x;
+  float acc = (ok && initial != nullptr) ? initial[vi] : 0.0f;
+  // A brick whose list overflowed walks every atom in input order instead.
+  const bool full_scan = counts[b] > cap;
+  const int cnt = full_scan ? n_atoms : counts[b];
+  // sort size: the next power of two >= cnt (cnt <= cap here); 0 in full-scan mode
+  int pw = 0;
+  if (!full_scan) {
+    pw = 1;
+    while (pw < cnt) pw <<= 1;
+  }
+  for (int t = threadIdx.x; t < pw; t += blockDim.x) s_ids[t] = t < cnt ? lists[(size_t)b * cap + t] : INT_MAX;
+  __syncthreads();
+  // bitonic sort: the atomics appended in arbitrary order
+  for (int k = 2; !full_scan && k <= pw; k <<= 1)
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int t = threadIdx.x; t < pw; t += blockDim.x) {
+        const int o = t ^ j;
+        if (o > t) {
+          const int a = s_ids[t], c = s_ids[o];
+          const bool up = (t & k) == 0;
+          if ((a > c) == up) { s_ids[t] = c; s_ids[o] = a; }
+        }
+      }
+      __syncthreads();
+    }
+  const float fx = (float)x, fy = (float)y, fz = (float)z;
+  for (int base = 0; base < cnt; base += 64) {
+    const int nchunk = min(64, cnt - base);
+    __syncthreads();
+    if (threadIdx.x < nchunk) s_rec[threadIdx.x] = atoms[full_scan ? base + threadIdx.x : s_ids[base + threadIdx.x]];
+    __syncthreads();
+    for (int t = 0; t < nchunk; ++t) {
+      const AtomRec a = s_rec[t];
+      if ((a.zk_hi == 0.0f && a.zk_lo == 0.0f) || x < a.lx || x >= a.ux || y < a.ly || y >= a.uy || z < a.lz ||
+          z >= a.uz)
+        continue;
+      const float dx = __fsub_rn(fx, a.px), dy = __fsub_rn(fy, a.py), dz = __fsub_rn(fz, a.pz);
+      const float rr = sqrtf(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+      const float ph = __fmul_rn(rr, rp_hi);
+      const float pe = __fmaf_rn(rr, rp_hi, -ph);
+      const float expo = -__fadd_rn(ph, __fmaf_rn(rr, rp_lo, pe));
+      const float e = expf(expo);
+      const float vh = __fmul_rn(a.zk_hi, e);
+      const float ve = __fmaf_rn(a.zk_hi, e, -vh);
+      acc = __fadd_rn(acc, __fadd_rn(vh, __fmaf_rn(a.zk_lo, e, ve)));
+    }
+  }
+  if (!ok) return;
+  if (out != nullptr) out[vi] = acc;
+  if (padded != nullptr) {
+    const int m = 2 * box, half = box / 2;
+    const float fzv = fftfreq_shifted_f32(z + half, m), fyv = fftfreq_shifted_f32(y + half, m),
+                fxv = fftfreq_shifted_f32(x + half, m);
+    const float w = sinc2_f32(__fmul_rn(fzv, fzv), __fmul_rn(fyv, fyv), __fmul_rn(fxv, fxv));
+    const int zs = (z + 3 * half) % m, ys = (y + 3 * half) % m, xs = (x + 3 * half) % m;
+    padded[((size_t)zs * m + ys) * m + xs] = __fmul_rn(acc, w);
+  }
+}
+
+}  // namespace
+
+int splat_bin_cap() { return 1024; }
+int splat_bin_count(int box) {
+  const int nb = (box + kBin - 1) / kBin;
+  return nb * nb * nb;
+}
+
+cudaError_t launch_splat_binned(cudaStream_t st, const float* xyz, const float* numbers, int n, int transform,
+                                const float* pivot, const double* rot, const double* shift, const float* initial,
+                                float* out, float* padded, int box, int width, double apix, double rp, double kn,
+                                void* atom_recs, int* counts, int* lists) {
+  const int nbricks = splat_bin_count(box), cap = splat_bin_cap();
+  cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(int) * nbricks, st);
+  if (e != cudaSuccess) return e;
+  if (n > 0) {
+    atoms_prepare_binned<<<(n + 255) / 256, 256, 0, st>>>(xyz, numbers, n, transform, pivot, rot, shift, box,
+                                                           width, apix, kn, (AtomRec*)atom_recs, counts, lists,
+                                                           cap);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  const float rp_hi = (float)rp, rp_lo = (float)(rp - (double)rp_hi);
+  splat_binned<<<nbricks, 512, cap * sizeof(int), st>>>((const AtomRec*)atom_recs, n, counts, lists, cap,
+                                                       initial, out, padded, box, rp_hi, rp_lo);
+  return cudaGetLastError();
 }

@@ -69,6 +69,18 @@ def test_deposit_is_deterministic_and_edge_atoms(golden32):
     assert float(empty.abs().sum()) == 0.0
 
 
+def test_deposit_crowded_brick_falls_back_in_order():
+    """More atoms touch one 8^3 brick than its list holds: that brick walks
+    every atom in input order and the density still matches."""
+    rng = np.random.default_rng(7)
+    xyz = (rng.normal(size=(1500, 3)) * 1.5).astype(np.float32)
+    z = rng.choice(np.asarray([6, 7, 8, 16], np.float32), size=1500)
+    a = density_from_coords(xyz, z, 32, 3.0, 6.0, device=DEV).cpu().numpy()
+    b = density_from_coords(xyz, z, 32, 3.0, 6.0, device=DEV).cpu().numpy()
+    np.testing.assert_array_equal(a, b)
+    assert rrms(a, O.splat_density(xyz, z, 32, 3.0, 6.0)) < DENSITY_RRMS
+
+
 def test_deposit_box64_slab(golden64):
     g = golden64
     spec = syn.WORKLOADS["box64_200p"]

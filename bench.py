@@ -50,6 +50,7 @@ def parse_args():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=48, help="particles and templates in the CPU sample")
+    ap.add_argument("--batch", type=int, default=64, help="candidates per batched generation (0: skip)")
     return ap.parse_args()
 
 
@@ -108,11 +109,21 @@ class ClockSampler:
 # workload
 # ---------------------------------------------------------------------------
 
-def make_workload(name: str, seed: int, device: str, particles: int = 0):
+BATCH_CHAINS = (1500, 3000, 6000)  # moving-chain sizes mixed in a batched generation
+
+
+def make_workload(name: str, seed: int, device: str, particles: int = 0, with_models: bool = False):
+    """Seeded job data; with_models also returns moving-chain variants of
+    1,500 / 3,000 / 6,000 atoms sharing the job's fixed context (the job's
+    particles come from the 3,000-atom model)."""
     from gisapr_gb300 import synthetic as syn
     spec = syn.WORKLOADS[name]
-    job = syn.make_job(spec, seed=seed, device=device, n_particles=particles or None)
-    return spec, job
+    if not with_models:
+        job = syn.make_job(spec, seed=seed, device=device, n_particles=particles or None)
+        return spec, job
+    models = syn.make_models_shared_fixed(BATCH_CHAINS, spec.n_fixed_atoms, seed)
+    job = syn.make_job(spec, seed=seed, device=device, n_particles=particles or None, model=models[1])
+    return spec, job, models
 
 
 def job_records(job):
@@ -212,7 +223,8 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
     device = torch.device("cuda", local_rank)
     torch.cuda.set_device(device)
     t_setup = time.perf_counter()
-    spec, data = make_workload(args.workload, args.seed + rank, str(device), args.particles)
+    spec, data, models = make_workload(args.workload, args.seed + rank, str(device), args.particles,
+                                       with_models=True)
     t_data = time.perf_counter() - t_setup
     cfg = JobConfig(box=spec.box, apix=spec.apix, crop=spec.crop, psi_step=spec.psi_step,
                     local_range=spec.local_range, mask_edge=spec.mask_edge, kk=spec.kk)
@@ -270,10 +282,70 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
     barrier()
     e2e_elapsed = e0.elapsed_time(e1) / 1e3
 
-    times = torch.tensor([elapsed, e2e_elapsed], dtype=torch.float64, device=device)
+    # ---- batched generations: args.batch candidates per step, one CUDA graph
+    batched = None
+    b_elapsed = 0.0
+    if args.batch > 0:
+        from gisapr_gb300.engine import BatchScoringJob
+        from gisapr_gb300.pdb2mrc import MovedChainDensity
+        dens = [MovedChainDensity(m.pdb_text, "A", spec.box, spec.apix, spec.res, device, from_text=True)
+                for m in models]
+        model_of = [i % len(dens) for i in range(args.batch)]
+        bj = BatchScoringJob(job, args.batch, models=dens, model_of=model_of)
+        gen = [syn.candidate_poses(args.batch, args.seed + 1000 + 31 * k + rank, 5.0, 3.0) for k in range(K + W)]
+        for k in range(W):
+            bj.score_batch(gen[k])
+        barrier()
+        torch.cuda.synchronize(device)
+        b0 = torch.cuda.Event(enable_timing=True)
+        b1 = torch.cuda.Event(enable_timing=True)
+        b_steps = []
+        with torch.cuda.stream(bj.stream):
+            b0.record()
+            for k in range(K):
+                bj.set_poses(gen[W + k])
+                ev = torch.cuda.Event(enable_timing=True)
+                ev.record()
+                b_steps.append(ev)
+                bj.run()
+            b1.record()
+        torch.cuda.synchronize(device)
+        barrier()
+        b_elapsed = b0.elapsed_time(b1) / 1e3
+        b_steps.append(b1)
+        b_lat = sorted(b_steps[i].elapsed_time(b_steps[i + 1]) for i in range(K))
+        # end to end: poses from host, scores and per-particle peaks back, every generation
+        bpeaks_host = torch.empty(tuple(bj.peak.shape), dtype=torch.float32).pin_memory()
+        e2 = torch.cuda.Event(enable_timing=True)
+        e3 = torch.cuda.Event(enable_timing=True)
+        e2.record()
+        for k in range(K):
+            bj.score_batch(gen[W + k])
+            bpeaks_host.copy_(bj.peak, non_blocking=True)
+        e3.record()
+        torch.cuda.synchronize(device)
+        b_e2e = e2.elapsed_time(e3) / 1e3
+        batched = {"candidates_per_step": args.batch, "moving_chain_atoms": [m.n_moving for m in dens],
+                   "graph": bj.graph is not None, "ms_per_step": b_elapsed / K * 1e3,
+                   "latency_ms": {"p50": b_lat[len(b_lat) // 2],
+                                  "p99": b_lat[min(len(b_lat) - 1, int(math.ceil(0.99 * len(b_lat))) - 1)]},
+                   "e2e_elapsed_s": b_e2e, "e2e_h2d_bytes_per_step": 12 * 8 * args.batch,
+                   "e2e_d2h_bytes_per_step": 8 * args.batch + 4 * args.batch * len(job.records),
+                   "gpu_launches": bj.launches_per_batch() * K}
+
+    times = torch.tensor([elapsed, e2e_elapsed, b_elapsed, batched["e2e_elapsed_s"] if batched else 0.0],
+                         dtype=torch.float64, device=device)
     if world > 1:
         torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
     elapsed, e2e_elapsed = float(times[0]), float(times[1])
+    if batched is not None:
+        batched["value"] = world * K * args.batch / float(times[2])
+        batched["unit"] = UNIT
+        batched["e2e"] = {"value": world * K * args.batch / float(times[3]), "unit": UNIT,
+                          "h2d_bytes_per_step": batched.pop("e2e_h2d_bytes_per_step"),
+                          "d2h_bytes_per_step": batched.pop("e2e_d2h_bytes_per_step")}
+        batched.pop("e2e_elapsed_s")
+        batched["vs_plain_single"] = batched["value"] / (world * K / elapsed)
     if rank != 0:
         return
     value = world * K / elapsed
@@ -312,6 +384,8 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
         "setup_s": {"synthetic_data": t_data, "job": job.setup_s},
         "score_sample": scores[0],
     }
+    if batched is not None:
+        line["batched"] = batched
     if world == 1 and not args.no_cpu_baseline:
         cb = cpu_baseline(spec, data, poses[W], args.cpu_sample)
         line["cpu_baseline"] = {

@@ -32,6 +32,9 @@ SIGNATURES = {
     "gisapr_correlate": [_p, _p, _p, _p, _p, _p, _i, _i, _i, _i, _p, _p, _p],
     "gisapr_particle_results": [_p, _p, _p, _p, _p, _i, _i, _p, _p, _p, _p, _p, _p],
     "gisapr_score_sum": [_p, _p, _p, _i, _p],
+    "gisapr_correlate_batch": [_p, _p, _p, C.c_longlong, _i, _p, _p, _p, _i, _i, _i, _i, _i, _p, _p, _p],
+    "gisapr_particle_results_batch": [_p, _p, _p, _p, _p, _i, _i, _i, _p, _p, _p, _p, _p, _p],
+    "gisapr_score_sum_batch": [_p, _p, _p, _i, _i, _p],
 }
 
 _lib = None

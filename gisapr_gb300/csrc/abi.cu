@@ -48,10 +48,10 @@ int correlate_cluster_size(int n);
 size_t correlate_smem_bytes(int n, int n_psi, int crop);
 cudaError_t launch_correlate_plain(cudaStream_t, const float2*, const float2*, const int*,
                                    const int*, int, int, int, int, const float2*, const float2*,
-                                   float*, int*, int*);
+                                   float*, int*, int*, int, long long, int);
 cudaError_t launch_particle_results(cudaStream_t, const int*, const float*, const int*, const int*,
-                                    int, int, int*, int*, float*, int*, int*, float*);
-cudaError_t launch_score_sum(cudaStream_t, const int*, const float*, int, double*);
+                                    int, int, int*, int*, float*, int*, int*, float*, int);
+cudaError_t launch_score_sum(cudaStream_t, const int*, const float*, int, double*, int);
 
 namespace {
 
@@ -449,6 +449,36 @@ int gisapr_prepare_particles(gisapr_ctx ctx, void* stream, const float* images, 
   return GISAPR_OK;
 }
 
+int gisapr_correlate_batch(gisapr_ctx ctx, void* stream, const float* bank, long long bank_stride, int n_cand,
+                           const float* stack, const int* local_ptr, const int* local_idx, int n_particles,
+                           int nnz, int n_psi, int n, int crop, float* out_score, int* out_y, int* out_x) {
+  if (!ctx) return fail(GISAPR_ERR_ARGUMENT, "context is NULL");
+  if (n_particles < 0 || n_psi <= 0 || n_cand < 0)
+    return fail(GISAPR_ERR_ARGUMENT, "n_particles < 0, n_psi <= 0 or n_cand < 0");
+  if (n_particles == 0 || n_cand == 0) return GISAPR_OK;
+  if (!bank || !stack || !local_ptr || !local_idx || !out_score || !out_y || !out_x)
+    return fail(GISAPR_ERR_ARGUMENT, "a required pointer is NULL");
+  if (n_cand > 1 && bank_stride <= 0) return fail(GISAPR_ERR_ARGUMENT, "bank_stride must be positive");
+  if (n < 32 || n > 256 || n % 16 != 0)
+    return fail(GISAPR_ERR_UNSUPPORTED, "correlation size must be a multiple of 16 in [32, 256]");
+  if (crop < 2 || crop > 16 || crop % 2 != 0 || crop > n)
+    return fail(GISAPR_ERR_UNSUPPORTED, "crop must be even, 2..16 and <= n");
+  const size_t smem = correlate_smem_bytes(n, n_psi, crop);
+  if (smem > 227 * 1024)
+    return fail(GISAPR_ERR_UNSUPPORTED, "too many psi angles for the shared-memory particle slice");
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  CorrTables t;
+  rc = get_corr_tables(ctx, n, crop, &t);
+  if (rc) return rc;
+  if (nnz < 0) return fail(GISAPR_ERR_ARGUMENT, "nnz < 0");
+  GISAPR_CHECK_CUDA(launch_correlate_plain((cudaStream_t)stream, (const float2*)bank, (const float2*)stack,
+                                           local_ptr, local_idx, n_particles, n_psi, n, crop, t.outer, t.col,
+                                           out_score, out_y, out_x, n_cand, bank_stride, nnz),
+                    "correlate");
+  return GISAPR_OK;
+}
+
 int gisapr_correlate(gisapr_ctx ctx, void* stream, const float* bank, const float* stack,
                      const int* local_ptr, const int* local_idx, int n_particles, int n_psi, int n,
                      int crop, float* out_score, int* out_y, int* out_x) {
@@ -471,30 +501,45 @@ int gisapr_correlate(gisapr_ctx ctx, void* stream, const float* bank, const floa
   if (rc) return rc;
   GISAPR_CHECK_CUDA(launch_correlate_plain((cudaStream_t)stream, (const float2*)bank, (const float2*)stack,
                                            local_ptr, local_idx, n_particles, n_psi, n, crop, t.outer, t.col,
-                                           out_score, out_y, out_x),
+                                           out_score, out_y, out_x, 1, 0, 0),
                     "correlate");
+  return GISAPR_OK;
+}
+
+int gisapr_particle_results_batch(void* stream, const int* local_ptr, const float* score, const int* ys,
+                                  const int* xs, int n_particles, int n_psi, int n_cand, int* best_entry,
+                                  int* best_psi, float* peak, int* peak_y, int* peak_x, float* zscore) {
+  if (n_particles < 0 || n_psi <= 0 || n_cand < 0)
+    return fail(GISAPR_ERR_ARGUMENT, "n_particles < 0, n_psi <= 0 or n_cand < 0");
+  if (n_particles == 0 || n_cand == 0) return GISAPR_OK;
+  if (!local_ptr || !score || !ys || !xs || !best_entry || !best_psi || !peak || !peak_y || !peak_x ||
+      !zscore)
+    return fail(GISAPR_ERR_ARGUMENT, "a required pointer is NULL");
+  if (n_cand > 65535) return fail(GISAPR_ERR_ARGUMENT, "at most 65535 candidates per call");
+  GISAPR_CHECK_CUDA(launch_particle_results((cudaStream_t)stream, local_ptr, score, ys, xs, n_particles, n_psi,
+                                            best_entry, best_psi, peak, peak_y, peak_x, zscore, n_cand),
+                    "particle_results");
   return GISAPR_OK;
 }
 
 int gisapr_particle_results(void* stream, const int* local_ptr, const float* score, const int* ys,
                             const int* xs, int n_particles, int n_psi, int* best_entry, int* best_psi,
                             float* peak, int* peak_y, int* peak_x, float* zscore) {
-  if (n_particles < 0 || n_psi <= 0) return fail(GISAPR_ERR_ARGUMENT, "n_particles < 0 or n_psi <= 0");
-  if (n_particles == 0) return GISAPR_OK;
-  if (!local_ptr || !score || !ys || !xs || !best_entry || !best_psi || !peak || !peak_y || !peak_x ||
-      !zscore)
-    return fail(GISAPR_ERR_ARGUMENT, "a required pointer is NULL");
-  GISAPR_CHECK_CUDA(launch_particle_results((cudaStream_t)stream, local_ptr, score, ys, xs, n_particles, n_psi,
-                                            best_entry, best_psi, peak, peak_y, peak_x, zscore),
-                    "particle_results");
+  return gisapr_particle_results_batch(stream, local_ptr, score, ys, xs, n_particles, n_psi, 1, best_entry,
+                                       best_psi, peak, peak_y, peak_x, zscore);
+}
+
+int gisapr_score_sum_batch(void* stream, const int* local_ptr, const float* peak, int n_particles, int n_cand,
+                           double* out) {
+  if (n_particles < 0 || n_cand < 0 || !out) return fail(GISAPR_ERR_ARGUMENT, "bad arguments");
+  if (n_particles > 0 && (!local_ptr || !peak)) return fail(GISAPR_ERR_ARGUMENT, "a required pointer is NULL");
+  GISAPR_CHECK_CUDA(launch_score_sum((cudaStream_t)stream, local_ptr, peak, n_particles, out, n_cand),
+                    "score_sum");
   return GISAPR_OK;
 }
 
 int gisapr_score_sum(void* stream, const int* local_ptr, const float* peak, int n_particles, double* out) {
-  if (n_particles < 0 || !out) return fail(GISAPR_ERR_ARGUMENT, "bad arguments");
-  if (n_particles > 0 && (!local_ptr || !peak)) return fail(GISAPR_ERR_ARGUMENT, "a required pointer is NULL");
-  GISAPR_CHECK_CUDA(launch_score_sum((cudaStream_t)stream, local_ptr, peak, n_particles, out), "score_sum");
-  return GISAPR_OK;
+  return gisapr_score_sum_batch(stream, local_ptr, peak, n_particles, 1, out);
 }
 
 }  // extern "C"

@@ -35,10 +35,13 @@ struct CorrParams {
   const int* local_idx;    // template index per entry
   const float2* tw_outer;  // [M][C]  exp(+2 pi i q y / n)
   const float2* tw_col;    // [H][C]  w_c exp(+2 pi i c x / n)
-  float* out_score;        // [nnz][n_psi]
+  float* out_score;        // [n_cand][nnz][n_psi]
   int* out_y;
   int* out_x;
   int n_particles, n_psi, n, cluster;
+  int n_cand;              // candidates sharing the particle spectra
+  long long bank_stride;   // complex elements between candidates' banks
+  int nnz;                 // entries of the CSR (output stride per candidate)
 };
 
 __host__ __device__ inline int col_lo(int H, int K, int r) {
@@ -77,6 +80,9 @@ __global__ void __launch_bounds__(kThreads) correlate_plain(CorrParams P) {
   }
   __syncthreads();
 
+  for (int cand = 0; cand < P.n_cand; ++cand) {
+  const float2* bank = P.bank + (size_t)cand * (size_t)P.bank_stride;
+  const size_t out_base = (size_t)cand * P.nnz * n_psi;
   for (int sg = 0; sg < d; sg += kMaxLocal) {
     const int dsg = min(kMaxLocal, d - sg);
     for (int g0 = 0; g0 < dsg; g0 += kGroup) {
@@ -88,7 +94,7 @@ __global__ void __launch_bounds__(kThreads) correlate_plain(CorrParams P) {
         const int gp = t / cw;
         const int psi = gp % n_psi, g = gp / n_psi;
         const int tmpl = P.local_idx[e0 + sg + g0 + g];
-        const float2* T = P.bank + (size_t)tmpl * n * H + clo + cl;
+        const float2* T = bank + (size_t)tmpl * n * H + clo + cl;
         const float2* Pp = Pq + (size_t)psi * n * cwmax + cl;
         float2 Z[C];
 #pragma unroll
@@ -154,7 +160,7 @@ __global__ void __launch_bounds__(kThreads) correlate_plain(CorrParams P) {
         }
         if (lane == 0) {
           const int a = sg + mp / n_psi, psi = mp % n_psi;
-          const size_t o = (size_t)(e0 + a) * n_psi + psi;
+          const size_t o = out_base + (size_t)(e0 + a) * n_psi + psi;
           P.out_score[o] = best * 1024.0f;
           P.out_y[o] = bi / C;
           P.out_x[o] = bi % C;
@@ -162,6 +168,7 @@ __global__ void __launch_bounds__(kThreads) correlate_plain(CorrParams P) {
       }
     }
     cluster.sync();
+  }
   }
 }
 
@@ -174,6 +181,12 @@ __global__ void particle_results(const int* __restrict__ local_ptr, const float*
                                  int* __restrict__ peak_x, float* __restrict__ zscore) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= n_particles) return;
+  {  // candidate blockIdx.y: its scores follow the previous candidates'
+    const int nnz = local_ptr[n_particles];
+    const size_t so = (size_t)blockIdx.y * nnz * n_psi, po = (size_t)blockIdx.y * n_particles;
+    score += so; ys += so; xs += so;
+    best_entry += po; best_psi += po; peak += po; peak_y += po; peak_x += po; zscore += po;
+  }
   const int e0 = local_ptr[warp], cnt = (local_ptr[warp + 1] - e0) * n_psi;
   if (cnt <= 0) {
     if (lane == 0) {
@@ -220,6 +233,8 @@ __global__ void particle_results(const int* __restrict__ local_ptr, const float*
 __global__ void score_sum(const int* __restrict__ local_ptr, const float* __restrict__ peak,
                           int n_particles, double* __restrict__ out) {
   __shared__ double red[32];
+  peak += (size_t)blockIdx.x * n_particles;  // candidate blockIdx.x
+  out += blockIdx.x;
   double acc = 0.0;
   for (int p = threadIdx.x; p < n_particles; p += blockDim.x)
     if (local_ptr[p + 1] > local_ptr[p]) acc += exp((double)peak[p] / 1024.0);
@@ -246,12 +261,12 @@ size_t correlate_smem_bytes(int n, int n_psi, int crop) {
 
 template <int C>
 static cudaError_t launch_c(const CorrParams& P, size_t smem, cudaStream_t st) {
-  cudaError_t e = cudaFuncSetAttribute(correlate_plain<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
-  if (e != cudaSuccess) return e;
-  if (P.cluster > 1) {
-    e = cudaFuncSetAttribute(correlate_plain<C>, cudaFuncAttributeNonPortableClusterSizeAllowed, 0);
-    (void)e;
+  static size_t set_smem = 0;  // attribute set once per size, never inside a stream capture
+  if (set_smem < smem) {
+    cudaError_t e = cudaFuncSetAttribute(correlate_plain<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    set_smem = smem;
   }
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(P.n_particles * P.cluster));
@@ -271,9 +286,11 @@ static cudaError_t launch_c(const CorrParams& P, size_t smem, cudaStream_t st) {
 cudaError_t launch_correlate_plain(cudaStream_t st, const float2* bank, const float2* stack,
                                    const int* local_ptr, const int* local_idx, int n_particles,
                                    int n_psi, int n, int crop, const float2* tw_outer,
-                                   const float2* tw_col, float* out_score, int* out_y, int* out_x) {
-  if (n_particles <= 0) return cudaSuccess;
+                                   const float2* tw_col, float* out_score, int* out_y, int* out_x,
+                                   int n_cand, long long bank_stride, int nnz) {
+  if (n_particles <= 0 || n_cand <= 0) return cudaSuccess;
   CorrParams P;
+  P.n_cand = n_cand; P.bank_stride = bank_stride; P.nnz = nnz;
   P.bank = bank; P.stack = stack; P.local_ptr = local_ptr; P.local_idx = local_idx;
   P.tw_outer = tw_outer; P.tw_col = tw_col; P.out_score = out_score; P.out_y = out_y;
   P.out_x = out_x; P.n_particles = n_particles; P.n_psi = n_psi; P.n = n;
@@ -295,16 +312,17 @@ cudaError_t launch_correlate_plain(cudaStream_t st, const float2* bank, const fl
 cudaError_t launch_particle_results(cudaStream_t st, const int* local_ptr, const float* score,
                                     const int* ys, const int* xs, int n_particles, int n_psi,
                                     int* best_entry, int* best_psi, float* peak, int* peak_y,
-                                    int* peak_x, float* zscore) {
-  if (n_particles <= 0) return cudaSuccess;
+                                    int* peak_x, float* zscore, int n_cand) {
+  if (n_particles <= 0 || n_cand <= 0) return cudaSuccess;
   const int threads = 256, warps = threads / 32;
-  particle_results<<<(n_particles + warps - 1) / warps, threads, 0, st>>>(
+  particle_results<<<dim3((n_particles + warps - 1) / warps, n_cand), threads, 0, st>>>(
       local_ptr, score, ys, xs, n_particles, n_psi, best_entry, best_psi, peak, peak_y, peak_x, zscore);
   return cudaGetLastError();
 }
 
 cudaError_t launch_score_sum(cudaStream_t st, const int* local_ptr, const float* peak, int n_particles,
-                             double* out) {
-  score_sum<<<1, 1024, 0, st>>>(local_ptr, peak, n_particles, out);
+                             double* out, int n_cand) {
+  if (n_cand <= 0) return cudaSuccess;
+  score_sum<<<n_cand, 1024, 0, st>>>(local_ptr, peak, n_particles, out);
   return cudaGetLastError();
 }

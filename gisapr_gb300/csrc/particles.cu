@@ -205,9 +205,13 @@ cudaError_t launch_prepare_particles(cudaStream_t st, const float* images, int n
   P.ctf = ctf; P.out = out; P.scratch = scratch; P.scratch_stride = prepare_scratch_elems(N, nb);
   P.tw = tw; P.n = n; P.n_psi = n_psi; P.N = N; P.nb = nb;
   const size_t smem = prepare_smem_bytes(N);
-  cudaError_t e = cudaFuncSetAttribute(prepare_particles, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
-  if (e != cudaSuccess) return e;
+  static size_t set_smem = 0;
+  if (set_smem < smem) {
+    cudaError_t e = cudaFuncSetAttribute(prepare_particles, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    set_smem = smem;
+  }
   prepare_particles<<<grid, kThreads, smem, st>>>(P);
   return cudaGetLastError();
 }

@@ -428,9 +428,13 @@ cudaError_t launch_project_templates(cudaStream_t st, const float2* spectrum, co
   P.n_bins = n_bins; P.tw = tw; P.bank = bank; P.out_slot = out_slot; P.scratch = scratch;
   P.scratch_stride = project_scratch_elems(N, nb); P.N = N; P.nb = nb;
   const size_t smem = project_smem_bytes(N, n_bins);
-  cudaError_t e = cudaFuncSetAttribute(project_templates, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
-  if (e != cudaSuccess) return e;
+  static size_t set_smem = 0;
+  if (set_smem < smem) {
+    cudaError_t e = cudaFuncSetAttribute(project_templates, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    set_smem = smem;
+  }
   project_templates<<<grid, kThreads, smem, st>>>(P);
   return cudaGetLastError();
 }
@@ -448,28 +452,101 @@ cudaError_t launch_project_templates(cudaStream_t st, const float2* spectrum, co
 // ===========================================================================
 namespace {
 
-constexpr int kSmemThreads = 512;
+constexpr int kSmemThreads = 256;
 constexpr int kSmemWarps = kSmemThreads / 32;
 
-// In-place four-step FFT of ``nlines`` (<= 32 / (N/16)) lines starting at
-// ``buf``; line l, element k at buf[l * ls + k * es]. Natural order in and out.
-template <int N, int DIR>
-__device__ __forceinline__ void warp_fft(float2* buf, int nlines, int ls, int es, const float2* tw) {
+// Row stride (complex elements) of the padded shared-memory plane: holds the
+// N + 1 columns plus one spare slot per 8, chosen by a bank-conflict search.
+__host__ __device__ constexpr int plane_ld(int N) { return N == 128 ? 150 : (N == 64 ? 74 : 38); }
+__host__ __device__ constexpr int plane_rows(int N) { return N + N / 8; }
+
+// Trilinear sample at the slice point's voxel coordinates (grid_sample's
+// normalise/un-normalise pair with align_corners=True is the identity, so
+// the coordinates are used directly, clamped for border padding). Corners
+// past the last voxel carry weight 0 and are read clamped.
+template <int N>
+__device__ __forceinline__ float2 sample_slice(const float2* __restrict__ vol, float cz, float cy, float cx) {
+  constexpr int m = 2 * N, W = N + 1;
+  const float pz = fminf((float)(m - 1), fmaxf(cz, 0.0f));
+  const float py = fminf((float)(m - 1), fmaxf(cy, 0.0f));
+  const float px = fminf((float)(W - 1), fmaxf(cx, 0.0f));
+  const float fz = floorf(pz), fy = floorf(py), fx = floorf(px);
+  const int z0 = (int)fz, y0 = (int)fy, x0 = (int)fx;
+  const int z1 = min(z0 + 1, m - 1), y1 = min(y0 + 1, m - 1), x1 = min(x0 + 1, W - 1);
+  const float wz1 = __fsub_rn(pz, fz), wy1 = __fsub_rn(py, fy), wx1 = __fsub_rn(px, fx);
+  const float wz0 = __fsub_rn(fz + 1.0f, pz), wy0 = __fsub_rn(fy + 1.0f, py), wx0 = __fsub_rn(fx + 1.0f, px);
+  // storage is unshifted along z and y: stored index = (i + N) mod 2N
+  const int zs0 = z0 < N ? z0 + N : z0 - N, zs1 = z1 < N ? z1 + N : z1 - N;
+  const int ys0 = y0 < N ? y0 + N : y0 - N, ys1 = y1 < N ? y1 + N : y1 - N;
+  const float2* r00 = vol + (zs0 * m + ys0) * W;
+  const float2* r01 = vol + (zs0 * m + ys1) * W;
+  const float2* r10 = vol + (zs1 * m + ys0) * W;
+  const float2* r11 = vol + (zs1 * m + ys1) * W;
+  const float2 v000 = __ldg(r00 + x0), v001 = __ldg(r00 + x1), v010 = __ldg(r01 + x0), v011 = __ldg(r01 + x1);
+  const float2 v100 = __ldg(r10 + x0), v101 = __ldg(r10 + x1), v110 = __ldg(r11 + x0), v111 = __ldg(r11 + x1);
+  const float w000 = __fmul_rn(__fmul_rn(wx0, wy0), wz0), w001 = __fmul_rn(__fmul_rn(wx1, wy0), wz0);
+  const float w010 = __fmul_rn(__fmul_rn(wx0, wy1), wz0), w011 = __fmul_rn(__fmul_rn(wx1, wy1), wz0);
+  const float w100 = __fmul_rn(__fmul_rn(wx0, wy0), wz1), w101 = __fmul_rn(__fmul_rn(wx1, wy0), wz1);
+  const float w110 = __fmul_rn(__fmul_rn(wx0, wy1), wz1), w111 = __fmul_rn(__fmul_rn(wx1, wy1), wz1);
+  float2 a;
+  a.x = v000.x * w000; a.y = v000.y * w000;
+  a.x = fmaf(v001.x, w001, a.x); a.y = fmaf(v001.y, w001, a.y);
+  a.x = fmaf(v010.x, w010, a.x); a.y = fmaf(v010.y, w010, a.y);
+  a.x = fmaf(v011.x, w011, a.x); a.y = fmaf(v011.y, w011, a.y);
+  a.x = fmaf(v100.x, w100, a.x); a.y = fmaf(v100.y, w100, a.y);
+  a.x = fmaf(v101.x, w101, a.x); a.y = fmaf(v101.y, w101, a.y);
+  a.x = fmaf(v110.x, w110, a.x); a.y = fmaf(v110.y, w110, a.y);
+  a.x = fmaf(v111.x, w111, a.x); a.y = fmaf(v111.y, w111, a.y);
+  return a;
+}
+
+// Padded plane layout: one spare slot after every 8 elements along both rows
+// and columns, row stride plane_ld(N). With it the four-step loads and stores
+// of row and column passes touch each 8-byte bank at most twice (three times
+// for two of the six patterns) per warp access.
+template <int N>
+struct Plane {
+  float2* p;
+  __device__ __forceinline__ int off(int r, int c) const { return (r + (r >> 3)) * plane_ld(N) + c + (c >> 3); }
+  __device__ __forceinline__ float2& operator()(int r, int c) const { return p[off(r, c)]; }
+};
+
+// Line accessors for warp_fft: element k of line g.
+template <int N>
+struct RowLines {  // lines are plane rows r0 + g
+  Plane<N> pl; int r0;
+  __device__ __forceinline__ float2& at(int g, int k) const { return pl(r0 + g, k); }
+};
+template <int N>
+struct ColLines {  // lines are plane columns c0 + g
+  Plane<N> pl; int c0;
+  __device__ __forceinline__ float2& at(int g, int k) const { return pl(k, c0 + g); }
+};
+template <int N>
+struct StageLines {  // staging lines of one warp, same padding along the line
+  float2* p;
+  __device__ __forceinline__ float2& at(int g, int k) const { return p[g * plane_ld(N) + k + (k >> 3)]; }
+};
+
+// In-place four-step FFT of ``nlines`` (<= 32 / (N/16)) lines, natural order
+// in and out: a 16-point register codelet over n1, twiddles, then N/16-point
+// codelets over n2 (N = 16 * (N/16)). One warp, warp barriers only.
+template <int N, int DIR, class Lines>
+__device__ __forceinline__ void warp_fft(const Lines& L, int nlines, const float2* tw) {
   constexpr int L2 = N / 16, G = 32 / L2, T = (G * 16) / 32;
   const int lane = threadIdx.x & 31;
   {
     const int g = lane / L2, n2 = lane % L2;
     if (g < nlines) {
-      float2* p = buf + g * ls;
       float2 x[16];
 #pragma unroll
-      for (int n1 = 0; n1 < 16; ++n1) x[n1] = p[(L2 * n1 + n2) * es];
+      for (int n1 = 0; n1 < 16; ++n1) x[n1] = L.at(g, L2 * n1 + n2);
       dft<16, DIR>(x);
 #pragma unroll
       for (int k1 = 1; k1 < 16; ++k1)
         if (n2) x[k1] = cmul(x[k1], tw_full<DIR>(tw, n2 * k1, N));
 #pragma unroll
-      for (int k1 = 0; k1 < 16; ++k1) p[(L2 * k1 + n2) * es] = x[k1];
+      for (int k1 = 0; k1 < 16; ++k1) L.at(g, L2 * k1 + n2) = x[k1];
     }
   }
   __syncwarp();
@@ -478,9 +555,8 @@ __device__ __forceinline__ void warp_fft(float2* buf, int nlines, int ls, int es
   for (int t = 0; t < T; ++t) {
     const int task = lane + 32 * t, g = task / 16, k1 = task % 16;
     if (g < nlines) {
-      const float2* p = buf + g * ls;
 #pragma unroll
-      for (int n2 = 0; n2 < L2; ++n2) y[t][n2] = p[(L2 * k1 + n2) * es];
+      for (int n2 = 0; n2 < L2; ++n2) y[t][n2] = L.at(g, L2 * k1 + n2);
       dft<L2, DIR>(y[t]);
     }
   }
@@ -489,9 +565,8 @@ __device__ __forceinline__ void warp_fft(float2* buf, int nlines, int ls, int es
   for (int t = 0; t < T; ++t) {
     const int task = lane + 32 * t, g = task / 16, k1 = task % 16;
     if (g < nlines) {
-      float2* p = buf + g * ls;
 #pragma unroll
-      for (int k2 = 0; k2 < L2; ++k2) p[(k1 + 16 * k2) * es] = y[t][k2];
+      for (int k2 = 0; k2 < L2; ++k2) L.at(g, k1 + 16 * k2) = y[t][k2];
     }
   }
   __syncwarp();
@@ -500,74 +575,53 @@ __device__ __forceinline__ void warp_fft(float2* buf, int nlines, int ls, int es
 template <int N>
 __device__ void build_one_smem(const ProjParams& P, int dir, int slot, float2* Zs, float2* stage_all,
                                const float2* tw, float* s_div, double* red, double* s_coef) {
-  constexpr int m = 2 * N, W = N + 1, LDZ = N + 1, HC = N / 2 + 1, L2 = N / 16, G = 32 / L2;
+  constexpr int m = 2 * N, W = N + 1, HC = N / 2 + 1, L2 = N / 16, G = 32 / L2;
+  const Plane<N> Z{Zs};
   const int nb = P.nb, H = nb / 2 + 1;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const float* R = P.rot + (size_t)dir * 9;
   const float R00 = R[0], R01 = R[1], R10 = R[3], R11 = R[4], R20 = R[6], R21 = R[7];
   const float inv_m = (float)(1.0 / (double)m);
 
-  // ---- pass A: gather + pruned row inverse, 16/L2 columns per warp round
+  // ---- pass A: gather + pruned row inverse. A warp round takes CPR = 16/L2
+  // columns: both parities of each column form G = 2*CPR lines of N samples
+  // in the warp's staging area, one warp FFT transforms them, and the
+  // even/odd pair combines into the N centred rows of the 2N-point inverse.
   {
-    constexpr int CPR = 16 / L2;  // columns per warp round
-    float2* stage = stage_all + warp * (CPR * 2 * N);
+    constexpr int CPR = 16 / L2;
+    const StageLines<N> S{stage_all + warp * (G * plane_ld(N))};
     for (int c0 = warp * CPR; c0 < W; c0 += kSmemWarps * CPR) {
-      {  // step 1: lane -> (column, parity, n2)
-        const int cl = lane / (2 * L2), e = (lane / L2) & 1, n2 = lane % L2;
+#pragma unroll 2
+      for (int idx = lane; idx < CPR * m; idx += 32) {
+        const int cl = idx / m, r = idx % m;  // r: standard-order row of the 2N grid
         const int c = c0 + cl;
+        float2 v = make_float2(0.f, 0.f);
         if (c < W) {
-          float2 x[16];
-#pragma unroll
-          for (int n1 = 0; n1 < 16; ++n1) {
-            const int r = 2 * (L2 * n1 + n2) + e;  // standard-order row of the 2N grid
-            const int kys = (r + N) % m;
-            const float gy = __fmul_rn((float)(kys - N), inv_m);
-            const float gx = __fmul_rn((float)c, inv_m);
-            float rx = __fadd_rn(__fmul_rn(R00, gx), __fmul_rn(R01, gy));
-            float ry = __fadd_rn(__fmul_rn(R10, gx), __fmul_rn(R11, gy));
-            float rz = __fadd_rn(__fmul_rn(R20, gx), __fmul_rn(R21, gy));
-            const bool conj = rx < 0.0f;
-            if (conj) { rx = -rx; ry = -ry; rz = -rz; }
-            const float cz = __fadd_rn(__fmul_rn(rz, (float)m), (float)(m / 2));
-            const float cy = __fadd_rn(__fmul_rn(ry, (float)m), (float)(m / 2));
-            const float cx = __fmul_rn(rx, (float)m);
-            float2 v = sample_trilinear(P.spectrum, m, W, grid_pixel(cz, m), grid_pixel(cy, m),
-                                        grid_pixel(cx, W));
-            if (conj) v.y = -v.y;
-            x[n1] = v;
-          }
-          dft<16, 1>(x);
-#pragma unroll
-          for (int k1 = 1; k1 < 16; ++k1)
-            if (n2) x[k1] = cmul(x[k1], tw_full<1>(tw, n2 * k1, N));
-          float2* s = stage + (cl * 2 + e) * N;
-#pragma unroll
-          for (int k1 = 0; k1 < 16; ++k1) s[L2 * k1 + n2] = x[k1];
+          const int kys = (r + N) % m;
+          const float gy = __fmul_rn((float)(kys - N), inv_m);
+          const float gx = __fmul_rn((float)c, inv_m);
+          float rx = __fadd_rn(__fmul_rn(R00, gx), __fmul_rn(R01, gy));
+          float ry = __fadd_rn(__fmul_rn(R10, gx), __fmul_rn(R11, gy));
+          float rz = __fadd_rn(__fmul_rn(R20, gx), __fmul_rn(R21, gy));
+          const bool conj = rx < 0.0f;
+          if (conj) { rx = -rx; ry = -ry; rz = -rz; }
+          const float cz = __fadd_rn(__fmul_rn(rz, (float)m), (float)(m / 2));
+          const float cy = __fadd_rn(__fmul_rn(ry, (float)m), (float)(m / 2));
+          const float cx = __fmul_rn(rx, (float)m);
+          v = sample_slice<N>(P.spectrum, cz, cy, cx);
+          if (conj) v.y = -v.y;
         }
+        S.at(cl * 2 + (r & 1), r >> 1) = v;
       }
       __syncwarp();
-      {  // step 2: tasks (column, k1), both parities, combine into Zs
-        constexpr int T2 = (CPR * 16) / 32;
-#pragma unroll
-        for (int t = 0; t < T2; ++t) {
-          const int task = lane + 32 * t, cl = task / 16, k1 = task % 16;
-          const int c = c0 + cl;
-          if (c < W) {
-            float2 a0[L2], a1[L2];
-            const float2* s0 = stage + (cl * 2) * N;
-            const float2* s1 = s0 + N;
-#pragma unroll
-            for (int n2 = 0; n2 < L2; ++n2) { a0[n2] = s0[L2 * k1 + n2]; a1[n2] = s1[L2 * k1 + n2]; }
-            dft<L2, 1>(a0);
-            dft<L2, 1>(a1);
-#pragma unroll
-            for (int k2 = 0; k2 < L2; ++k2) {
-              const int k = k1 + 16 * k2;
-              const int u = k < N / 2 ? k : k - N;
-              const float2 z = cadd(a0[k2], cmul(tw_pos(tw, u, m), a1[k2]));
-              Zs[(u + N / 2) * LDZ + c] = z;
-            }
-          }
+      warp_fft<N, 1>(S, G, tw);
+      for (int idx = lane; idx < CPR * N; idx += 32) {
+        const int cl = idx / N, k = idx % N;
+        const int c = c0 + cl;
+        if (c < W) {
+          const int u = k < N / 2 ? k : k - N;
+          const float2 a0 = S.at(cl * 2, k), a1 = S.at(cl * 2 + 1, k);
+          Z(u + N / 2, c) = cadd(a0, cmul(tw_pos(tw, u, m), a1));
         }
       }
       __syncwarp();
@@ -578,65 +632,61 @@ __device__ void build_one_smem(const ProjParams& P, int dir, int slot, float2* Z
   // ---- pass B: C2R along columns, keep centred N, then forward row FFT
   const float scale_b = (float)(1.0 / ((double)m * (double)m));
   for (int r0 = warp * G; r0 < N; r0 += kSmemWarps * G) {
-    float2* rows = Zs + r0 * LDZ;
-    {  // W = Ye + i Yo, read all then write (k and N-k cross)
-      float2 wv[16];
-#pragma unroll
-      for (int t = 0; t < 16; ++t) {
-        const int idx = lane + 32 * t, g = idx / N, k = idx % N;
-        const float2* Z = rows + g * LDZ;
-        float2 ye, yo;
-        if (k == 0) {
-          const float a = Z[0].x, b = Z[N].x;
-          ye = make_float2(a + b, 0.f);
-          yo = make_float2(a - b, 0.f);
+    const RowLines<N> RL{Z, r0};
+    // W = Ye + i Yo. A lane owns the pair (k, N-k): both outputs depend on
+    // Z_k and Z_{N-k} only, so the rows are rewritten in place.
+    for (int idx = lane; idx < G * (N / 2 + 1); idx += 32) {
+      const int g = idx / (N / 2 + 1), k = idx % (N / 2 + 1);
+      if (k == 0) {
+        const float a = RL.at(g, 0).x, b = RL.at(g, N).x;
+        RL.at(g, 0) = make_float2(a + b, a - b);  // Ye = a + b, Yo = a - b (both real)
+      } else {
+        const float2 zk = RL.at(g, k), zn = RL.at(g, N - k);
+        const float2 ye = cadd(zk, cconj(zn));
+        const float2 yo = cmul(csub(zk, cconj(zn)), tw_pos(tw, k, m));
+        if (k == N / 2) {
+          RL.at(g, k) = make_float2(ye.x - yo.y, ye.y + yo.x);
         } else {
-          const float2 zk = Z[k], zc = cconj(Z[N - k]);
-          ye = cadd(zk, zc);
-          yo = cmul(csub(zk, zc), tw_pos(tw, k, m));
+          const float2 ye2 = cadd(zn, cconj(zk));
+          const float2 yo2 = cmul(csub(zn, cconj(zk)), tw_full<1>(tw, N - k, m));
+          RL.at(g, k) = make_float2(ye.x - yo.y, ye.y + yo.x);
+          RL.at(g, N - k) = make_float2(ye2.x - yo2.y, ye2.y + yo2.x);
         }
-        wv[t] = make_float2(ye.x - yo.y, ye.y + yo.x);
       }
-      __syncwarp();
-#pragma unroll
-      for (int t = 0; t < 16; ++t) {
-        const int idx = lane + 32 * t, g = idx / N, k = idx % N;
-        rows[g * LDZ + k] = wv[t];
-      }
-      __syncwarp();
     }
-    warp_fft<N, 1>(rows, G, LDZ, 1, tw);
+    __syncwarp();
+    warp_fft<N, 1>(RL, G, tw);
     {  // p(2n) = Re z(n), p(2n+1) = Im z(n); keep v = (j - N/2) mod 2N
       float pv[16];
 #pragma unroll
       for (int t = 0; t < 16; ++t) {
         const int idx = lane + 32 * t, g = idx / N, j = idx % N;
         const int v = (j - N / 2 + m) % m;
-        const float2 zz = rows[g * LDZ + (v >> 1)];
+        const float2 zz = RL.at(g, v >> 1);
         pv[t] = ((v & 1) ? zz.y : zz.x) * scale_b;
       }
       __syncwarp();
 #pragma unroll
       for (int t = 0; t < 16; ++t) {
         const int idx = lane + 32 * t, g = idx / N, j = idx % N;
-        rows[g * LDZ + j] = make_float2(pv[t], 0.f);
+        RL.at(g, j) = make_float2(pv[t], 0.f);
       }
       __syncwarp();
     }
-    warp_fft<N, -1>(rows, G, LDZ, 1, tw);
+    warp_fft<N, -1>(RL, G, tw);
   }
   __syncthreads();
 
   // ---- pass C: forward column FFT over kx in [0, N/2]
   for (int c0 = warp * G; c0 < HC; c0 += kSmemWarps * G)
-    warp_fft<N, -1>(Zs + c0, min(G, HC - c0), 1, LDZ, tw);
+    warp_fft<N, -1>(ColLines<N>{Z, c0}, min(G, HC - c0), tw);
   __syncthreads();
   for (int b = warp; b < P.n_bins; b += kSmemWarps) {
     double acc = 0.0;
     for (int e = P.bin_ptr[b] + lane; e < P.bin_ptr[b + 1]; e += 32) {
       const int idx = P.bin_list[e];
       const int r = idx / HC, kx = idx - r * HC;
-      const float2 f = Zs[r * LDZ + kx];
+      const float2 f = Z(r, kx);
       const double a = (double)hypotf(f.x, f.y);
       acc += (kx == 0 || kx == N / 2) ? a : 2.0 * a;
     }
@@ -652,10 +702,10 @@ __device__ void build_one_smem(const ProjParams& P, int dir, int slot, float2* Z
       const int cl = idx / N, r = idx % N, kx = c0 + cl;
       const int ky = r < N / 2 ? r : r - N;
       const int bin = (int)rintf(sqrtf((float)(ky * ky + kx * kx)));
-      Zs[r * LDZ + kx] = cscale(Zs[r * LDZ + kx], s_div[bin]);
+      Z(r, kx) = cscale(Z(r, kx), s_div[bin]);
     }
     __syncwarp();
-    warp_fft<N, 1>(Zs + c0, nc, 1, LDZ, tw);
+    warp_fft<N, 1>(ColLines<N>{Z, c0}, nc, tw);
   }
   __syncthreads();
 
@@ -663,28 +713,22 @@ __device__ void build_one_smem(const ProjParams& P, int dir, int slot, float2* Z
   const float scale_e = (float)(1.0 / ((double)N * (double)N));
   double sz = 0.0, sxz = 0.0, syz = 0.0;
   for (int r0 = warp * G; r0 < N; r0 += kSmemWarps * G) {
-    float2* rows = Zs + r0 * LDZ;
-    float2 hv[16];
-#pragma unroll
-    for (int t = 0; t < 16; ++t) {
-      const int idx = lane + 32 * t, g = idx / N, k = idx % N;
-      const float2* Gr = rows + g * LDZ;
-      hv[t] = (k == 0 || k == N / 2) ? make_float2(Gr[k].x, 0.f) : (k < N / 2 ? Gr[k] : cconj(Gr[N - k]));
+    const RowLines<N> RL{Z, r0};
+    // Hermitian extension of each row: position N-k takes conj(G(k)); only
+    // positions above N/2 are written, from positions below, so no barrier.
+    for (int idx = lane; idx < G * (N / 2 + 1); idx += 32) {
+      const int g = idx / (N / 2 + 1), k = idx % (N / 2 + 1);
+      if (k == 0 || k == N / 2) RL.at(g, k).y = 0.f;
+      else RL.at(g, N - k) = cconj(RL.at(g, k));
     }
     __syncwarp();
-#pragma unroll
-    for (int t = 0; t < 16; ++t) {
-      const int idx = lane + 32 * t, g = idx / N, k = idx % N;
-      rows[g * LDZ + k] = hv[t];
-    }
-    __syncwarp();
-    warp_fft<N, 1>(rows, G, LDZ, 1, tw);
+    warp_fft<N, 1>(RL, G, tw);
 #pragma unroll
     for (int t = 0; t < 16; ++t) {
       const int idx = lane + 32 * t, g = idx / N, j = idx % N;
       const int i = r0 + g;
-      const float w = rows[g * LDZ + j].x * scale_e;
-      rows[g * LDZ + j] = make_float2(w, 0.f);
+      const float w = RL.at(g, j).x * scale_e;
+      RL.at(g, j) = make_float2(w, 0.f);
       sz += (double)w;
       sxz += (double)i * (double)w;
       syz += (double)j * (double)w;
@@ -718,7 +762,7 @@ __device__ void build_one_smem(const ProjParams& P, int dir, int slot, float2* Z
   double sv = 0.0;
   for (int t = threadIdx.x; t < N * N; t += blockDim.x) {
     const int i = t / N, j = t - i * N;
-    const double v = (double)Zs[i * LDZ + j].x - (pc0 * i + pc1 * j + pc2) - mean;
+    const double v = (double)Z(i, j).x - (pc0 * i + pc1 * j + pc2) - mean;
     sv += v * v;
   }
   sv = block_sum_d(sv, red);
@@ -727,22 +771,22 @@ __device__ void build_one_smem(const ProjParams& P, int dir, int slot, float2* Z
 
   // ---- pass F: normalise, mask, forward row FFT
   for (int r0 = warp * G; r0 < N; r0 += kSmemWarps * G) {
-    float2* rows = Zs + r0 * LDZ;
+    const RowLines<N> RL{Z, r0};
 #pragma unroll
     for (int t = 0; t < 16; ++t) {
       const int idx = lane + 32 * t, g = idx / N, j = idx % N;
       const int i = r0 + g;
-      float f = (float)(((double)rows[g * LDZ + j].x - (pc0 * i + pc1 * j + pc2) - mean) * inv_sd);
+      float f = (float)(((double)RL.at(g, j).x - (pc0 * i + pc1 * j + pc2) - mean) * inv_sd);
       if (P.mask != nullptr) f *= P.mask[i * N + j];
-      rows[g * LDZ + j] = make_float2(f, 0.f);
+      RL.at(g, j) = make_float2(f, 0.f);
     }
     __syncwarp();
-    warp_fft<N, -1>(rows, G, LDZ, 1, tw);
+    warp_fft<N, -1>(RL, G, tw);
   }
   __syncthreads();
   // ---- pass G: forward column FFT
   for (int c0 = warp * G; c0 < HC; c0 += kSmemWarps * G)
-    warp_fft<N, -1>(Zs + c0, min(G, HC - c0), 1, LDZ, tw);
+    warp_fft<N, -1>(ColLines<N>{Z, c0}, min(G, HC - c0), tw);
   __syncthreads();
   // crop + pack + FSC, L2 norm, pre-shifted write
   double ss = 0.0;
@@ -750,9 +794,9 @@ __device__ void build_one_smem(const ProjParams& P, int dir, int slot, float2* Z
     const int r = t / H, c = t - r * H;
     const int ky = r < nb / 2 ? r : r - nb;
     float2 f;
-    if (c < nb / 2) f = Zs[((ky + N) % N) * LDZ + c];
-    else if (nb == N) f = Zs[((ky + N) % N) * LDZ + N / 2];
-    else f = cconj(Zs[((-ky + N) % N) * LDZ + nb / 2]);
+    if (c < nb / 2) f = Z((ky + N) % N, c);
+    else if (nb == N) f = Z((ky + N) % N, N / 2);
+    else f = cconj(Z((-ky + N) % N, nb / 2));
     f = cscale(f, P.fsc[t]);
     ss += (double)f.x * f.x + (double)f.y * f.y;
   }
@@ -763,9 +807,9 @@ __device__ void build_one_smem(const ProjParams& P, int dir, int slot, float2* Z
     const int r = t / H, c = t - r * H;
     const int ky = r < nb / 2 ? r : r - nb;
     float2 f;
-    if (c < nb / 2) f = Zs[((ky + N) % N) * LDZ + c];
-    else if (nb == N) f = Zs[((ky + N) % N) * LDZ + N / 2];
-    else f = cconj(Zs[((-ky + N) % N) * LDZ + nb / 2]);
+    if (c < nb / 2) f = Z((ky + N) % N, c);
+    else if (nb == N) f = Z((ky + N) % N, N / 2);
+    else f = cconj(Z((-ky + N) % N, nb / 2));
     f = cscale(f, P.fsc[t]);
     const int rs = (r + nb / 2) % nb, cs = (c + H / 2) % H;
     out[(size_t)rs * H + cs] = cscale(f, inv_norm);
@@ -776,10 +820,10 @@ __device__ void build_one_smem(const ProjParams& P, int dir, int slot, float2* Z
 template <int N>
 __global__ void __launch_bounds__(kSmemThreads, 1) project_templates_smem(ProjParams P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr int LDZ = N + 1, L2 = N / 16, CPR = 16 / L2;
+  constexpr int L2 = N / 16;
   float2* Zs = reinterpret_cast<float2*>(smem_raw);
-  float2* stage = Zs + N * LDZ;
-  float2* s_tw = stage + kSmemWarps * CPR * 2 * N;
+  float2* stage = Zs + plane_rows(N) * plane_ld(N);
+  float2* s_tw = stage + kSmemWarps * (32 / L2) * plane_ld(N);
   double* red = reinterpret_cast<double*>(s_tw + kMaxFftLen / 2);
   double* s_coef = red + 32;
   float* s_div = reinterpret_cast<float*>(s_coef + 8);
@@ -795,17 +839,21 @@ __global__ void __launch_bounds__(kSmemThreads, 1) project_templates_smem(ProjPa
 }  // namespace
 
 size_t project_smem_bytes_fast(int N, int n_bins) {
-  const int L2 = N / 16, CPR = 16 / L2;
-  return (size_t)N * (N + 1) * sizeof(float2) + (size_t)kSmemWarps * CPR * 2 * N * sizeof(float2) +
+  const int L2 = N / 16;
+  return (size_t)plane_rows(N) * plane_ld(N) * sizeof(float2) + (size_t)kSmemWarps * (32 / L2) * plane_ld(N) * sizeof(float2) +
          (kMaxFftLen / 2) * sizeof(float2) + 40 * sizeof(double) + (size_t)(n_bins + 4) * sizeof(float);
 }
 
 template <int N>
 static cudaError_t launch_fast(const ProjParams& P, int grid, cudaStream_t st) {
   const size_t smem = project_smem_bytes_fast(N, P.n_bins);
-  cudaError_t e = cudaFuncSetAttribute(project_templates_smem<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
-  if (e != cudaSuccess) return e;
+  static size_t set_smem = 0;  // attribute set once per size, never inside a stream capture
+  if (set_smem < smem) {
+    cudaError_t e = cudaFuncSetAttribute(project_templates_smem<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    set_smem = smem;
+  }
   project_templates_smem<N><<<grid, kSmemThreads, smem, st>>>(P);
   return cudaGetLastError();
 }

@@ -144,7 +144,6 @@ splat_bricks(const AtomRec* __restrict__ atoms, int n_atoms, const float* __rest
              float* __restrict__ out, float* __restrict__ padded, int box, float rp_hi,
              float rp_lo) {
   __shared__ AtomRec s_atoms[256];
-  __shared__ int s_list[256];
   __shared__ int s_count;
   const int nbx = (box + kBrick - 1) / kBrick;
   const int bz = blockIdx.x / (nbx * nbx);
@@ -195,7 +194,6 @@ splat_bricks(const AtomRec* __restrict__ atoms, int n_atoms, const float* __rest
     if (hit) {
       const int pos = s_warp_base[threadIdx.x >> 5] + __popc(mask & ((1u << (threadIdx.x & 31)) - 1u));
       s_atoms[pos] = r;
-      s_list[pos] = ai;
     }
     __syncthreads();
     const int cnt = s_count;
@@ -224,7 +222,6 @@ splat_bricks(const AtomRec* __restrict__ atoms, int n_atoms, const float* __rest
       }
     }
   }
-  (void)s_list;
   if (!col_ok) return;
   const int m = 2 * box;
   const int half = box / 2;

@@ -227,3 +227,116 @@ class ScoringJob:
 
     def search_text(self) -> str:
         return "".join(str(row) + "\n" for row in self.result_records())
+
+
+class BatchScoringJob:
+    """Many candidates per launch sequence, replayed as one CUDA graph.
+
+    A PSO/simplex generation is a batch of candidate poses; each slot of the
+    batch is bound to one moving-chain model (models share the job's fixed
+    context, so chains of different atom counts mix in one batch). Per slot
+    the splat, volume FFT and projector write that candidate's template bank;
+    one batched correlation then stages each particle's spectra on chip once
+    for all candidates, and batched record and score kernels finish. After a
+    warm-up run the whole sequence is captured into a CUDA graph; scoring a
+    new generation copies the poses in and replays the graph. This is the
+    GPU form of the Lite tree's round-batched evaluation
+    (ZL gisapr_batch_search.py:251-364).
+    """
+
+    def __init__(self, job: ScoringJob, n_cand: int, models: Optional[Sequence] = None,
+                 model_of: Optional[Sequence[int]] = None, use_graph: bool = True):
+        self.job = job
+        self.n_cand = int(n_cand)
+        self.models = list(models) if models else [job.density]
+        self.model_of = list(model_of) if model_of is not None else [i % len(self.models) for i in range(self.n_cand)]
+        if len(self.model_of) != self.n_cand:
+            raise ValueError("model_of needs one model index per candidate")
+        dev = job.device
+        nb = job.cfg.new_box
+        n_needed = max(1, len(job.needed))
+        self.banks = torch.empty((self.n_cand, n_needed, nb, nb // 2 + 1), dtype=torch.complex64, device=dev)
+        self.bank_stride = n_needed * nb * (nb // 2 + 1)
+        m = max(1, job.nnz) * job.n_psi
+        self.score_buf = torch.empty((self.n_cand, m), dtype=torch.float32, device=dev)
+        self.y_buf = torch.empty((self.n_cand, m), dtype=torch.int32, device=dev)
+        self.x_buf = torch.empty((self.n_cand, m), dtype=torch.int32, device=dev)
+        np_ = len(job.records)
+        shape = (self.n_cand, np_)
+        self.best_entry = torch.empty(shape, dtype=torch.int32, device=dev)
+        self.best_psi = torch.empty(shape, dtype=torch.int32, device=dev)
+        self.peak = torch.empty(shape, dtype=torch.float32, device=dev)
+        self.peak_y = torch.empty(shape, dtype=torch.int32, device=dev)
+        self.peak_x = torch.empty(shape, dtype=torch.int32, device=dev)
+        self.zscore = torch.empty(shape, dtype=torch.float32, device=dev)
+        self.totals = torch.zeros(self.n_cand, dtype=torch.float64, device=dev)
+        self.poses_dev = torch.zeros((self.n_cand, 12), dtype=torch.float64, device=dev)
+        self.poses_host = torch.zeros((self.n_cand, 12), dtype=torch.float64).pin_memory()
+        self.totals_host = torch.zeros(self.n_cand, dtype=torch.float64).pin_memory()
+        self.use_graph = bool(use_graph)
+        self.graph = None
+        self.stream = torch.cuda.Stream(dev)
+
+    KERNELS_PER_CANDIDATE = 3  # splat (2 launches) and projector, per slot
+    KERNELS_PER_BATCH = 3      # correlation, records, score sums
+
+    def launches_per_batch(self) -> int:
+        return self.n_cand * self.KERNELS_PER_CANDIDATE + self.KERNELS_PER_BATCH
+
+    def enqueue(self) -> None:
+        """Enqueue the whole batch on the current stream (poses already on the device)."""
+        job = self.job
+        dev = job.device
+        ctx = nat.Context.for_device(dev).handle
+        st = nat.stream_of(dev)
+        for c in range(self.n_cand):
+            self.models[self.model_of[c]].generate(None, write_padded=True, pose_device=self.poses_dev[c])
+            job.projector.volume_spectrum(None)
+            if job.needed:
+                job.projector.project(job.angles, job.needed_dirs, self.banks[c], job.needed_slots)
+        np_ = len(job.records)
+        nat.call("gisapr_correlate_batch", ctx, st, nat.ptr(self.banks), self.bank_stride, self.n_cand,
+                 nat.ptr(job.stack), nat.ptr(job.local_ptr), nat.ptr(job.local_idx), np_, job.nnz, job.n_psi,
+                 job.cfg.new_box, job.cfg.crop, nat.ptr(self.score_buf), nat.ptr(self.y_buf), nat.ptr(self.x_buf))
+        nat.call("gisapr_particle_results_batch", st, nat.ptr(job.local_ptr), nat.ptr(self.score_buf),
+                 nat.ptr(self.y_buf), nat.ptr(self.x_buf), np_, job.n_psi, self.n_cand, nat.ptr(self.best_entry),
+                 nat.ptr(self.best_psi), nat.ptr(self.peak), nat.ptr(self.peak_y), nat.ptr(self.peak_x),
+                 nat.ptr(self.zscore))
+        nat.call("gisapr_score_sum_batch", st, nat.ptr(job.local_ptr), nat.ptr(self.peak), np_, self.n_cand,
+                 nat.ptr(self.totals))
+
+    def _ensure_graph(self) -> None:
+        if self.graph is not None or not self.use_graph:
+            return
+        # warm-up outside capture: plans, tables and scratch are created here
+        with torch.cuda.stream(self.stream):
+            self.enqueue()
+        self.stream.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=self.stream):
+            self.enqueue()
+        self.graph = g
+
+    def run(self) -> None:
+        """Score the poses already in poses_dev (enqueue only; graph replay if captured)."""
+        self._ensure_graph()
+        if self.graph is not None:
+            self.graph.replay()
+        else:
+            self.enqueue()
+
+    def set_poses(self, poses) -> None:
+        for c, p in enumerate(poses):
+            self.poses_host[c].copy_(self.models[self.model_of[c]].pose_tensor(p))
+        self.poses_dev.copy_(self.poses_host, non_blocking=True)
+
+    def score_batch(self, poses) -> np.ndarray:
+        """Scores of len(poses) == n_cand poses, in slot order."""
+        if len(poses) != self.n_cand:
+            raise ValueError(f"expected {self.n_cand} poses, got {len(poses)}")
+        self._ensure_graph()
+        self.set_poses(poses)
+        self.run()
+        self.totals_host.copy_(self.totals, non_blocking=True)
+        torch.cuda.current_stream(self.job.device).synchronize()
+        return self.totals_host.numpy().copy()

@@ -530,3 +530,39 @@ def reference_density(coords, elements, box, apix, res) -> np.ndarray:
         idx = v[..., 0] + box * (v[..., 1] + box * v[..., 2])
         vol += np.bincount(idx[ok], weights=val[ok], minlength=box ** 3)
     return vol.reshape(box, box, box).astype(np.float32)
+
+
+def make_models_shared_fixed(moving_atoms: Sequence[int], n_fixed_atoms: int, seed: int,
+                             s_fraction: float = 0.05) -> List[SyntheticModel]:
+    """Models that share one fixed chain B and differ in the moving chain A
+    (the mixed 1,500 / 3,000 / 6,000-atom batches). Chain B comes from its
+    own seeded generator, so it is identical in every model."""
+    rng_b = np.random.default_rng(seed + 7919)
+    nb = residues_for_atoms(n_fixed_atoms, s_fraction)
+    rb = max(12.0, 1.25 * (31.0 * nb) ** (1.0 / 3.0))
+    xb, names_b, els_b = _residue_atoms(_ca_walk(nb, rng_b, rb), rng_b, s_fraction)
+    xb = xb - xb.mean(axis=0)
+    models = []
+    for k, n_atoms in enumerate(moving_atoms):
+        rng_a = np.random.default_rng(seed + 104729 * (k + 1))
+        na = residues_for_atoms(n_atoms, s_fraction)
+        ra = max(12.0, 1.25 * (31.0 * na) ** (1.0 / 3.0))
+        xa, names_a, els_a = _residue_atoms(_ca_walk(na, rng_a, ra), rng_a, s_fraction)
+        xa = xa - xa.mean(axis=0)
+        lines, coords, elements, chains = [], [], [], []
+        serial = 1
+        for chain, (xyz, names, els) in zip("AB", ((xa, names_a, els_a), (xb, names_b, els_b))):
+            res = 0
+            for p, nm, el in zip(xyz, names, els):
+                if nm == "N":
+                    res += 1
+                p = np.asarray([float(f"{v:8.3f}") for v in p])
+                lines.append(_pdb_line(serial, nm, "ALA" if nm != "SG" else "CYS", chain, res, p, el))
+                coords.append(p)
+                elements.append(el)
+                chains.append(chain)
+                serial += 1
+            lines.append("TER\n")
+        lines.append("END\n")
+        models.append(SyntheticModel(np.asarray(coords), elements, chains, "".join(lines)))
+    return models

@@ -160,6 +160,19 @@ int gisapr_correlate(gisapr_ctx ctx, void* stream, const float* bank, const floa
                      int crop, float* out_score, int* out_y, int* out_x);
 
 /*
+ * gisapr_correlate for n_cand candidates at once: candidate c's template bank
+ * starts bank_stride complex elements after candidate c-1's, and its outputs
+ * follow the previous candidate's (out_score [n_cand][nnz][n_psi]). Each
+ * particle's spectra are staged on chip once for all candidates. nnz =
+ * local_ptr[n_particles], passed so that no value is read back during graph
+ * capture. Replaces the candidate loop of the Lite tree's round-batched
+ * search (ZL/gisapr_batch_search.py:314-349).
+ */
+int gisapr_correlate_batch(gisapr_ctx ctx, void* stream, const float* bank, long long bank_stride, int n_cand,
+                           const float* stack, const int* local_ptr, const int* local_idx, int n_particles,
+                           int nnz, int n_psi, int n, int crop, float* out_score, int* out_y, int* out_x);
+
+/*
  * Per particle: first maximum over (local entry, psi), its crop position and
  * the z-score (peak - mean) / population sigma over all the particle's
  * scores. Replaces the numeric part of make_result_records (v606:1466-1491).
@@ -169,6 +182,11 @@ int gisapr_particle_results(void* stream, const int* local_ptr, const float* sco
                             const int* xs, int n_particles, int n_psi, int* best_entry,
                             int* best_psi, float* peak, int* peak_y, int* peak_x, float* zscore);
 
+/* gisapr_particle_results for n_cand candidates laid out one after another. */
+int gisapr_particle_results_batch(void* stream, const int* local_ptr, const float* score, const int* ys,
+                                  const int* xs, int n_particles, int n_psi, int n_cand, int* best_entry,
+                                  int* best_psi, float* peak, int* peak_y, int* peak_x, float* zscore);
+
 /*
  * Candidate score sum over particles with directions of exp(peak / 1024),
  * float64 into out[0]. Replaces ZL/gisapr_batch_search.py:361 and the
@@ -177,6 +195,10 @@ int gisapr_particle_results(void* stream, const int* local_ptr, const float* sco
  */
 int gisapr_score_sum(void* stream, const int* local_ptr, const float* peak, int n_particles,
                      double* out);
+
+/* gisapr_score_sum for n_cand candidates: peak [n_cand][n_particles], out [n_cand]. */
+int gisapr_score_sum_batch(void* stream, const int* local_ptr, const float* peak, int n_particles, int n_cand,
+                           double* out);
 
 #ifdef __cplusplus
 }

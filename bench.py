@@ -51,6 +51,8 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=48, help="particles and templates in the CPU sample")
     ap.add_argument("--batch", type=int, default=64, help="candidates per batched generation (0: skip)")
+    ap.add_argument("--precisions", default="fp32,fp16x3",
+                    help="batched correlation forms to time: fp32 (plain), fp16x3 (tensor-core split), fp16")
     return ap.parse_args()
 
 
@@ -132,6 +134,58 @@ def job_records(job):
     return [ParticleRecord(int(r.line_index[i]), f"{i + 1}@particles.mrcs", float(r.rot[i]), float(r.tilt[i]),
                            float(r.psi[i]), float(r.defocus_u[i]), float(r.defocus_v[i]),
                            float(r.defocus_angle[i])) for i in range(len(r.rot))]
+
+
+def run_batched(job, dens, gen, precision, n_batch, K, W, device, barrier):
+    """Time K graph-replayed generations of n_batch candidates (device events on
+    the batch stream), then K end-to-end generations (poses from the host,
+    scores and per-particle peaks back)."""
+    import torch
+    from gisapr_gb300.engine import BatchScoringJob
+    model_of = [i % len(dens) for i in range(n_batch)]
+    bj = BatchScoringJob(job, n_batch, models=dens, model_of=model_of, precision=precision)
+    for k in range(W):
+        bj.score_batch(gen[k])
+    barrier()
+    torch.cuda.synchronize(device)
+    b0 = torch.cuda.Event(enable_timing=True)
+    b1 = torch.cuda.Event(enable_timing=True)
+    b_steps = []
+    with torch.cuda.stream(bj.stream):
+        b0.record()
+        for k in range(K):
+            bj.set_poses(gen[W + k])
+            ev = torch.cuda.Event(enable_timing=True)
+            ev.record()
+            b_steps.append(ev)
+            bj.run()
+        b1.record()
+    torch.cuda.synchronize(device)
+    barrier()
+    bj.check_status()
+    b_elapsed = b0.elapsed_time(b1) / 1e3
+    b_steps.append(b1)
+    b_lat = sorted(b_steps[i].elapsed_time(b_steps[i + 1]) for i in range(K))
+    bpeaks_host = torch.empty(tuple(bj.peak.shape), dtype=torch.float32).pin_memory()
+    e2 = torch.cuda.Event(enable_timing=True)
+    e3 = torch.cuda.Event(enable_timing=True)
+    e2.record()
+    for k in range(K):
+        bj.score_batch(gen[W + k])
+        bpeaks_host.copy_(bj.peak, non_blocking=True)
+    e3.record()
+    torch.cuda.synchronize(device)
+    b_e2e = e2.elapsed_time(e3) / 1e3
+    stages = bj.stage_ms(gen[W])
+    return {"candidates_per_step": n_batch, "precision": precision,
+            "moving_chain_atoms": [m.n_moving for m in dens],
+            "graph": bj.graph is not None, "ms_per_step": b_elapsed / K * 1e3,
+            "latency_ms": {"p50": b_lat[len(b_lat) // 2],
+                           "p99": b_lat[min(len(b_lat) - 1, int(math.ceil(0.99 * len(b_lat))) - 1)]},
+            "stage_ms": stages,
+            "elapsed_s": b_elapsed, "e2e_elapsed_s": b_e2e, "e2e_h2d_bytes_per_step": 12 * 8 * n_batch,
+            "e2e_d2h_bytes_per_step": 8 * n_batch + 4 * n_batch * len(job.records),
+            "gpu_launches": bj.launches_per_batch() * K}
 
 
 def cpu_baseline(spec, job, pose, sample: int):
@@ -283,69 +337,33 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
     e2e_elapsed = e0.elapsed_time(e1) / 1e3
 
     # ---- batched generations: args.batch candidates per step, one CUDA graph
-    batched = None
-    b_elapsed = 0.0
+    batched = {}
     if args.batch > 0:
-        from gisapr_gb300.engine import BatchScoringJob
         from gisapr_gb300.pdb2mrc import MovedChainDensity
         dens = [MovedChainDensity(m.pdb_text, "A", spec.box, spec.apix, spec.res, device, from_text=True)
                 for m in models]
-        model_of = [i % len(dens) for i in range(args.batch)]
-        bj = BatchScoringJob(job, args.batch, models=dens, model_of=model_of)
         gen = [syn.candidate_poses(args.batch, args.seed + 1000 + 31 * k + rank, 5.0, 3.0) for k in range(K + W)]
-        for k in range(W):
-            bj.score_batch(gen[k])
-        barrier()
-        torch.cuda.synchronize(device)
-        b0 = torch.cuda.Event(enable_timing=True)
-        b1 = torch.cuda.Event(enable_timing=True)
-        b_steps = []
-        with torch.cuda.stream(bj.stream):
-            b0.record()
-            for k in range(K):
-                bj.set_poses(gen[W + k])
-                ev = torch.cuda.Event(enable_timing=True)
-                ev.record()
-                b_steps.append(ev)
-                bj.run()
-            b1.record()
-        torch.cuda.synchronize(device)
-        barrier()
-        b_elapsed = b0.elapsed_time(b1) / 1e3
-        b_steps.append(b1)
-        b_lat = sorted(b_steps[i].elapsed_time(b_steps[i + 1]) for i in range(K))
-        # end to end: poses from host, scores and per-particle peaks back, every generation
-        bpeaks_host = torch.empty(tuple(bj.peak.shape), dtype=torch.float32).pin_memory()
-        e2 = torch.cuda.Event(enable_timing=True)
-        e3 = torch.cuda.Event(enable_timing=True)
-        e2.record()
-        for k in range(K):
-            bj.score_batch(gen[W + k])
-            bpeaks_host.copy_(bj.peak, non_blocking=True)
-        e3.record()
-        torch.cuda.synchronize(device)
-        b_e2e = e2.elapsed_time(e3) / 1e3
-        batched = {"candidates_per_step": args.batch, "moving_chain_atoms": [m.n_moving for m in dens],
-                   "graph": bj.graph is not None, "ms_per_step": b_elapsed / K * 1e3,
-                   "latency_ms": {"p50": b_lat[len(b_lat) // 2],
-                                  "p99": b_lat[min(len(b_lat) - 1, int(math.ceil(0.99 * len(b_lat))) - 1)]},
-                   "e2e_elapsed_s": b_e2e, "e2e_h2d_bytes_per_step": 12 * 8 * args.batch,
-                   "e2e_d2h_bytes_per_step": 8 * args.batch + 4 * args.batch * len(job.records),
-                   "gpu_launches": bj.launches_per_batch() * K}
-
-    times = torch.tensor([elapsed, e2e_elapsed, b_elapsed, batched["e2e_elapsed_s"] if batched else 0.0],
-                         dtype=torch.float64, device=device)
+        for precision in args.precisions.split(","):
+            batched[precision] = run_batched(job, dens, gen, precision, args.batch, K, W, device, barrier)
+    tl = [elapsed, e2e_elapsed]
+    for b in batched.values():
+        tl += [b["elapsed_s"], b["e2e_elapsed_s"]]
+    times = torch.tensor(tl, dtype=torch.float64, device=device)
     if world > 1:
         torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
     elapsed, e2e_elapsed = float(times[0]), float(times[1])
-    if batched is not None:
-        batched["value"] = world * K * args.batch / float(times[2])
-        batched["unit"] = UNIT
-        batched["e2e"] = {"value": world * K * args.batch / float(times[3]), "unit": UNIT,
-                          "h2d_bytes_per_step": batched.pop("e2e_h2d_bytes_per_step"),
-                          "d2h_bytes_per_step": batched.pop("e2e_d2h_bytes_per_step")}
-        batched.pop("e2e_elapsed_s")
-        batched["vs_plain_single"] = batched["value"] / (world * K / elapsed)
+    for i, b in enumerate(batched.values()):
+        b["value"] = world * K * args.batch / float(times[2 + 2 * i])
+        b["unit"] = UNIT
+        b["e2e"] = {"value": world * K * args.batch / float(times[3 + 2 * i]), "unit": UNIT,
+                    "h2d_bytes_per_step": b.pop("e2e_h2d_bytes_per_step"),
+                    "d2h_bytes_per_step": b.pop("e2e_d2h_bytes_per_step")}
+        b.pop("elapsed_s")
+        b.pop("e2e_elapsed_s")
+        b["vs_plain_single"] = b["value"] / (world * K / elapsed)
+    if "fp32" in batched:
+        for b in batched.values():
+            b["vs_plain_batched"] = b["value"] / batched["fp32"]["value"]
     if rank != 0:
         return
     value = world * K / elapsed
@@ -384,7 +402,7 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
         "setup_s": {"synthetic_data": t_data, "job": job.setup_s},
         "score_sample": scores[0],
     }
-    if batched is not None:
+    if batched:
         line["batched"] = batched
     if world == 1 and not args.no_cpu_baseline:
         cb = cpu_baseline(spec, data, poses[W], args.cpu_sample)

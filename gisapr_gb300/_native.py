@@ -35,7 +35,14 @@ SIGNATURES = {
     "gisapr_correlate_batch": [_p, _p, _p, C.c_longlong, _i, _p, _p, _p, _i, _i, _i, _i, _i, _p, _p, _p],
     "gisapr_particle_results_batch": [_p, _p, _p, _p, _p, _i, _i, _i, _p, _p, _p, _p, _p, _p],
     "gisapr_score_sum_batch": [_p, _p, _p, _i, _i, _p],
+    "gisapr_tc_bank_bytes": [_i, _i],
+    "gisapr_tc_plan_work": [_p, _p, _i, _i, _i, _p, _i, _p],
+    "gisapr_correlate_tc_batch": [_p, _p, _p, C.c_longlong, _i, _i, _p, _p, _p, _p, _p, _i, _i, _i, _i, _i, _i,
+                                  _p, _p, _p, _p],
 }
+
+# functions that return something other than an int status
+RESTYPES = {"gisapr_tc_bank_bytes": C.c_longlong}
 
 _lib = None
 _lock = threading.Lock()
@@ -55,7 +62,7 @@ def load():
         for name, args in SIGNATURES.items():
             fn = getattr(lib, name)
             fn.argtypes = args
-            fn.restype = C.c_int
+            fn.restype = RESTYPES.get(name, C.c_int)
         lib.gisapr_last_error.argtypes = []
         lib.gisapr_last_error.restype = C.c_char_p
         _lib = lib

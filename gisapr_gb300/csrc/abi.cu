@@ -3,7 +3,9 @@
 #include <cuda_runtime.h>
 #include <cufft.h>
 
+#include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -52,6 +54,15 @@ cudaError_t launch_correlate_plain(cudaStream_t, const float2*, const float2*, c
 cudaError_t launch_particle_results(cudaStream_t, const int*, const float*, const int*, const int*,
                                     int, int, int*, int*, float*, int*, int*, float*, int);
 cudaError_t launch_score_sum(cudaStream_t, const int*, const float*, int, double*, int);
+int correlate_tc_max_psi();
+int correlate_tc_max_n();
+size_t correlate_tc_smem_bytes(int n, int crop);
+long long correlate_tc_bank_halves(int n_slot, int n);
+int correlate_tc_plan(const int*, const int*, int, int, int, int*, int);
+cudaError_t launch_bank_to_fp16(cudaStream_t, const float2*, long long, int, int, int, void*);
+cudaError_t launch_correlate_tc(cudaStream_t, const void*, int, int, const float2*, const int*, const int*,
+                                const int*, int, int, int, int, int, int, const float2*, const float2*, float*,
+                                int*, int*, int*, int);
 
 namespace {
 
@@ -90,6 +101,7 @@ struct BinTable {
 struct CorrTables {
   float2* outer = nullptr;  // [M][C]
   float2* col = nullptr;    // [H][C]
+  float2* row = nullptr;    // [n] exp(+2 pi i t / n)
 };
 
 }  // namespace
@@ -217,7 +229,15 @@ int get_corr_tables(gisapr_ctx ctx, int n, int crop, CorrTables* out) {
       col[(size_t)c * crop + xi] = make_float2((float)(w * std::cos(a)), (float)(w * std::sin(a)));
     }
   }
+  std::vector<float2> row(n);
+  for (int t = 0; t < n; ++t) {
+    const double a = two_pi * (double)t / (double)n;
+    row[t] = make_float2((float)std::cos(a), (float)std::sin(a));
+  }
   CorrTables t;
+  GISAPR_CHECK_CUDA(cudaMalloc(&t.row, row.size() * sizeof(float2)), "cudaMalloc(corr)");
+  GISAPR_CHECK_CUDA(cudaMemcpy(t.row, row.data(), row.size() * sizeof(float2), cudaMemcpyHostToDevice),
+                    "cudaMemcpy(corr)");
   GISAPR_CHECK_CUDA(cudaMalloc(&t.outer, outer.size() * sizeof(float2)), "cudaMalloc(corr)");
   GISAPR_CHECK_CUDA(cudaMalloc(&t.col, col.size() * sizeof(float2)), "cudaMalloc(corr)");
   GISAPR_CHECK_CUDA(cudaMemcpy(t.outer, outer.data(), outer.size() * sizeof(float2), cudaMemcpyHostToDevice),
@@ -503,6 +523,65 @@ int gisapr_correlate(gisapr_ctx ctx, void* stream, const float* bank, const floa
                                            local_ptr, local_idx, n_particles, n_psi, n, crop, t.outer, t.col,
                                            out_score, out_y, out_x, 1, 0, 0),
                     "correlate");
+  return GISAPR_OK;
+}
+
+long long gisapr_tc_bank_bytes(int n_slot, int n) {
+  if (n_slot < 0 || n <= 0) return 0;
+  return correlate_tc_bank_halves(n_slot, n) * 2;
+}
+
+int gisapr_tc_plan_work(const int* local_ptr, const int* local_idx, int n_particles, int n_cand, int n_psi,
+                        int* work, int max_work, int* n_work) {
+  if (!n_work) return fail(GISAPR_ERR_ARGUMENT, "n_work is NULL");
+  *n_work = 0;
+  if (n_particles < 0 || n_cand <= 0 || n_psi <= 0)
+    return fail(GISAPR_ERR_ARGUMENT, "n_particles < 0, n_cand <= 0 or n_psi <= 0");
+  if (n_particles == 0) return GISAPR_OK;
+  if (!local_ptr || !local_idx) return fail(GISAPR_ERR_ARGUMENT, "a required pointer is NULL");
+  for (int b = 0; b < n_particles; ++b)
+    if (local_ptr[b + 1] < local_ptr[b]) return fail(GISAPR_ERR_ARGUMENT, "local_ptr must be non-decreasing");
+  const int count = correlate_tc_plan(local_ptr, local_idx, n_particles, n_cand, n_psi, nullptr, 0);
+  if (work != nullptr) {
+    if (max_work < count) return fail(GISAPR_ERR_ARGUMENT, "work holds fewer than the planned items");
+    correlate_tc_plan(local_ptr, local_idx, n_particles, n_cand, n_psi, work, max_work);
+  }
+  *n_work = count;
+  return GISAPR_OK;
+}
+
+int gisapr_correlate_tc_batch(gisapr_ctx ctx, void* stream, const float* bank, long long bank_stride, int n_cand,
+                              int n_slot, void* tbank, const float* stack, const int* local_ptr,
+                              const int* local_idx, const int* work, int n_work, int nnz, int n_psi, int n, int crop,
+                              int split, float* out_score, int* out_y, int* out_x, int* status) {
+  if (!ctx) return fail(GISAPR_ERR_ARGUMENT, "context is NULL");
+  if (n_cand < 0 || n_slot < 0 || n_work < 0 || nnz < 0 || n_psi <= 0)
+    return fail(GISAPR_ERR_ARGUMENT, "n_cand, n_slot, n_work or nnz < 0, or n_psi <= 0");
+  if (n_cand == 0 || n_work == 0) return GISAPR_OK;
+  if (!bank || !tbank || !stack || !local_ptr || !local_idx || !work || !out_score || !out_y || !out_x)
+    return fail(GISAPR_ERR_ARGUMENT, "a required pointer is NULL");
+  if (n_slot == 0) return fail(GISAPR_ERR_ARGUMENT, "n_slot must be positive when there is work");
+  if (n_cand > 1 && bank_stride < (long long)n_slot * n * (n / 2 + 1))
+    return fail(GISAPR_ERR_ARGUMENT, "bank_stride is smaller than one candidate's bank");
+  if (n != 32 && n != 64 && n != 128)
+    return fail(GISAPR_ERR_UNSUPPORTED, "tensor-core correlation takes n in {32, 64, 128}");
+  if (crop < 2 || crop > 12 || crop % 2 != 0 || crop > n)
+    return fail(GISAPR_ERR_UNSUPPORTED, "tensor-core correlation takes an even crop in 2..12");
+  if (n_slot > 65535) return fail(GISAPR_ERR_ARGUMENT, "at most 65535 template slots");
+  if (((uintptr_t)tbank & 15) != 0) return fail(GISAPR_ERR_ARGUMENT, "tbank must be 16-byte aligned");
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  CorrTables t;
+  rc = get_corr_tables(ctx, n, crop, &t);
+  if (rc) return rc;
+  const cudaStream_t st = (cudaStream_t)stream;
+  GISAPR_CHECK_CUDA(launch_bank_to_fp16(st, (const float2*)bank, bank_stride, n_cand, n_slot, n, tbank),
+                    "bank_to_fp16");
+  const int grid = std::min(n_work, ctx->sm_count);
+  GISAPR_CHECK_CUDA(launch_correlate_tc(st, tbank, n_slot, n_cand, (const float2*)stack, local_ptr, local_idx, work,
+                                        n_work, n_psi, n, crop, nnz, split, t.row, t.col, out_score, out_y, out_x,
+                                        status, grid),
+                    "correlate_tc");
   return GISAPR_OK;
 }
 

@@ -13,6 +13,7 @@ run_search (v606:1749-1810) replaced by batched kernels.
 """
 from __future__ import annotations
 
+import ctypes as C
 import time
 from dataclasses import dataclass
 from typing import Dict, List, Optional, Sequence
@@ -229,6 +230,11 @@ class ScoringJob:
         return "".join(str(row) + "\n" for row in self.result_records())
 
 
+def idx_ptr(a: np.ndarray) -> C.c_void_p:
+    """Host address of a contiguous numpy array (for the host-side ABI helpers)."""
+    return C.c_void_p(a.ctypes.data)
+
+
 class BatchScoringJob:
     """Many candidates per launch sequence, replayed as one CUDA graph.
 
@@ -244,8 +250,13 @@ class BatchScoringJob:
     (ZL gisapr_batch_search.py:251-364).
     """
 
+    PRECISIONS = ("fp32", "fp16x3", "fp16")
+
     def __init__(self, job: ScoringJob, n_cand: int, models: Optional[Sequence] = None,
-                 model_of: Optional[Sequence[int]] = None, use_graph: bool = True):
+                 model_of: Optional[Sequence[int]] = None, use_graph: bool = True, precision: str = "fp32"):
+        if precision not in self.PRECISIONS:
+            raise ValueError(f"precision must be one of {self.PRECISIONS}, got {precision!r}")
+        self.precision = precision
         self.job = job
         self.n_cand = int(n_cand)
         self.models = list(models) if models else [job.density]
@@ -276,34 +287,95 @@ class BatchScoringJob:
         self.use_graph = bool(use_graph)
         self.graph = None
         self.stream = torch.cuda.Stream(dev)
+        if precision != "fp32":
+            self._setup_tensor_path(n_needed)
+
+    def _setup_tensor_path(self, n_needed: int) -> None:
+        """fp16 hi/lo bank scratch, direction-sorted work list and status word."""
+        job = self.job
+        lib = nat.load()
+        nb = job.cfg.new_box
+        self.n_slot = n_needed
+        per_cand = int(lib.gisapr_tc_bank_bytes(n_needed, nb))
+        self.tbank = torch.empty(self.n_cand * per_cand, dtype=torch.uint8, device=job.device)
+        ptr = np.ascontiguousarray(job.local_ptr.cpu().numpy(), dtype=np.int32)
+        idx = np.ascontiguousarray(job.local_idx.cpu().numpy(), dtype=np.int32)
+        count = C.c_int(0)
+        np_ = len(job.records)
+        nat.call("gisapr_tc_plan_work", idx_ptr(ptr), idx_ptr(idx), np_, self.n_cand, job.n_psi, None, 0,
+                 C.byref(count))
+        work = np.zeros((max(1, count.value), 2), dtype=np.int32)
+        nat.call("gisapr_tc_plan_work", idx_ptr(ptr), idx_ptr(idx), np_, self.n_cand, job.n_psi, idx_ptr(work),
+                 work.shape[0], C.byref(count))
+        self.n_work = count.value
+        self.work = torch.from_numpy(work).to(job.device)
+        self.tc_status = torch.zeros(1, dtype=torch.int32, device=job.device)
+
+    def check_status(self) -> None:
+        """Raise if an on-chip barrier wait of the tensor-core kernel ran out."""
+        if self.precision != "fp32" and int(self.tc_status.item()) != 0:
+            raise RuntimeError("tensor-core correlation: an on-chip barrier wait ran out; results are incomplete")
 
     KERNELS_PER_CANDIDATE = 3  # splat (2 launches) and projector, per slot
     KERNELS_PER_BATCH = 3      # correlation, records, score sums
 
     def launches_per_batch(self) -> int:
-        return self.n_cand * self.KERNELS_PER_CANDIDATE + self.KERNELS_PER_BATCH
+        extra = 1 if self.precision != "fp32" else 0  # fp16 hi/lo bank copy before the tensor-core kernel
+        return self.n_cand * self.KERNELS_PER_CANDIDATE + self.KERNELS_PER_BATCH + extra
 
-    def enqueue(self) -> None:
-        """Enqueue the whole batch on the current stream (poses already on the device)."""
+    def enqueue(self, marks: Optional[list] = None) -> None:
+        """Enqueue the whole batch on the current stream (poses already on the device).
+
+        ``marks``: when a list is given (eager runs only), a CUDA event is
+        recorded after each stage and appended as (stage, event)."""
         job = self.job
         dev = job.device
         ctx = nat.Context.for_device(dev).handle
         st = nat.stream_of(dev)
+
+        def mark(name):
+            if marks is not None:
+                ev = torch.cuda.Event(enable_timing=True)
+                ev.record()
+                marks.append((name, ev))
+
+        mark("start")
         for c in range(self.n_cand):
             self.models[self.model_of[c]].generate(None, write_padded=True, pose_device=self.poses_dev[c])
             job.projector.volume_spectrum(None)
             if job.needed:
                 job.projector.project(job.angles, job.needed_dirs, self.banks[c], job.needed_slots)
+        mark("templates")
         np_ = len(job.records)
-        nat.call("gisapr_correlate_batch", ctx, st, nat.ptr(self.banks), self.bank_stride, self.n_cand,
-                 nat.ptr(job.stack), nat.ptr(job.local_ptr), nat.ptr(job.local_idx), np_, job.nnz, job.n_psi,
-                 job.cfg.new_box, job.cfg.crop, nat.ptr(self.score_buf), nat.ptr(self.y_buf), nat.ptr(self.x_buf))
+        if self.precision == "fp32":
+            nat.call("gisapr_correlate_batch", ctx, st, nat.ptr(self.banks), self.bank_stride, self.n_cand,
+                     nat.ptr(job.stack), nat.ptr(job.local_ptr), nat.ptr(job.local_idx), np_, job.nnz, job.n_psi,
+                     job.cfg.new_box, job.cfg.crop, nat.ptr(self.score_buf), nat.ptr(self.y_buf),
+                     nat.ptr(self.x_buf))
+        else:
+            nat.call("gisapr_correlate_tc_batch", ctx, st, nat.ptr(self.banks), self.bank_stride, self.n_cand,
+                     self.n_slot, nat.ptr(self.tbank), nat.ptr(job.stack), nat.ptr(job.local_ptr),
+                     nat.ptr(job.local_idx), nat.ptr(self.work), self.n_work, job.nnz, job.n_psi, job.cfg.new_box,
+                     job.cfg.crop, 1 if self.precision == "fp16x3" else 0, nat.ptr(self.score_buf),
+                     nat.ptr(self.y_buf), nat.ptr(self.x_buf), nat.ptr(self.tc_status))
+        mark("correlate")
         nat.call("gisapr_particle_results_batch", st, nat.ptr(job.local_ptr), nat.ptr(self.score_buf),
                  nat.ptr(self.y_buf), nat.ptr(self.x_buf), np_, job.n_psi, self.n_cand, nat.ptr(self.best_entry),
                  nat.ptr(self.best_psi), nat.ptr(self.peak), nat.ptr(self.peak_y), nat.ptr(self.peak_x),
                  nat.ptr(self.zscore))
         nat.call("gisapr_score_sum_batch", st, nat.ptr(job.local_ptr), nat.ptr(self.peak), np_, self.n_cand,
                  nat.ptr(self.totals))
+        mark("records")
+
+    def stage_ms(self, poses) -> Dict[str, float]:
+        """Device time of each stage of one eager batch (CUDA events on the batch stream)."""
+        self.set_poses(poses)
+        marks: list = []
+        self.stream.wait_stream(torch.cuda.current_stream(self.job.device))
+        with torch.cuda.stream(self.stream):
+            self.enqueue(marks)
+        self.stream.synchronize()
+        return {marks[i][0]: marks[i - 1][1].elapsed_time(marks[i][1]) for i in range(1, len(marks))}
 
     def _ensure_graph(self) -> None:
         if self.graph is not None or not self.use_graph:
@@ -339,4 +411,5 @@ class BatchScoringJob:
         self.run()
         self.totals_host.copy_(self.totals, non_blocking=True)
         torch.cuda.current_stream(self.job.device).synchronize()
+        self.check_status()
         return self.totals_host.numpy().copy()

@@ -173,6 +173,33 @@ int gisapr_correlate_batch(gisapr_ctx ctx, void* stream, const float* bank, long
                            int nnz, int n_psi, int n, int crop, float* out_score, int* out_y, int* out_x);
 
 /*
+ * Tensor-core form of gisapr_correlate_batch (tcgen05 MMA, FP32 accumulate),
+ * same inputs and output layout. The stage that contracts template and
+ * particle columns over rows runs as a real GEMM on fp16 operands scaled by
+ * 2^13; split != 0 adds the hi*lo and lo*hi products of an fp16 hi/lo split
+ * (about 22 significant bits), split == 0 keeps hi*hi only. Replaces the
+ * same reference interfaces as gisapr_correlate_batch (v606:1418-1449 per
+ * candidate; ZL/gisapr_batch_search.py:314-349 for the candidate loop); the
+ * precision modes have no reference counterpart.
+ *   tbank: caller scratch of n_cand * gisapr_tc_bank_bytes(n_slot, n) bytes,
+ *     rewritten on every call (fp16 hi/lo copy of the banks);
+ *   work, n_work: device copy of the list made by gisapr_tc_plan_work
+ *     (host arrays in, host array out: [n_work][2] (particle, tile of 128
+ *     rows * psi groups + group of three psi angles), sorted by direction;
+ *     work == NULL only counts; n_psi must match the correlation call);
+ *   status: device int, set to 1 if an on-chip barrier wait ran out (the
+ *     outputs are then incomplete); the caller zeroes it.
+ * Sizes: n in {32, 64, 128}, crop even in 2..12.
+ */
+long long gisapr_tc_bank_bytes(int n_slot, int n);
+int gisapr_tc_plan_work(const int* local_ptr, const int* local_idx, int n_particles, int n_cand, int n_psi,
+                        int* work, int max_work, int* n_work);
+int gisapr_correlate_tc_batch(gisapr_ctx ctx, void* stream, const float* bank, long long bank_stride, int n_cand,
+                              int n_slot, void* tbank, const float* stack, const int* local_ptr,
+                              const int* local_idx, const int* work, int n_work, int nnz, int n_psi, int n, int crop,
+                              int split, float* out_score, int* out_y, int* out_x, int* status);
+
+/*
  * Per particle: first maximum over (local entry, psi), its crop position and
  * the z-score (peak - mean) / population sigma over all the particle's
  * scores. Replaces the numeric part of make_result_records (v606:1466-1491).

@@ -12,7 +12,7 @@ ROOT = Path(__file__).resolve().parent.parent
 def declared_functions():
     text = (ROOT / "include" / "gisapr_gb300.h").read_text()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(gisapr_\w+)\s*\(", text, flags=re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|long long|const char\*)\s+(gisapr_\w+)\s*\(", text, flags=re.M)))
 
 
 def test_header_declares_entry_points():
@@ -51,3 +51,33 @@ def test_cpu_device_is_rejected():
     from gisapr_gb300.pdb2mrc import density_from_coords
     with pytest.raises(ValueError):
         density_from_coords([[0, 0, 0]], [6], 32, 3.0, 6.0, device="cpu")
+
+
+def test_tensor_core_work_plan_on_host(native_lib):
+    """gisapr_tc_plan_work is host code: every (particle, tile of 128 rows)
+    appears once, tiles hold whole directions (row = direction * n_cand +
+    candidate) and the list is sorted by the tile's first direction."""
+    import numpy as np
+    from gisapr_gb300 import _native
+    lib = _native.load()
+    rng = np.random.default_rng(3)
+    counts = rng.integers(0, 9, size=40)
+    ptr = np.concatenate([[0], np.cumsum(counts)]).astype(np.int32)
+    idx = np.concatenate([np.sort(rng.choice(50, size=c, replace=False)) for c in counts]).astype(np.int32)
+    vp = lambda a: C.c_void_p(a.ctypes.data)
+    for n_cand, n_psi in ((1, 1), (5, 3), (64, 3), (200, 5), (7, 7)):
+        groups = -(-n_psi // 3)
+        n = C.c_int(-1)
+        assert lib.gisapr_tc_plan_work(vp(ptr), vp(idx), 40, n_cand, n_psi, None, 0, C.byref(n)) == 0
+        want = sum(-(-int(c) * n_cand // 128) for c in counts) * groups
+        assert n.value == want
+        work = np.zeros((max(1, want), 2), np.int32)
+        assert lib.gisapr_tc_plan_work(vp(ptr), vp(idx), 40, n_cand, n_psi, vp(work), want, C.byref(n)) == 0
+        pairs = {(int(b), int(t)) for b, t in work[:want]}
+        assert len(pairs) == want
+        keys = [int(idx[ptr[b] + ((t // groups) * 128) // n_cand]) for b, t in work[:want]]
+        assert keys == sorted(keys)
+        if want > 1:
+            assert lib.gisapr_tc_plan_work(vp(ptr), vp(idx), 40, n_cand, n_psi, vp(work), want - 1,
+                                           C.byref(n)) == 1
+    assert lib.gisapr_tc_bank_bytes(760, 128) == 760 * 65 * 2 * 256 * 2

@@ -60,9 +60,10 @@ size_t correlate_tc_smem_bytes(int n, int crop);
 long long correlate_tc_bank_halves(int n_slot, int n);
 int correlate_tc_plan(const int*, const int*, int, int, int, int*, int);
 cudaError_t launch_bank_to_fp16(cudaStream_t, const float2*, long long, int, int, int, void*);
-cudaError_t launch_correlate_tc(cudaStream_t, const void*, int, int, const float2*, const int*, const int*,
-                                const int*, int, int, int, int, int, int, const float2*, const float2*, float*,
-                                int*, int*, int*, int);
+int correlate_tc_max_cand();
+cudaError_t launch_correlate_tc(cudaStream_t, const void*, int, const float2*, const int*, const int*, const int*,
+                                int, int, int, int, int, int, const float2*, const float2*, float*, int*, int*, int*,
+                                int);
 
 namespace {
 
@@ -537,6 +538,8 @@ int gisapr_tc_plan_work(const int* local_ptr, const int* local_idx, int n_partic
   *n_work = 0;
   if (n_particles < 0 || n_cand <= 0 || n_psi <= 0)
     return fail(GISAPR_ERR_ARGUMENT, "n_particles < 0, n_cand <= 0 or n_psi <= 0");
+  if (n_cand > correlate_tc_max_cand())
+    return fail(GISAPR_ERR_ARGUMENT, "at most 128 candidates per tensor-core call");
   if (n_particles == 0) return GISAPR_OK;
   if (!local_ptr || !local_idx) return fail(GISAPR_ERR_ARGUMENT, "a required pointer is NULL");
   for (int b = 0; b < n_particles; ++b)
@@ -568,6 +571,8 @@ int gisapr_correlate_tc_batch(gisapr_ctx ctx, void* stream, const float* bank, l
   if (crop < 2 || crop > 12 || crop % 2 != 0 || crop > n)
     return fail(GISAPR_ERR_UNSUPPORTED, "tensor-core correlation takes an even crop in 2..12");
   if (n_slot > 65535) return fail(GISAPR_ERR_ARGUMENT, "at most 65535 template slots");
+  if (n_cand > correlate_tc_max_cand())
+    return fail(GISAPR_ERR_ARGUMENT, "at most 128 candidates per tensor-core call");
   if (((uintptr_t)tbank & 15) != 0) return fail(GISAPR_ERR_ARGUMENT, "tbank must be 16-byte aligned");
   int rc = set_device(ctx);
   if (rc) return rc;
@@ -578,9 +583,9 @@ int gisapr_correlate_tc_batch(gisapr_ctx ctx, void* stream, const float* bank, l
   GISAPR_CHECK_CUDA(launch_bank_to_fp16(st, (const float2*)bank, bank_stride, n_cand, n_slot, n, tbank),
                     "bank_to_fp16");
   const int grid = std::min(n_work, ctx->sm_count);
-  GISAPR_CHECK_CUDA(launch_correlate_tc(st, tbank, n_slot, n_cand, (const float2*)stack, local_ptr, local_idx, work,
-                                        n_work, n_psi, n, crop, nnz, split, t.row, t.col, out_score, out_y, out_x,
-                                        status, grid),
+  GISAPR_CHECK_CUDA(launch_correlate_tc(st, tbank, n_cand, (const float2*)stack, local_ptr, local_idx, work, n_work,
+                                        n_psi, n, crop, nnz, split, t.row, t.col, out_score, out_y, out_x, status,
+                                        grid),
                     "correlate_tc");
   return GISAPR_OK;
 }

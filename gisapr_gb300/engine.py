@@ -290,25 +290,35 @@ class BatchScoringJob:
         if precision != "fp32":
             self._setup_tensor_path(n_needed)
 
+    TC_MAX_CAND = 128  # candidates per tensor-core launch
+
     def _setup_tensor_path(self, n_needed: int) -> None:
-        """fp16 hi/lo bank scratch, direction-sorted work list and status word."""
+        """fp16 hi/lo bank scratch, direction-sorted work lists and status word.
+
+        Batches of more than 128 candidates run as equal chunks, one
+        tensor-core launch each (the tile shape depends on the chunk size)."""
         job = self.job
         lib = nat.load()
         nb = job.cfg.new_box
         self.n_slot = n_needed
+        n_chunks = -(-self.n_cand // self.TC_MAX_CAND)
+        size = -(-self.n_cand // n_chunks)
+        self.tc_chunks = [(c0, min(size, self.n_cand - c0)) for c0 in range(0, self.n_cand, size)]
         per_cand = int(lib.gisapr_tc_bank_bytes(n_needed, nb))
-        self.tbank = torch.empty(self.n_cand * per_cand, dtype=torch.uint8, device=job.device)
+        self.tbank = torch.empty(size * per_cand, dtype=torch.uint8, device=job.device)
         ptr = np.ascontiguousarray(job.local_ptr.cpu().numpy(), dtype=np.int32)
         idx = np.ascontiguousarray(job.local_idx.cpu().numpy(), dtype=np.int32)
-        count = C.c_int(0)
         np_ = len(job.records)
-        nat.call("gisapr_tc_plan_work", idx_ptr(ptr), idx_ptr(idx), np_, self.n_cand, job.n_psi, None, 0,
-                 C.byref(count))
-        work = np.zeros((max(1, count.value), 2), dtype=np.int32)
-        nat.call("gisapr_tc_plan_work", idx_ptr(ptr), idx_ptr(idx), np_, self.n_cand, job.n_psi, idx_ptr(work),
-                 work.shape[0], C.byref(count))
-        self.n_work = count.value
-        self.work = torch.from_numpy(work).to(job.device)
+        self.tc_plans = {}
+        for _, cc in self.tc_chunks:
+            if cc in self.tc_plans:
+                continue
+            count = C.c_int(0)
+            nat.call("gisapr_tc_plan_work", idx_ptr(ptr), idx_ptr(idx), np_, cc, job.n_psi, None, 0, C.byref(count))
+            work = np.zeros((max(1, count.value), 2), dtype=np.int32)
+            nat.call("gisapr_tc_plan_work", idx_ptr(ptr), idx_ptr(idx), np_, cc, job.n_psi, idx_ptr(work),
+                     work.shape[0], C.byref(count))
+            self.tc_plans[cc] = (torch.from_numpy(work).to(job.device), count.value)
         self.tc_status = torch.zeros(1, dtype=torch.int32, device=job.device)
 
     def check_status(self) -> None:
@@ -320,7 +330,8 @@ class BatchScoringJob:
     KERNELS_PER_BATCH = 3      # correlation, records, score sums
 
     def launches_per_batch(self) -> int:
-        extra = 1 if self.precision != "fp32" else 0  # fp16 hi/lo bank copy before the tensor-core kernel
+        # fp16 hi/lo bank copy and tensor-core kernel per chunk instead of one plain kernel
+        extra = 2 * len(self.tc_chunks) - 1 if self.precision != "fp32" else 0
         return self.n_cand * self.KERNELS_PER_CANDIDATE + self.KERNELS_PER_BATCH + extra
 
     def enqueue(self, marks: Optional[list] = None) -> None:
@@ -353,11 +364,15 @@ class BatchScoringJob:
                      job.cfg.new_box, job.cfg.crop, nat.ptr(self.score_buf), nat.ptr(self.y_buf),
                      nat.ptr(self.x_buf))
         else:
-            nat.call("gisapr_correlate_tc_batch", ctx, st, nat.ptr(self.banks), self.bank_stride, self.n_cand,
-                     self.n_slot, nat.ptr(self.tbank), nat.ptr(job.stack), nat.ptr(job.local_ptr),
-                     nat.ptr(job.local_idx), nat.ptr(self.work), self.n_work, job.nnz, job.n_psi, job.cfg.new_box,
-                     job.cfg.crop, 1 if self.precision == "fp16x3" else 0, nat.ptr(self.score_buf),
-                     nat.ptr(self.y_buf), nat.ptr(self.x_buf), nat.ptr(self.tc_status))
+            m = max(1, job.nnz) * job.n_psi
+            for c0, cc in self.tc_chunks:
+                work, n_work = self.tc_plans[cc]
+                nat.call("gisapr_correlate_tc_batch", ctx, st, nat.c_ptr_offset(self.banks, c0 * self.bank_stride * 8),
+                         self.bank_stride, cc, self.n_slot, nat.ptr(self.tbank), nat.ptr(job.stack),
+                         nat.ptr(job.local_ptr), nat.ptr(job.local_idx), nat.ptr(work), n_work, job.nnz, job.n_psi,
+                         job.cfg.new_box, job.cfg.crop, 1 if self.precision == "fp16x3" else 0,
+                         nat.c_ptr_offset(self.score_buf, c0 * m * 4), nat.c_ptr_offset(self.y_buf, c0 * m * 4),
+                         nat.c_ptr_offset(self.x_buf, c0 * m * 4), nat.ptr(self.tc_status))
         mark("correlate")
         nat.call("gisapr_particle_results_batch", st, nat.ptr(job.local_ptr), nat.ptr(self.score_buf),
                  nat.ptr(self.y_buf), nat.ptr(self.x_buf), np_, job.n_psi, self.n_cand, nat.ptr(self.best_entry),

@@ -65,19 +65,22 @@ def test_tensor_core_work_plan_on_host(native_lib):
     ptr = np.concatenate([[0], np.cumsum(counts)]).astype(np.int32)
     idx = np.concatenate([np.sort(rng.choice(50, size=c, replace=False)) for c in counts]).astype(np.int32)
     vp = lambda a: C.c_void_p(a.ctypes.data)
-    for n_cand, n_psi in ((1, 1), (5, 3), (64, 3), (200, 5), (7, 7)):
+    for n_cand, n_psi in ((1, 1), (5, 3), (64, 3), (128, 5), (48, 7), (100, 2)):
         groups = -(-n_psi // 3)
+        dpt = 128 // n_cand
         n = C.c_int(-1)
         assert lib.gisapr_tc_plan_work(vp(ptr), vp(idx), 40, n_cand, n_psi, None, 0, C.byref(n)) == 0
-        want = sum(-(-int(c) * n_cand // 128) for c in counts) * groups
+        want = sum(-(-int(c) // dpt) for c in counts) * groups
         assert n.value == want
         work = np.zeros((max(1, want), 2), np.int32)
         assert lib.gisapr_tc_plan_work(vp(ptr), vp(idx), 40, n_cand, n_psi, vp(work), want, C.byref(n)) == 0
         pairs = {(int(b), int(t)) for b, t in work[:want]}
         assert len(pairs) == want
-        keys = [int(idx[ptr[b] + ((t // groups) * 128) // n_cand]) for b, t in work[:want]]
+        keys = [int(idx[ptr[b] + (t // groups) * dpt]) for b, t in work[:want]]
         assert keys == sorted(keys)
         if want > 1:
             assert lib.gisapr_tc_plan_work(vp(ptr), vp(idx), 40, n_cand, n_psi, vp(work), want - 1,
                                            C.byref(n)) == 1
+    n = C.c_int(0)
+    assert lib.gisapr_tc_plan_work(vp(ptr), vp(idx), 40, 129, 3, None, 0, C.byref(n)) == 1
     assert lib.gisapr_tc_bank_bytes(760, 128) == 760 * 65 * 2 * 256 * 2

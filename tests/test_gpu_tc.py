@@ -157,6 +157,20 @@ def test_split_graph_replay_equals_eager(golden32):
                                   BatchScoringJob(job, 6, use_graph=False, precision="fp16x3").score_batch(poses2))
 
 
+def test_split_more_than_128_candidates_in_chunks(golden32):
+    """A batch above 128 candidates runs as equal chunks; each slot's scores
+    equal those of a batch holding only that slot's pose."""
+    g = golden32
+    job = _golden32_job(g)
+    poses = list(syn.candidate_poses(130, 31, 5.0, 3.0))
+    big = BatchScoringJob(job, len(poses), use_graph=False, precision="fp16x3")
+    assert [cc for _, cc in big.tc_chunks] == [65, 65]
+    got = big.score_batch(poses)
+    small = BatchScoringJob(job, 65, use_graph=False, precision="fp16x3")
+    np.testing.assert_array_equal(got[65:], small.score_batch(poses[65:]))
+    np.testing.assert_array_equal(got[:65], small.score_batch(poses[:65]))
+
+
 def test_tensor_path_rejects_unsupported_sizes(golden32):
     import ctypes as C
     from gisapr_gb300 import _native as nat
@@ -168,4 +182,7 @@ def test_tensor_path_rejects_unsupported_sizes(golden32):
         with pytest.raises(ValueError):
             nat.call("gisapr_correlate_tc_batch", ctx, st, p, 0, 1, 1, p, p, p, p, p, 1, 1, n_psi, n, crop, 1,
                      p, p, p, p)
+    with pytest.raises(ValueError):  # more than 128 candidates in one call
+        nat.call("gisapr_correlate_tc_batch", ctx, st, p, 1 << 10, 129, 1, p, p, p, p, p, 1, 1, 3, 128, 12, 1,
+                 p, p, p, p)
     _ = C

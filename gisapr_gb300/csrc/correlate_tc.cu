@@ -43,12 +43,13 @@
 
 namespace {
 
-constexpr int kTcThreads = 384;   // 12 warps: 3 per TMEM lane quarter
+constexpr int kTcThreads = 512;   // 16 warps in four warpgroups (roles below)
 constexpr int kTcM = 128;         // rows per tile (TMEM lanes)
 constexpr int kTcPsi = 3;         // psi angles per particle held by a tile
-constexpr int kTcMaxN = 128;      // half of K = n <= 128 per stage
+constexpr int kTcMaxN = 128;      // K = 2n <= 256, in steps of 64 (32 rows r)
+constexpr int kTcStages = 4;      // shared-memory ring of K steps
 constexpr int kTcMaxCand = 128;   // candidates per launch
-constexpr int kTcTmemCols = 256;  // two accumulator buffers of kN <= 80 columns
+constexpr int kTcTmemCols = 512;  // two MMA accumulators of kN <= 80 columns + stage-2 rows
 constexpr float kTcScale = 8192.0f;               // 2^13 on each operand
 constexpr float kTcUnscale = 1.0f / 67108864.0f;  // 2^-26 for the product
 constexpr unsigned kWaitLimit = 1u << 24;         // bounded mbarrier spin
@@ -76,17 +77,6 @@ struct TcParams {
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-// tcgen05 shared-memory matrix descriptor, no swizzle (K-major core matrices):
-// lbo = byte step between core matrices along K, sbo = between 8-row groups.
-__device__ __forceinline__ uint64_t make_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
-  uint64_t d = 0;
-  d |= (uint64_t)((addr & 0x3FFFF) >> 4);
-  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
-  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
-  d |= (uint64_t)1 << 46;  // descriptor version for tcgen05
-  return d;                // base offset 0, relative LBO, no swizzle
 }
 
 // kind::f16 instruction descriptor: FP32 accumulate, F16 A and B, both K-major.
@@ -126,6 +116,10 @@ __device__ __forceinline__ void bulk_copy(void* dst, const void* src, uint32_t b
       : "memory");
 }
 
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar)));
 }
@@ -149,62 +143,238 @@ __device__ __forceinline__ uint4 neg8(uint4 v) {
   return make_uint4(v.x ^ 0x80008000u, v.y ^ 0x80008000u, v.z ^ 0x80008000u, v.w ^ 0x80008000u);
 }
 
-// Accumulate stage 2 for the crop-row pair yp from a TMEM load of
-// (Re Z(2yp), Re Z(2yp+1), Im Z(2yp), Im Z(2yp+1)):
-// acc[yp][x] += (Re Z pair) * Er(x) - (Im Z pair) * Ei(x), with the twiddles
-// stored pre-broadcast as (Er, Er, -Ei, -Ei).
+// Stage 2 uses the symmetry of the crop twiddles E(c, x) = w_c e^{2 pi i c (x-h)/n}:
+// E(c, h-k) = conj E(c, h+k). With A_k = sum_c Re Z Re E(c, h+k) and
+// B_k = sum_c Im Z Im E(c, h+k), raw(h+k) = A_k - B_k and raw(h-k) = A_k + B_k
+// for k = 1..h-1, raw(h) = A_0, and raw(0) (no partner) is accumulated
+// directly. Accumulator slots per crop row: 0: A_0, 1: raw(0), 2..h: A_1..A_{h-1},
+// h+1..2h-1: B_1..B_{h-1}. The per-column twiddle table (floats, 16-byte
+// groups) holds Re E(h), Re E(0), -Im E(0), a pad entry, then Re E(h+k),
+// Im E(h+k) for k = 1..h-1.
+__host__ __device__ constexpr int tc_tw_entries(int C) { return ((C + 2 + 3) / 4) * 4; }
+
 // The twiddle loads are volatile so that they are not hoisted out of the
-// crop-row loop (that would hold 4 C more registers next to the accumulators).
+// crop-row loop (that would hold the table in registers next to the
+// accumulators).
 __device__ __forceinline__ float4 lds_v4(uint32_t addr) {
   float4 r;
   asm volatile("ld.shared.v4.f32 {%0,%1,%2,%3}, [%4];" : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w) : "r"(addr));
   return r;
 }
 
+// stage 2 for one crop row held in a[C] (Re Z = zr, Im Z = zi)
 template <int C>
-__device__ __forceinline__ void stage2_pair(float2 (&acc)[C / 2][C], const uint32_t (&v)[4], int yp,
-                                            uint32_t tw) {
-  const float2 zr = make_float2(__uint_as_float(v[0]), __uint_as_float(v[1]));
-  const float2 zi = make_float2(__uint_as_float(v[2]), __uint_as_float(v[3]));
+__device__ __forceinline__ void stage2_row(float (&a)[C], float zr, float zi, uint32_t tw) {
+  constexpr int h = C / 2;
+  const float4 e = lds_v4(tw);  // Re E(h), Re E(0), -Im E(0), pad
+  a[0] = fmaf(zr, e.x, a[0]);
+  a[1] = fmaf(zi, e.z, fmaf(zr, e.y, a[1]));
 #pragma unroll
-  for (int x = 0; x < C; ++x) {
-    const float4 e = lds_v4(tw + 16 * x);
-    acc[yp][x] = __ffma2_rn(zi, make_float2(e.z, e.w), acc[yp][x]);
-    acc[yp][x] = __ffma2_rn(zr, make_float2(e.x, e.y), acc[yp][x]);
+  for (int k = 1; k < h; k += 2) {
+    const float4 f = lds_v4(tw + 16 + 8 * (k - 1));  // k and k+1: Re E, Im E
+    a[1 + k] = fmaf(zr, f.x, a[1 + k]);
+    a[h + k] = fmaf(zi, f.y, a[h + k]);
+    if (k + 1 < h) {
+      a[2 + k] = fmaf(zr, f.z, a[2 + k]);
+      a[h + k + 1] = fmaf(zi, f.w, a[h + k + 1]);
+    }
   }
 }
 
+// TMEM load / store of one accumulator row (C 32-bit columns)
 template <int C>
+__device__ __forceinline__ void tmem_ld_row(float (&a)[C], uint32_t ta) {
+  static_assert(C == 12 || C == 10 || C == 8 || C == 6 || C == 4 || C == 2, "even crop up to 12");
+  uint32_t* r = reinterpret_cast<uint32_t*>(a);
+  if constexpr (C >= 8) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(ta));
+  }
+  if constexpr (C == 12 || C == 4) {
+    constexpr int o = C - 4;
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[o]), "=r"(r[o + 1]), "=r"(r[o + 2]), "=r"(r[o + 3])
+                 : "r"(ta + o));
+  }
+  if constexpr (C == 10 || C == 6 || C == 2) {
+    constexpr int o = C - 2;
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0,%1}, [%2];" : "=r"(r[o]), "=r"(r[o + 1]) : "r"(ta + o));
+  }
+  if constexpr (C == 6) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(ta));
+  }
+  asm volatile("tcgen05.wait::ld.sync.aligned;");
+}
+template <int C>
+__device__ __forceinline__ void tmem_st_row(const float (&a)[C], uint32_t ta) {
+  const uint32_t* r = reinterpret_cast<const uint32_t*>(a);
+  if constexpr (C >= 8) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(ta), "r"(r[0]),
+                 "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]));
+  }
+  if constexpr (C == 12 || C == 4) {
+    constexpr int o = C - 4;
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(ta + o), "r"(r[o]),
+                 "r"(r[o + 1]), "r"(r[o + 2]), "r"(r[o + 3]));
+  }
+  if constexpr (C == 10 || C == 6 || C == 2) {
+    constexpr int o = C - 2;
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x2.b32 [%0], {%1,%2};" ::"r"(ta + o), "r"(r[o]), "r"(r[o + 1]));
+  }
+  if constexpr (C == 6) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(ta), "r"(r[0]), "r"(r[1]),
+                 "r"(r[2]), "r"(r[3]));
+  }
+}
+
+// raw(y, x) of a crop row from its accumulator slots (see stage2_pair)
+template <int C>
+__device__ __forceinline__ float raw_at(const float (&a)[C], int x) {
+  constexpr int h = C / 2;
+  if (x == 0) return a[1];
+  if (x == h) return a[0];
+  if (x < h) return a[1 + (h - x)] + a[h + (h - x)];
+  return a[1 + (x - h)] - a[h + (x - h)];
+}
+
+// Entry j of column col's stage-2 twiddle table (see stage2_pair), times 2^-26.
+template <int C>
+__device__ __forceinline__ float tw_entry(const float2* __restrict__ tw_col, int col, int j) {
+  constexpr int h = C / 2;
+  const float2* e = tw_col + (size_t)col * C;
+  float v = 0.f;
+  if (j == 0) v = e[h].x;
+  else if (j == 1) v = e[0].x;
+  else if (j == 2) v = -e[0].y;
+  else if (j >= 4 && j < 4 + 2 * (h - 1)) {
+    const int k = 1 + (j - 4) / 2;
+    v = ((j - 4) & 1) ? e[h + k].y : e[h + k].x;
+  }
+  return v * kTcUnscale;
+}
+
+// tcgen05 shared-memory descriptor of a 128-byte-swizzled K-major tile
+// (8-row atoms of 1024 B; the leading byte offset is unused and set to 1).
+__device__ __forceinline__ uint64_t make_desc_sw128(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFF) >> 4);
+  d |= (uint64_t)1 << 16;             // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset: 8 rows x 128 B
+  d |= (uint64_t)1 << 46;             // descriptor version for tcgen05
+  d |= (uint64_t)2 << 61;             // 128-byte swizzle
+  return d;
+}
+
+// One K step (64 elements = four MMAs of K = 16) per pass: pass 0 A_hi*B_hi,
+// pass 1 A_hi*B_lo, pass 2 A_lo*B_hi; d accumulates unless first.
+__device__ __forceinline__ void issue_mma_step(uint32_t d, uint32_t a0, uint32_t b0, uint32_t a_part,
+                                               uint32_t b_part, uint32_t idesc, int n_pass, bool accumulate) {
+  uint32_t acc_in = accumulate ? 1u : 0u;
+  for (int pass = 0; pass < n_pass; ++pass) {
+    const uint32_t ap = a0 + (pass == 2 ? a_part : 0u);
+    const uint32_t bp = b0 + (pass == 1 ? b_part : 0u);
+#pragma unroll
+    for (int ks = 0; ks < 4; ++ks) {
+      const uint64_t ad = make_desc_sw128(ap + 32 * ks);
+      const uint64_t bd = make_desc_sw128(bp + 32 * ks);
+      asm volatile(
+          "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+          " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+          "l"(ad), "l"(bd), "r"(idesc), "r"(acc_in));
+      acc_in = 1;
+    }
+  }
+}
+
+// One work item as every role of the CTA sees it.
+struct TcItem {
+  const float2* pb;  // this particle's spectra from the group's first psi
+  int e0, a0, nd, psi0, g_psi;
+};
+
+__device__ __forceinline__ TcItem tc_item(const TcParams& P, int wi, int n, int H) {
+  const int n_groups = (P.n_psi + kTcPsi - 1) / kTcPsi;
+  const int b = P.work[2 * wi], tile = P.work[2 * wi + 1] / n_groups;
+  TcItem it;
+  it.psi0 = (P.work[2 * wi + 1] - tile * n_groups) * kTcPsi;
+  it.g_psi = min(kTcPsi, P.n_psi - it.psi0);
+  it.e0 = P.local_ptr[b];
+  const int d = P.local_ptr[b + 1] - it.e0;
+  it.a0 = tile * P.dpt;
+  it.nd = min(P.dpt, d - it.a0);
+  it.pb = P.stack + ((size_t)b * P.n_psi + it.psi0) * n * H;
+  return it;
+}
+
+// byte offset of 16-byte chunk c of row j in a 128-byte-swizzled K-major tile
+__device__ __forceinline__ uint32_t sw128(int j, int c) {
+  return (uint32_t)(j * 128 + ((c ^ (j & 7)) << 4));
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Warp roles (16 warps, 128 registers a thread): warp 0 issues the MMAs (one
+// elected lane), warp 1 the bulk copies of A, warps 2-3 build B, and warps
+// 4-15 accumulate stage 2 (warp 4 + 4 s + q reads TMEM lane quarter q for
+// psi s). Stage-2 rows [0, tc_reg_rows) live in registers and the rest in
+// TMEM columns after the two MMA accumulators, so every role fits the
+// 65,536-register file without spilling.
+template <int C>
+__host__ __device__ constexpr int tc_reg_rows() { return C * C <= 100 ? C : ((96 / C) & ~1); }
+constexpr int kTcEpiWarps = 12;
+constexpr int kTcBuilders = 64;  // threads of warps 2-3
+
+template <int C, int N>
 __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   static_assert(C % 2 == 0 && C <= 12, "even crop up to 12");
+  static_assert(kTcThreads == 512, "four warpgroups");
   constexpr int kN = tc_n(C);
   constexpr int kPS = tc_psi_stride(C);
   constexpr int h = C / 2;
-  const int n = P.n, H = n / 2 + 1, n_psi = P.n_psi, n_cand = P.n_cand;
-  const int kc_n = n / 8;                                      // 16-byte K chunks per half
-  const uint32_t a_part = (uint32_t)kc_n * kTcM * 16;          // bytes of A (hi or lo) per stage
-  const uint32_t lbo_b = kN * 16 + 16;                         // B chunk stride, padded so chunks spread banks
-  const uint32_t b_part = (uint32_t)kc_n * lbo_b;
-  const uint32_t stage_bytes = 2 * a_part + 2 * b_part;
-  unsigned char* stages = smem_raw;                            // [2][A hi, A lo, B hi, B lo]
-  float2* s_p = reinterpret_cast<float2*>(smem_raw + 2 * stage_bytes);  // [kTcPsi][n] scaled column
-  float2* s_twr = s_p + kTcPsi * n;                            // [n]
-  float4* s_twc = reinterpret_cast<float4*>(s_twr + n);        // [2][16] (Er, Er, -Ei, -Ei) times 2^-26
-  uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_twc + 32);   // full[2], empty[2], tmem[2]
-  uint32_t* s_taddr = reinterpret_cast<uint32_t*>(s_bar + 6);
+  constexpr int S = kTcStages;
+  constexpr int NQ = N / 32;               // K steps per column: 32 rows r (64 K) each
+  constexpr int n = N, H = N / 2 + 1;
+  constexpr uint32_t a_part = kTcM * 128;  // bytes of A (hi or lo) per stage: 128 rows x 128 B
+  constexpr uint32_t b_part = kN * 128;
+  constexpr uint32_t stage_bytes = 2 * a_part + 2 * b_part;
+  static_assert(stage_bytes % 1024 == 0, "stages keep the 1024-byte swizzle alignment");
+  const int n_cand = P.n_cand;
+  const int nc8 = (n_cand + 7) & ~7;       // rows per direction in a tile
+  unsigned char* stages = smem_raw;        // [S][A hi, A lo, B hi, B lo]
+  float2* s_p = reinterpret_cast<float2*>(smem_raw + S * stage_bytes);  // [3][kTcPsi][n] particle columns
+  float2* s_twr = s_p + 3 * kTcPsi * n;                        // [n]
+  float* s_twall = reinterpret_cast<float*>(s_twr + n);      // [H][tc_tw_entries] column tables
+  uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_twall + H * tc_tw_entries(C));
+  uint64_t* bar_afull = s_bar;           // [S] A bytes landed (copy warp's expect_tx)
+  uint64_t* bar_bfull = s_bar + S;       // [S] both builder warps wrote B
+  uint64_t* bar_empty = s_bar + 2 * S;   // [S] the MMAs reading the stage are done
+  uint64_t* bar_tfull = s_bar + 3 * S;   // [2] a column's accumulator is final
+  uint64_t* bar_tempty = s_bar + 3 * S + 2;  // [2] every stage-2 warp read its accumulator
+  uint32_t* s_taddr = reinterpret_cast<uint32_t*>(s_bar + 3 * S + 4);
   int* s_fail = reinterpret_cast<int*>(s_taddr + 1);
-  int* s_slot = s_fail + 1;                                    // [kTcM] template slot per tile direction
-  uint64_t* bar_full = s_bar;
-  uint64_t* bar_empty = s_bar + 2;
-  uint64_t* bar_tmem = s_bar + 4;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   for (int t = tid; t < n; t += blockDim.x) s_twr[t] = P.tw_row[t];
-  for (uint32_t t = tid; t < 2 * stage_bytes / 16; t += blockDim.x)
+  for (int t = tid; t < H * tc_tw_entries(C); t += blockDim.x)
+    s_twall[t] = tw_entry<C>(P.tw_col, t / tc_tw_entries(C), t % tc_tw_entries(C));
+  for (uint32_t t = tid; t < S * stage_bytes / 16; t += blockDim.x)
     reinterpret_cast<uint4*>(stages)[t] = make_uint4(0, 0, 0, 0);
   if (tid == 0) {
-    for (int i = 0; i < 6; ++i) mbar_init(s_bar + i, 1);
+    for (int i = 0; i < S; ++i) {
+      mbar_init(bar_afull + i, 1);
+      mbar_init(bar_bfull + i, 2);
+      mbar_init(bar_empty + i, 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(bar_tfull + i, 1);
+      mbar_init(bar_tempty + i, kTcEpiWarps);
+    }
     *s_fail = 0;
     asm volatile("fence.mbarrier_init.release.cluster;");
   }
@@ -213,251 +383,316 @@ __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
                  "r"(kTcTmemCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
+  asm volatile("fence.proxy.async.shared::cta;");
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t taddr = *s_taddr;
-  const uint32_t idesc = make_idesc(kTcM, kN);
-  const int parts = P.split ? 2 : 1;
-  const int n_pass = P.split ? 3 : 1;
-  uint32_t uses[2] = {0, 0};        // commits issued per stage (one per use)
-  uint32_t tmem_waits[2] = {0, 0};  // completions consumed per TMEM buffer
-  bool ok = true;
 
-  // epilogue role: TMEM lane quarter q (warp % 4 by the tcgen05.ld rule), psi
-  const int q = warp & 3, my_psi = warp >> 2;
-  const int my_row = 32 * q + lane;
-  const int n_groups = (n_psi + kTcPsi - 1) / kTcPsi;
-  int zeroed_from = kTcM;  // rows [zeroed_from, 128) of A are zero in both stages
+  // bounded wait that gives up at once after any failure in the CTA
+  auto wait = [&](uint64_t* bar, uint32_t parity) -> bool {
+    if (*reinterpret_cast<volatile int*>(s_fail) != 0) return false;
+    const bool r = mbar_wait(bar, parity);
+    if (!r) *reinterpret_cast<volatile int*>(s_fail) = 1;
+    return r;
+  };
 
-  for (int wi = blockIdx.x; wi < P.n_work && ok; wi += gridDim.x) {
-    const int b = P.work[2 * wi], tile = P.work[2 * wi + 1] / n_groups;
-    const int psi0 = (P.work[2 * wi + 1] - tile * n_groups) * kTcPsi;
-    const int g_psi = min(kTcPsi, n_psi - psi0);  // psi angles in this group
-    const int e0 = P.local_ptr[b], d = P.local_ptr[b + 1] - e0;
-    const int a0 = tile * P.dpt, nd = min(P.dpt, d - a0);
-    const int used = nd * n_cand;
-    if (tid < nd) s_slot[tid] = P.local_idx[e0 + a0 + tid];
-    if (used < zeroed_from) {
-      // rows this tile leaves empty must read as zero (no MMA is in flight here)
-      const int nz = zeroed_from - used;  // rows [used, zeroed_from) per K chunk
-      const int per_chunk = nz;           // 16-byte rows per (stage, part, chunk)
-      const int total = 2 * 2 * kc_n * per_chunk;
-      for (int t = tid; t < total; t += blockDim.x) {
-        const int row = used + t % per_chunk;
-        const int rest = t / per_chunk;
-        const int kc = rest % kc_n, sp = rest / kc_n;  // sp = stage * 2 + part
-        unsigned char* base = stages + (sp >> 1) * stage_bytes + (sp & 1) * a_part;
-        *reinterpret_cast<uint4*>(base + (size_t)kc * kTcM * 16 + row * 16) = make_uint4(0, 0, 0, 0);
-      }
-      asm volatile("fence.proxy.async.shared::cta;");
-    }
-    zeroed_from = used;
-    __syncthreads();
-    const int jrows = g_psi * kPS;
-    const int b_tasks = g_psi * C * (n / 16);  // (psi, y, 8-row chunk) per half
-    float2 acc[C / 2][C];  // .x: crop row 2yp, .y: crop row 2yp + 1
-#pragma unroll
-    for (int yp = 0; yp < C / 2; ++yp)
-#pragma unroll
-      for (int x = 0; x < C; ++x) acc[yp][x] = make_float2(0.f, 0.f);
-    const float2* Pb = P.stack + ((size_t)b * n_psi + psi0) * n * H;
-    (void)jrows;
-
-    for (int col = 0; col <= H && ok; ++col) {
-      if (col < H) {
-        for (int hh = 0; hh < 2; ++hh) {
-          unsigned char* stA = stages + hh * stage_bytes;
-          unsigned char* stB = stA + 2 * a_part;
-          if (uses[hh] > 0) {
-            // the MMAs that last read this stage are done
-            const bool done = mbar_wait(bar_empty + hh, (uses[hh] - 1) & 1u);
-            ok = __syncthreads_and(done ? 1 : 0) != 0;
-            if (!ok) break;
-          }
-          // ---- A: one bulk copy per (part, K chunk, direction), n_cand rows of 16 B
-          if (warp == 0) {
-            const uint32_t chunk = (uint32_t)n_cand * 16;
-            if (lane == 0) mbar_expect_tx(bar_full + hh, (uint32_t)(parts * kc_n * nd) * chunk);
-            __syncwarp();
-            for (int qd = lane; qd < parts * kc_n * nd; qd += 32) {
-              const int part = qd / (kc_n * nd), rem = qd - part * (kc_n * nd);
-              const int kc = rem / nd, dl = rem - kc * nd;
-              const __half* src = P.tbank + ((((size_t)s_slot[dl] * H + col) * 2 + hh) * 2 + part) *
-                                                (size_t)kc_n * n_cand * 8 +
-                                  (size_t)kc * n_cand * 8;
-              bulk_copy(stA + part * a_part + (uint32_t)kc * kTcM * 16 + (uint32_t)dl * chunk, src, chunk,
-                        bar_full + hh);
-            }
-          }
-          if (hh == 0) {
-            for (int t = tid; t < g_psi * n; t += blockDim.x) {
-              const int s = t / n, r = t - s * n;
-              s_p[t] = cscale(__ldg(Pb + ((size_t)s * n + r) * H + col), kTcScale);
-            }
-            if (tid < C) {
-              const float2 e = P.tw_col[(size_t)col * C + tid];
-              const float er = e.x * kTcUnscale, ei = -e.y * kTcUnscale;
-              s_twc[(col & 1) * 16 + tid] = make_float4(er, er, ei, ei);
-            }
-            __syncthreads();
-          }
-          // ---- B for this half: rows r in [hh n/2, hh n/2 + n/2), chunk kc < n/16 holds
-          // Re (part-0 row) / Im (part-1 row), chunk n/16 + kc holds -Im / Re
-          for (int t = tid; t < b_tasks; t += blockDim.x) {
-            const int yi = t % C, rest = t / C;
-            const int s = rest % g_psi, rc = rest / g_psi;
-            const int y = yi - h;
-            const int r0 = hh * (n / 2) + rc * 8;
-            float2 tw = s_twr[(r0 * y) & (n - 1)];
-            const float2 step = s_twr[y & (n - 1)];
-            float re[8], im[8];
-            const float2* pp = s_p + s * n + r0;
-#pragma unroll
-            for (int i = 0; i < 8; ++i) {
-              const float2 u = cmul(pp[i], tw);
-              re[i] = u.x;
-              im[i] = u.y;
-              tw = cmul(tw, step);
-            }
-            // rows of psi s: per crop-row pair (Re y, Re y+1, Im y, Im y+1)
-            const int jr = s * kPS + 4 * (yi >> 1) + (yi & 1), ji = jr + 2;
-            unsigned char* c_re = stB + (uint32_t)rc * lbo_b;
-            unsigned char* c_im = stB + (uint32_t)(n / 16 + rc) * lbo_b;
-            uint4 hi, lo;
-            split8(re, hi, lo);  // Re U: Re-Z row first half, Im-Z row second half
-            *reinterpret_cast<uint4*>(c_re + jr * 16) = hi;
-            *reinterpret_cast<uint4*>(c_im + ji * 16) = hi;
-            if (P.split) {
-              *reinterpret_cast<uint4*>(c_re + b_part + jr * 16) = lo;
-              *reinterpret_cast<uint4*>(c_im + b_part + ji * 16) = lo;
-            }
-            split8(im, hi, lo);  // Im U: Im-Z row first half, negated in the Re-Z row second half
-            *reinterpret_cast<uint4*>(c_re + ji * 16) = hi;
-            *reinterpret_cast<uint4*>(c_im + jr * 16) = neg8(hi);
-            if (P.split) {
-              *reinterpret_cast<uint4*>(c_re + b_part + ji * 16) = lo;
-              *reinterpret_cast<uint4*>(c_im + b_part + jr * 16) = neg8(lo);
-            }
-          }
-          asm volatile("fence.proxy.async.shared::cta;");
-          asm volatile("tcgen05.fence::before_thread_sync;");
-          __syncthreads();
-          asm volatile("tcgen05.fence::after_thread_sync;");
-          // ---- stage 1 on the tensor cores: hi*hi [+ hi*lo + lo*hi] over this half
-          if (tid == 0) {
-            if (!mbar_wait(bar_full + hh, uses[hh] & 1u)) {
-              *s_fail = 1;
-            } else {
+  if (warp < 4) {
+    if (warp == 0) {
+      // ---------------- MMA issue (one lane)
+      if (lane == 0) {
+        uint32_t g = 0, tuse[2] = {0, 0};
+        const uint32_t idesc = make_idesc(kTcM, kN);
+        bool ok = true;
+        for (int wi = blockIdx.x; wi < P.n_work && ok; wi += gridDim.x) {
+          for (int col = 0; col < H && ok; ++col) {
+            const int tb = col & 1;
+            for (int qq = 0; qq < NQ && ok; ++qq, ++g) {
+              const uint32_t st = g % S;
+              if (qq == 0 && tuse[tb] > 0) ok = wait(bar_tempty + tb, (tuse[tb] - 1) & 1u);
+              ok = ok && wait(bar_bfull + st, (g / S) & 1u) && wait(bar_afull + st, (g / S) & 1u);
+              if (!ok) break;
               asm volatile("tcgen05.fence::after_thread_sync;");
-              const uint32_t a0s = smem_u32(stA), b0s = smem_u32(stB);
-              const uint32_t dt = taddr + (uint32_t)((col & 1) * kN);
-              const uint32_t lbo_a = kTcM * 16;
-              uint32_t acc_in = hh;
-              for (int pass = 0; pass < n_pass; ++pass) {
-                const uint32_t ap = a0s + (pass == 2 ? a_part : 0u);
-                const uint32_t bp = b0s + (pass == 1 ? b_part : 0u);
-                for (int ks = 0; ks < kc_n / 2; ++ks) {
-                  const uint64_t ad = make_desc(ap + (uint32_t)ks * 2 * lbo_a, lbo_a, 128);
-                  const uint64_t bd = make_desc(bp + (uint32_t)ks * 2 * lbo_b, lbo_b, 128);
-                  asm volatile(
-                      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dt),
-                      "l"(ad), "l"(bd), "r"(idesc), "r"(acc_in));
-                  acc_in = 1;
+              const uint32_t a0s = smem_u32(stages + st * stage_bytes);
+              issue_mma_step(taddr + (uint32_t)(tb * kN), a0s, a0s + 2 * a_part, a_part, b_part, idesc,
+                             P.split ? 3 : 1, qq > 0);
+              mma_commit(bar_empty + st);
+              if (qq == NQ - 1) {
+                mma_commit(bar_tfull + tb);
+                ++tuse[tb];
+              }
+            }
+          }
+        }
+      }
+    } else if (warp == 1) {
+      // ---------------- A: one bulk copy of n_cand 128-byte rows per (part, direction) and step
+      const int parts = P.split ? 2 : 1;
+      const uint32_t bytes = (uint32_t)n_cand * 128;
+      uint32_t g = 0;
+      int zeroed[S];  // rows [zeroed[s], 128) of stage s read as zero
+#pragma unroll
+      for (int s = 0; s < S; ++s) zeroed[s] = 0;
+      bool ok = true;
+      for (int wi = blockIdx.x; wi < P.n_work && ok; wi += gridDim.x) {
+        const TcItem it = tc_item(P, wi, n, H);
+        const int used = it.nd * nc8;
+        int slot = 0;
+        if (lane < parts * it.nd) slot = P.local_idx[it.e0 + it.a0 + lane % it.nd];
+        for (int col = 0; col < H && ok; ++col) {
+          for (int qq = 0; qq < NQ && ok; ++qq, ++g) {
+            const uint32_t st = g % S;
+            unsigned char* stA = stages + st * stage_bytes;
+            if (g >= (uint32_t)S) {
+              bool w = true;
+              if (lane == 0) w = wait(bar_empty + st, (g / S - 1) & 1u);
+              ok = __shfl_sync(0xffffffffu, w ? 1 : 0, 0) != 0;
+              if (!ok) break;
+            }
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+              if (s == (int)st && used < zeroed[s]) {
+                // rows this tile leaves empty must read as zero
+                for (int t = lane; t < 2 * (zeroed[s] - used) * 8; t += 32) {
+                  const int row = used + (t >> 3) % (zeroed[s] - used), part = (t >> 3) / (zeroed[s] - used);
+                  *reinterpret_cast<uint4*>(stA + part * a_part + row * 128 + (t & 7) * 16) =
+                      make_uint4(0, 0, 0, 0);
+                }
+                asm volatile("fence.proxy.async.shared::cta;");
+                __syncwarp();
+              }
+              if (s == (int)st) zeroed[s] = used;
+            }
+            if (lane == 0) mbar_expect_tx(bar_afull + st, (uint32_t)(parts * it.nd) * bytes);
+            __syncwarp();
+            if (lane < parts * it.nd) {
+              const int part = lane / it.nd, dl = lane - part * it.nd;
+              const __half* src =
+                  P.tbank + ((((size_t)slot * H + col) * NQ + qq) * 2 + part) * (size_t)n_cand * 64;
+              bulk_copy(stA + part * a_part + (uint32_t)dl * nc8 * 128, src, bytes, bar_afull + st);
+            }
+          }
+        }
+      }
+    } else {
+      // ---------------- B: U_{s,y}(r) = P_s(r, col) w^{r y}, scaled and split, per K step
+      // Both builder warps always run the same sequence of named barriers (no
+      // early exit): after a failure they only skip the work.
+      const int bt = tid - 64;  // 0..63
+      uint32_t g = 0;
+      bool ok = true;
+      for (int wi = blockIdx.x; wi < P.n_work; wi += gridDim.x) {
+        const TcItem it = tc_item(P, wi, n, H);
+        const int g_psi = it.g_psi;
+        // columns 0 and 1 of this particle; later columns arrive by cp.async two
+        // columns ahead (one group per column and thread)
+        asm volatile("bar.sync 1, 64;" ::: "memory");  // both builders left the previous item
+        for (int t = bt; t < g_psi * n; t += kTcBuilders) {
+          const int s = t / n, r = t - s * n;
+          const float2* pcol = it.pb + ((size_t)s * n + r) * H;
+          s_p[t] = __ldg(pcol);
+          s_p[kTcPsi * n + t] = __ldg(pcol + 1);
+        }
+        for (int col = 0; col < H; ++col) {
+          asm volatile("cp.async.wait_group 1;" ::: "memory");
+          asm volatile("bar.sync 1, 64;" ::: "memory");  // column col visible; column col-1 finished by both
+          if (col + 2 < H) {
+            for (int t = bt; t < g_psi * n; t += kTcBuilders) {
+              const int s = t / n, r = t - s * n;
+              cp_async8(s_p + ((col + 2) % 3) * kTcPsi * n + t, it.pb + ((size_t)s * n + r) * H + col + 2);
+            }
+          }
+          asm volatile("cp.async.commit_group;");
+          const float2* sp = s_p + (col % 3) * kTcPsi * n;
+          for (int qq = 0; qq < NQ; ++qq, ++g) {
+            const uint32_t st = g % S;
+            unsigned char* stB = stages + st * stage_bytes + 2 * a_part;
+            if (g >= (uint32_t)S) ok = wait(bar_empty + st, (g / S - 1) & 1u) && ok;
+            const int b_tasks = ok ? g_psi * C * 4 : 0;
+            for (int t = bt; t < b_tasks; t += kTcBuilders) {
+              const int yi = t % C, rest = t / C;
+              const int s = rest % g_psi, rc = rest / g_psi;
+              const int y = yi - h;
+              const int r0 = qq * 32 + rc * 8;
+              const float2 tw0 = cscale(s_twr[(r0 * y) & (n - 1)], kTcScale);  // the operand scale
+              const float2 step = s_twr[y & (n - 1)];
+              const float2* pp = sp + s * n + r0;
+              // rows of psi s: per crop-row pair (Re y, Re y+1, Im y, Im y+1)
+              const int jr = s * kPS + 4 * (yi >> 1) + (yi & 1), ji = jr + 2;
+#pragma unroll
+              for (int part = 0; part < 2; ++part) {
+                // part 0: Re U -> Re-Z row first half, Im-Z row second half;
+                // part 1: Im U -> Im-Z row first half, -Im U in the Re-Z row second half
+                float2 tw = tw0;
+                uint32_t hw[4], lw[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                  const float2 u0 = cmul(pp[2 * i], tw);
+                  tw = cmul(tw, step);
+                  const float2 u1 = cmul(pp[2 * i + 1], tw);
+                  tw = cmul(tw, step);
+                  const float a = part ? u0.y : u0.x, b = part ? u1.y : u1.x;
+                  const __half2 hv = __floats2half2_rn(a, b);
+                  const float2 hf = __half22float2(hv);
+                  const __half2 lv = __floats2half2_rn(a - hf.x, b - hf.y);
+                  hw[i] = *reinterpret_cast<const uint32_t*>(&hv);
+                  lw[i] = *reinterpret_cast<const uint32_t*>(&lv);
+                }
+                const uint4 hi = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+                const uint4 lo = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+                const int j1 = part ? ji : jr, j2 = part ? jr : ji;
+                *reinterpret_cast<uint4*>(stB + sw128(j1, rc)) = hi;
+                *reinterpret_cast<uint4*>(stB + sw128(j2, 4 + rc)) = part ? neg8(hi) : hi;
+                if (P.split) {
+                  *reinterpret_cast<uint4*>(stB + b_part + sw128(j1, rc)) = lo;
+                  *reinterpret_cast<uint4*>(stB + b_part + sw128(j2, 4 + rc)) = part ? neg8(lo) : lo;
                 }
               }
-              mma_commit(bar_empty + hh);
-              if (hh == 1) mma_commit(bar_tmem + (col & 1));
             }
-          }
-          ++uses[hh];
-        }
-        if (!ok) break;
-      }
-      if (col > 0) {
-        // ---- stage 2 for column col-1 while the tensor cores run column col
-        const int pb = (col - 1) & 1;
-        const bool done = mbar_wait(bar_tmem + pb, tmem_waits[pb] & 1u);
-        ++tmem_waits[pb];
-        ok = __syncthreads_and((done && *s_fail == 0) ? 1 : 0) != 0;
-        if (!ok) break;
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        if (my_psi < g_psi) {
-          const uint32_t ta = taddr + ((uint32_t)(32 * q) << 16) + (uint32_t)(pb * kN + my_psi * kPS);
-          const uint32_t tw = smem_u32(s_twc + pb * 16);
-          uint32_t v[4];
-#pragma unroll
-          for (int yp = 0; yp < C / 2; ++yp) {
-            asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
-                         : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3])
-                         : "r"(ta + 4 * yp));
-            asm volatile("tcgen05.wait::ld.sync.aligned;");
-            stage2_pair<C>(acc, v, yp, tw);
+            asm volatile("fence.proxy.async.shared::cta;");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(bar_bfull + st);
           }
         }
-        asm volatile("tcgen05.fence::before_thread_sync;");
+        asm volatile("cp.async.wait_all;" ::: "memory");
       }
     }
-    if (!ok) break;
-    // ---- first maximum of this (row, psi) map, row-major over (y, x)
-    if (my_psi < g_psi && my_row < used) {
+  } else {
+    // ---------------- stage 2 and the first maximum per (row, psi)
+    constexpr int RR = tc_reg_rows<C>();  // crop rows in registers; rows [RR, C) in TMEM
+    const int q4 = warp & 3, my_psi = (warp - 4) >> 2;
+    const int my_row = 32 * q4 + lane;
+    const uint32_t lane_off = (uint32_t)(32 * q4) << 16;
+    const uint32_t ta_z = taddr + lane_off + (uint32_t)(my_psi * kPS);
+    const uint32_t ta_acc = taddr + lane_off + (uint32_t)(2 * kN + my_psi * (C - RR) * C);
+    const uint32_t tw0 = smem_u32(s_twall);
+    uint32_t tuse[2] = {0, 0};
+    bool ok = true;
+    for (int wi = blockIdx.x; wi < P.n_work && ok; wi += gridDim.x) {
+      const bool active = my_psi < tc_item(P, wi, n, H).g_psi;  // warp-uniform; the rest is re-read at the end
+      float acc[RR][C];  // [crop row][slot]
+#pragma unroll
+      for (int y = 0; y < RR; ++y)
+#pragma unroll
+        for (int j = 0; j < C; ++j) acc[y][j] = 0.f;
+      if constexpr (RR < C) {
+        float z[C];
+#pragma unroll
+        for (int j = 0; j < C; ++j) z[j] = 0.f;
+#pragma unroll
+        for (int y = RR; y < C; ++y) tmem_st_row<C>(z, ta_acc + (uint32_t)((y - RR) * C));
+        asm volatile("tcgen05.wait::st.sync.aligned;");
+      }
+      for (int col = 0; col < H && ok; ++col) {
+        const int tb = col & 1;
+        ok = wait(bar_tfull + tb, tuse[tb] & 1u);
+        ++tuse[tb];
+        if (!ok) break;
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        if (active) {
+          const uint32_t tw = tw0 + (uint32_t)(col * tc_tw_entries(C) * 4);
+          const uint32_t tz = ta_z + (uint32_t)(tb * kN);
+#pragma unroll
+          for (int yp = 0; yp < C / 2; ++yp) {
+            uint32_t v[4];  // Re Z(2yp), Re Z(2yp+1), Im Z(2yp), Im Z(2yp+1)
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                         : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3])
+                         : "r"(tz + 4 * yp));
+            asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+            for (int hy = 0; hy < 2; ++hy) {
+              const int y = 2 * yp + hy;
+              const float zr = __uint_as_float(v[hy]), zi = __uint_as_float(v[2 + hy]);
+              if (y < RR) {
+                stage2_row<C>(acc[y < RR ? y : 0], zr, zi, tw);
+              } else {
+                float a[C];
+                tmem_ld_row<C>(a, ta_acc + (uint32_t)((y - RR) * C));
+                stage2_row<C>(a, zr, zi, tw);
+                tmem_st_row<C>(a, ta_acc + (uint32_t)((y - RR) * C));
+              }
+            }
+          }
+          asm volatile("tcgen05.wait::st.sync.aligned;");
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(bar_tempty + tb);
+      }
+      if (!ok) break;
+      // the first maximum, row-major over (y, x): register rows, then TMEM rows
       float best = -INFINITY;
       int bi = 0;
 #pragma unroll
-      for (int yp = 0; yp < C / 2; ++yp) {
+      for (int y = 0; y < RR; ++y) {
 #pragma unroll
-        for (int x = 0; x < C; ++x)
-          if (acc[yp][x].x > best) {
-            best = acc[yp][x].x;
-            bi = 2 * yp * C + x;
+        for (int x = 0; x < C; ++x) {
+          const float v = raw_at<C>(acc[y], x);
+          if (v > best) {
+            best = v;
+            bi = y * C + x;
           }
-#pragma unroll
-        for (int x = 0; x < C; ++x)
-          if (acc[yp][x].y > best) {
-            best = acc[yp][x].y;
-            bi = (2 * yp + 1) * C + x;
-          }
+        }
       }
-      const int dl = my_row / n_cand, cand = my_row - dl * n_cand;
-      const size_t o = (size_t)cand * P.nnz * n_psi + (size_t)(e0 + a0 + dl) * n_psi + psi0 + my_psi;
-      P.out_score[o] = best * 1024.0f;
-      P.out_y[o] = bi / C;
-      P.out_x[o] = bi % C;
+#pragma unroll
+      for (int y = RR; y < C; ++y) {
+        float a[C];
+        tmem_ld_row<C>(a, ta_acc + (uint32_t)((y - RR) * C));
+#pragma unroll
+        for (int x = 0; x < C; ++x) {
+          const float v = raw_at<C>(a, x);
+          if (v > best) {
+            best = v;
+            bi = y * C + x;
+          }
+        }
+      }
+      const TcItem it = tc_item(P, wi, n, H);
+      const int dl = my_row / nc8, cand = my_row - dl * nc8;
+      if (active && dl < it.nd && cand < n_cand) {
+        const size_t o = (size_t)cand * P.nnz * P.n_psi + (size_t)(it.e0 + it.a0 + dl) * P.n_psi + it.psi0 + my_psi;
+        P.out_score[o] = best * 1024.0f;
+        P.out_y[o] = bi / C;
+        P.out_x[o] = bi % C;
+      }
     }
-    __syncthreads();  // column twiddles, slots and TMEM buffers are reused by the next item
   }
-  if (!ok) {
-    if (tid == 0 && P.status != nullptr) atomicExch(P.status, 1);
-    // give MMAs still in flight a last bounded chance to retire before TMEM is freed
-    for (int s = 0; s < 2; ++s)
-      if (uses[s] > 0) mbar_wait(bar_empty + s, (uses[s] - 1) & 1u);
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;");
+  // every role has left its loop; on a failure, MMAs still in flight get a
+  // last bounded chance to retire before TMEM is freed
   __syncthreads();
+  if (*reinterpret_cast<volatile int*>(s_fail) != 0) {
+    if (tid == 0) {
+      if (P.status != nullptr) atomicExch(P.status, 1);
+      for (int s = 0; s < S; ++s) mbar_wait(bar_empty + s, 0), mbar_wait(bar_empty + s, 1);
+    }
+    __syncthreads();
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;");
   if (warp == 0) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(kTcTmemCols));
   }
 }
 
 // fp16 hi/lo copy of template banks for the tensor-core kernel:
-// out[slot][col][half][part][k/8][cand][k%8] with, per half hh, k < n/2 the
-// real part and k >= n/2 the imaginary part of rows r = hh n/2 + (k mod n/2),
-// scaled by 2^13. One block per (slot, candidate), transposed through shared
-// memory; every thread writes whole 16-byte chunks.
+// out[slot][col][step][part][cand][128 B]; step q covers rows r in
+// [32q, 32q + 32): logical 16-byte chunk c < 4 holds Re T of rows 32q + 8c..,
+// chunk 4 + c holds Im T of the same rows, scaled by 2^13; chunk c is stored
+// at position c ^ (cand & 7) (the 128-byte swizzle of the shared-memory tile,
+// whose direction blocks start on multiples of 8 rows). One block per
+// (slot, candidate); every candidate writes whole 128-byte rows.
 __global__ void bank_to_fp16(const float2* __restrict__ bank, long long bank_stride, int n, int n_cand,
                              __half* __restrict__ out) {
   extern __shared__ float2 s_t[];  // [n][H]
-  const int H = n / 2 + 1, kc_n = n / 8;
+  const int H = n / 2 + 1, nq = n / 32;
   const int slot = blockIdx.x, cand = blockIdx.y;
   const float2* src = bank + (size_t)cand * (size_t)bank_stride + (size_t)slot * n * H;
   for (int t = threadIdx.x; t < n * H; t += blockDim.x) s_t[t] = src[t];
   __syncthreads();
-  // one task per (col, half, K chunk): 8 consecutive k -> hi and lo chunks
-  for (int t = threadIdx.x; t < H * 2 * kc_n; t += blockDim.x) {
-    const int kc = t % kc_n, hh = (t / kc_n) % 2, col = t / (2 * kc_n);
-    const bool imag = kc >= kc_n / 2;
-    const int r0 = hh * (n / 2) + (kc % (kc_n / 2)) * 8;
+  // one task per (col, step, chunk): 8 consecutive k -> hi and lo 16-byte chunks
+  for (int t = threadIdx.x; t < H * nq * 8; t += blockDim.x) {
+    const int c = t & 7, qq = (t >> 3) % nq, col = t / (8 * nq);
+    const bool imag = c >= 4;
+    const int r0 = qq * 32 + (c & 3) * 8;
     float v[8];
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
@@ -466,22 +701,34 @@ __global__ void bank_to_fp16(const float2* __restrict__ bank, long long bank_str
     }
     uint4 hi, lo;
     split8(v, hi, lo);
-    const size_t base = ((((size_t)slot * H + col) * 2 + hh) * 2) * kc_n;  // part 0 chunk index
-    *reinterpret_cast<uint4*>(out + ((base + kc) * n_cand + cand) * 8) = hi;
-    *reinterpret_cast<uint4*>(out + ((base + kc_n + kc) * n_cand + cand) * 8) = lo;
+    const size_t row = (((size_t)slot * H + col) * nq + qq) * 2;  // part 0 row block
+    const int pos = c ^ (cand & 7);
+    *reinterpret_cast<uint4*>(out + ((row * n_cand + cand) * 8 + pos) * 8) = hi;
+    *reinterpret_cast<uint4*>(out + (((row + 1) * n_cand + cand) * 8 + pos) * 8) = lo;
   }
+}
+
+template <int C, int N>
+cudaError_t launch_tc_cn(const TcParams& P, size_t smem, int grid, cudaStream_t st) {
+  static size_t set_smem = 0;
+  if (set_smem < smem) {
+    cudaError_t e =
+        cudaFuncSetAttribute(correlate_tc<C, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    set_smem = smem;
+  }
+  correlate_tc<C, N><<<grid, kTcThreads, smem, st>>>(P);
+  return cudaGetLastError();
 }
 
 template <int C>
 cudaError_t launch_tc_c(const TcParams& P, size_t smem, int grid, cudaStream_t st) {
-  static size_t set_smem = 0;
-  if (set_smem < smem) {
-    cudaError_t e = cudaFuncSetAttribute(correlate_tc<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    set_smem = smem;
+  switch (P.n) {
+    case 32: return launch_tc_cn<C, 32>(P, smem, grid, st);
+    case 64: return launch_tc_cn<C, 64>(P, smem, grid, st);
+    case 128: return launch_tc_cn<C, 128>(P, smem, grid, st);
+    default: return cudaErrorInvalidValue;
   }
-  correlate_tc<C><<<grid, kTcThreads, smem, st>>>(P);
-  return cudaGetLastError();
 }
 
 }  // namespace
@@ -491,10 +738,9 @@ int correlate_tc_max_n() { return kTcMaxN; }
 int correlate_tc_max_cand() { return kTcMaxCand; }
 
 size_t correlate_tc_smem_bytes(int n, int crop) {
-  const size_t kc_n = (size_t)n / 8;
-  const size_t stage = 2 * kc_n * kTcM * 16 + 2 * kc_n * ((size_t)tc_n(crop) * 16 + 16);
-  return 2 * stage + (size_t)kTcPsi * n * sizeof(float2) + (size_t)n * sizeof(float2) + 32 * sizeof(float4) +
-         6 * 8 + 8 + (size_t)kTcM * sizeof(int);
+  const size_t stage = 2 * (size_t)kTcM * 128 + 2 * (size_t)tc_n(crop) * 128;
+  return kTcStages * stage + 3 * (size_t)kTcPsi * n * sizeof(float2) + (size_t)n * sizeof(float2) +
+         (size_t)(n / 2 + 1) * tc_tw_entries(crop) * sizeof(float) + (3 * kTcStages + 4) * 8 + 8;
 }
 
 // halves in the fp16 hi/lo bank copy of one candidate
@@ -502,8 +748,11 @@ long long correlate_tc_bank_halves(int n_slot, int n) {
   return (long long)n_slot * (n / 2 + 1) * 2 * (2LL * n);
 }
 
-// directions per tile for a launch of n_cand candidates
-int correlate_tc_dirs_per_tile(int n_cand) { return n_cand > 0 ? kTcM / std::min(n_cand, kTcMaxCand) : 0; }
+// directions per tile for a launch of n_cand candidates (rows per direction
+// rounded up to 8, the swizzle atom)
+int correlate_tc_dirs_per_tile(int n_cand) {
+  return n_cand > 0 ? kTcM / ((std::min(n_cand, kTcMaxCand) + 7) & ~7) : 0;
+}
 
 // Work list (particle, tile * n_groups + psi group) for the tensor-core
 // kernel, sorted by the slot of the tile's first direction (then particle),

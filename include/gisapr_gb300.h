@@ -190,8 +190,8 @@ int gisapr_correlate_batch(gisapr_ctx ctx, void* stream, const float* bank, long
  *   status: device int, set to 1 if an on-chip barrier wait ran out (the
  *     outputs are then incomplete); the caller zeroes it.
  * Sizes: n in {32, 64, 128}, crop even in 2..12, n_cand <= 128 per call (the
- * work list is planned for that n_cand: a tile holds 128 / n_cand whole
- * directions).
+ * work list is planned for that n_cand: a tile holds 128 / ceil8(n_cand)
+ * whole directions).
  */
 long long gisapr_tc_bank_bytes(int n_slot, int n);
 int gisapr_tc_plan_work(const int* local_ptr, const int* local_idx, int n_particles, int n_cand, int n_psi,

@@ -67,7 +67,7 @@ def test_tensor_core_work_plan_on_host(native_lib):
     vp = lambda a: C.c_void_p(a.ctypes.data)
     for n_cand, n_psi in ((1, 1), (5, 3), (64, 3), (128, 5), (48, 7), (100, 2)):
         groups = -(-n_psi // 3)
-        dpt = 128 // n_cand
+        dpt = 128 // (-(-n_cand // 8) * 8)  # rows per direction rounded up to 8
         n = C.c_int(-1)
         assert lib.gisapr_tc_plan_work(vp(ptr), vp(idx), 40, n_cand, n_psi, None, 0, C.byref(n)) == 0
         want = sum(-(-int(c) // dpt) for c in counts) * groups

@@ -51,6 +51,8 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=48, help="particles and templates in the CPU sample")
     ap.add_argument("--batch", type=int, default=64, help="candidates per batched generation (0: skip)")
+    ap.add_argument("--serve-requests", type=int, default=40,
+                    help="requests in the serving stream (0: skip the serving measurement)")
     ap.add_argument("--precisions", default="fp32,fp16x3",
                     help="batched correlation forms to time: fp32 (plain), fp16x3 (tensor-core split), fp16")
     return ap.parse_args()
@@ -265,6 +267,109 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+SERVE_JOBS = (("box64_small", 2000), ("box128_5kp", 1000), ("box128_5kp", 2500))  # (workload, particles)
+
+
+def run_serving(args, device):
+    """A seeded Poisson stream of candidate-evaluation requests from four
+    driver threads over three resident jobs, through the continuous-batching
+    server (fp16 hi/lo tensor-core correlation), and the same stream
+    evaluated serially through the plain FP32 per-candidate path. Latency is
+    arrival to scores on the host."""
+    import threading
+    import numpy as np
+    import torch
+    from gisapr_gb300 import synthetic as syn
+    from gisapr_gb300.engine import JobConfig, ScoringJob
+    from gisapr_gb300.serving import ScoringServer, job_footprint_bytes
+    from gisapr_gb300.tables import model_angles_from_lists
+
+    rng = np.random.default_rng(args.seed + 4242)
+    jobs = {}
+    for k, (name, npart) in enumerate(SERVE_JOBS):
+        spec = syn.WORKLOADS[name]
+        data = syn.make_job(spec, seed=args.seed + 50 + k, device=str(device), n_particles=npart)
+        cfg = JobConfig(box=spec.box, apix=spec.apix, crop=spec.crop, psi_step=spec.psi_step,
+                        local_range=spec.local_range, mask_edge=spec.mask_edge, kk=spec.kk)
+        jobs[f"job{k}"] = (cfg, data, spec)
+
+    def factory(jid):
+        cfg, data, _ = jobs[jid]
+        return lambda: ScoringJob(cfg, data.model.pdb_text, model_angles_from_lists(data.model_rot, data.model_tilt),
+                                  job_records(data), data.images, fsc_values=data.fsc, device=device)
+
+    n_req = args.serve_requests
+    jids = sorted(jobs)
+    req_job = [jids[int(i)] for i in rng.integers(0, len(jids), size=n_req)]
+    req_n = [int(x) for x in rng.integers(1, 17, size=n_req)]
+    req_poses = [syn.candidate_poses(k, args.seed + 9000 + i, 5.0, 3.0) for i, k in enumerate(req_n)]
+    gaps = rng.exponential(0.010, size=n_req)  # mean 10 ms between arrivals
+    arrive = np.cumsum(gaps)
+    max_batch = 32
+    with ScoringServer(device, hbm_cap_bytes=150e9, max_batch=max_batch, n_workers=3, precision="fp16x3") as srv:
+        for jid in jids:
+            cfg, data, spec = jobs[jid]
+            fp = job_footprint_bytes(cfg.box, cfg.new_box, len(data.records.rot), 3,
+                                     len(data.model_rot), max_batch, "fp16x3")
+            srv.register(jid, factory(jid), fp)
+        # warm-up: build every job and its batch buffers, compile plans
+        for jid in jids:
+            srv.submit(jid, req_poses[0][:1]).result()
+        srv.reset_stats()
+        torch.cuda.synchronize(device)
+        t0 = time.perf_counter()
+        futs = [None] * n_req
+
+        def driver(d):
+            for i in range(d, n_req, 4):
+                wait = t0 + arrive[i] - time.perf_counter()
+                if wait > 0:
+                    time.sleep(wait)
+                futs[i] = srv.submit(req_job[i], req_poses[i])
+
+        ts = [threading.Thread(target=driver, args=(d,)) for d in range(4)]
+        for t in ts:
+            t.start()
+        for t in ts:
+            t.join()
+        srv.drain()
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        served = [f.result() for f in futs]
+    # serial plain FP32, one candidate at a time, requests in arrival order
+    sjobs = {jid: factory(jid)() for jid in jids}
+    for jid in jids:
+        sjobs[jid].score(req_poses[0][0])
+    torch.cuda.synchronize(device)
+    lat = []
+    t_free = 0.0
+    serial_scores = []
+    t_busy = 0.0
+    for i in range(n_req):
+        t1 = time.perf_counter()
+        serial_scores.append(np.asarray([sjobs[req_job[i]].score(p) for p in req_poses[i]]))
+        dt = time.perf_counter() - t1
+        t_busy += dt
+        start = max(arrive[i], t_free)
+        t_free = start + dt
+        lat.append(t_free - arrive[i])
+    rel = max(float(np.max(np.abs(a / b - 1.0))) for a, b in zip(served, serial_scores))
+    lat_ms = np.asarray(lat) * 1e3
+    total = int(sum(req_n))
+    return {
+        "requests": n_req, "candidates": total, "jobs": [f"{n}: {p} particles" for n, p in SERVE_JOBS],
+        "drivers": 4, "workers": 3, "max_batch": max_batch, "precision": "fp16x3",
+        "arrivals": "Poisson, mean gap 10 ms, 1-16 candidates per request",
+        "value": total / wall, "unit": UNIT, "wall_s": wall,
+        "latency_ms": {"p50": st.latency_ms_p50, "p99": st.latency_ms_p99},
+        "batches": st.batches, "mean_batch": st.mean_batch,
+        "serial_plain_fp32": {"value": total / t_busy, "unit": UNIT,
+                              "latency_ms": {"p50": float(np.percentile(lat_ms, 50)),
+                                             "p99": float(np.percentile(lat_ms, 99))}},
+        "max_score_rel_diff_vs_serial_fp32": rel,
+    }
+
+
 def run_gb300(args, rank: int, world: int, local_rank: int):
     import numpy as np
     import torch
@@ -404,6 +509,8 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
     }
     if batched:
         line["batched"] = batched
+    if world == 1 and args.serve_requests > 0:
+        line["serving"] = run_serving(args, device)
     if world == 1 and not args.no_cpu_baseline:
         cb = cpu_baseline(spec, data, poses[W], args.cpu_sample)
         line["cpu_baseline"] = {

@@ -452,8 +452,14 @@ cudaError_t launch_project_templates(cudaStream_t st, const float2* spectrum, co
 // ===========================================================================
 namespace {
 
-constexpr int kSmemThreads = 256;
+constexpr int kSmemThreads = 384;
 constexpr int kSmemWarps = kSmemThreads / 32;
+
+// Columns a warp gathers per pass-A round (both row parities of each column
+// form one FFT line); at N = 128 one column, so that sixteen warps' staging
+// lines fit next to the plane.
+template <int N>
+__host__ __device__ constexpr int pass_a_cols() { return N == 128 ? 1 : 16 / (N / 16); }
 
 // Row stride (complex elements) of the padded shared-memory plane: holds the
 // N + 1 columns plus one spare slot per 8, chosen by a bank-conflict search.
@@ -588,8 +594,8 @@ __device__ void build_one_smem(const ProjParams& P, int dir, int slot, float2* Z
   // in the warp's staging area, one warp FFT transforms them, and the
   // even/odd pair combines into the N centred rows of the 2N-point inverse.
   {
-    constexpr int CPR = 16 / L2;
-    const StageLines<N> S{stage_all + warp * (G * plane_ld(N))};
+    constexpr int CPR = pass_a_cols<N>();
+    const StageLines<N> S{stage_all + warp * (2 * CPR * plane_ld(N))};
     for (int c0 = warp * CPR; c0 < W; c0 += kSmemWarps * CPR) {
 #pragma unroll 2
       for (int idx = lane; idx < CPR * m; idx += 32) {
@@ -614,7 +620,7 @@ __device__ void build_one_smem(const ProjParams& P, int dir, int slot, float2* Z
         S.at(cl * 2 + (r & 1), r >> 1) = v;
       }
       __syncwarp();
-      warp_fft<N, 1>(S, G, tw);
+      warp_fft<N, 1>(S, 2 * CPR, tw);
       for (int idx = lane; idx < CPR * N; idx += 32) {
         const int cl = idx / N, k = idx % N;
         const int c = c0 + cl;
@@ -823,7 +829,7 @@ __global__ void __launch_bounds__(kSmemThreads, 1) project_templates_smem(ProjPa
   constexpr int L2 = N / 16;
   float2* Zs = reinterpret_cast<float2*>(smem_raw);
   float2* stage = Zs + plane_rows(N) * plane_ld(N);
-  float2* s_tw = stage + kSmemWarps * (32 / L2) * plane_ld(N);
+  float2* s_tw = stage + kSmemWarps * (2 * pass_a_cols<N>()) * plane_ld(N);
   double* red = reinterpret_cast<double*>(s_tw + kMaxFftLen / 2);
   double* s_coef = red + 32;
   float* s_div = reinterpret_cast<float*>(s_coef + 8);
@@ -840,7 +846,8 @@ __global__ void __launch_bounds__(kSmemThreads, 1) project_templates_smem(ProjPa
 
 size_t project_smem_bytes_fast(int N, int n_bins) {
   const int L2 = N / 16;
-  return (size_t)plane_rows(N) * plane_ld(N) * sizeof(float2) + (size_t)kSmemWarps * (32 / L2) * plane_ld(N) * sizeof(float2) +
+  const int cpr = N == 128 ? 1 : 16 / L2;
+  return (size_t)plane_rows(N) * plane_ld(N) * sizeof(float2) + (size_t)kSmemWarps * (2 * cpr) * plane_ld(N) * sizeof(float2) +
          (kMaxFftLen / 2) * sizeof(float2) + 40 * sizeof(double) + (size_t)(n_bins + 4) * sizeof(float);
 }
 

@@ -309,17 +309,32 @@ class BatchScoringJob:
         ptr = np.ascontiguousarray(job.local_ptr.cpu().numpy(), dtype=np.int32)
         idx = np.ascontiguousarray(job.local_idx.cpu().numpy(), dtype=np.int32)
         np_ = len(job.records)
+        self._host_map = (ptr, idx)
         self.tc_plans = {}
         for _, cc in self.tc_chunks:
-            if cc in self.tc_plans:
-                continue
+            self._tc_plan(cc)
+        self.tc_status = torch.zeros(1, dtype=torch.int32, device=job.device)
+
+    def _tc_plan(self, cc: int):
+        """Work list of the tensor-core kernel for chunks of cc candidates (cached)."""
+        if cc not in self.tc_plans:
+            job = self.job
+            ptr, idx = self._host_map
+            np_ = len(job.records)
             count = C.c_int(0)
             nat.call("gisapr_tc_plan_work", idx_ptr(ptr), idx_ptr(idx), np_, cc, job.n_psi, None, 0, C.byref(count))
             work = np.zeros((max(1, count.value), 2), dtype=np.int32)
             nat.call("gisapr_tc_plan_work", idx_ptr(ptr), idx_ptr(idx), np_, cc, job.n_psi, idx_ptr(work),
                      work.shape[0], C.byref(count))
             self.tc_plans[cc] = (torch.from_numpy(work).to(job.device), count.value)
-        self.tc_status = torch.zeros(1, dtype=torch.int32, device=job.device)
+        return self.tc_plans[cc]
+
+    def _chunks(self, n_active: int):
+        if n_active == self.n_cand:
+            return self.tc_chunks
+        n_chunks = -(-n_active // self.TC_MAX_CAND)
+        size = -(-n_active // n_chunks)
+        return [(c0, min(size, n_active - c0)) for c0 in range(0, n_active, size)]
 
     def check_status(self) -> None:
         """Raise if an on-chip barrier wait of the tensor-core kernel ran out."""
@@ -334,12 +349,16 @@ class BatchScoringJob:
         extra = 2 * len(self.tc_chunks) - 1 if self.precision != "fp32" else 0
         return self.n_cand * self.KERNELS_PER_CANDIDATE + self.KERNELS_PER_BATCH + extra
 
-    def enqueue(self, marks: Optional[list] = None) -> None:
+    def enqueue(self, marks: Optional[list] = None, n_active: Optional[int] = None) -> None:
         """Enqueue the whole batch on the current stream (poses already on the device).
 
         ``marks``: when a list is given (eager runs only), a CUDA event is
-        recorded after each stage and appended as (stage, event)."""
+        recorded after each stage and appended as (stage, event).
+        ``n_active``: score only the first n_active slots (eager runs only)."""
         job = self.job
+        n_act = self.n_cand if n_active is None else int(n_active)
+        if not 0 < n_act <= self.n_cand:
+            raise ValueError(f"n_active must be in 1..{self.n_cand}, got {n_active}")
         dev = job.device
         ctx = nat.Context.for_device(dev).handle
         st = nat.stream_of(dev)
@@ -351,7 +370,7 @@ class BatchScoringJob:
                 marks.append((name, ev))
 
         mark("start")
-        for c in range(self.n_cand):
+        for c in range(n_act):
             self.models[self.model_of[c]].generate(None, write_padded=True, pose_device=self.poses_dev[c])
             job.projector.volume_spectrum(None)
             if job.needed:
@@ -359,14 +378,14 @@ class BatchScoringJob:
         mark("templates")
         np_ = len(job.records)
         if self.precision == "fp32":
-            nat.call("gisapr_correlate_batch", ctx, st, nat.ptr(self.banks), self.bank_stride, self.n_cand,
+            nat.call("gisapr_correlate_batch", ctx, st, nat.ptr(self.banks), self.bank_stride, n_act,
                      nat.ptr(job.stack), nat.ptr(job.local_ptr), nat.ptr(job.local_idx), np_, job.nnz, job.n_psi,
                      job.cfg.new_box, job.cfg.crop, nat.ptr(self.score_buf), nat.ptr(self.y_buf),
                      nat.ptr(self.x_buf))
         else:
             m = max(1, job.nnz) * job.n_psi
-            for c0, cc in self.tc_chunks:
-                work, n_work = self.tc_plans[cc]
+            for c0, cc in self._chunks(n_act):
+                work, n_work = self._tc_plan(cc)
                 nat.call("gisapr_correlate_tc_batch", ctx, st, nat.c_ptr_offset(self.banks, c0 * self.bank_stride * 8),
                          self.bank_stride, cc, self.n_slot, nat.ptr(self.tbank), nat.ptr(job.stack),
                          nat.ptr(job.local_ptr), nat.ptr(job.local_idx), nat.ptr(work), n_work, job.nnz, job.n_psi,
@@ -375,10 +394,10 @@ class BatchScoringJob:
                          nat.c_ptr_offset(self.x_buf, c0 * m * 4), nat.ptr(self.tc_status))
         mark("correlate")
         nat.call("gisapr_particle_results_batch", st, nat.ptr(job.local_ptr), nat.ptr(self.score_buf),
-                 nat.ptr(self.y_buf), nat.ptr(self.x_buf), np_, job.n_psi, self.n_cand, nat.ptr(self.best_entry),
+                 nat.ptr(self.y_buf), nat.ptr(self.x_buf), np_, job.n_psi, n_act, nat.ptr(self.best_entry),
                  nat.ptr(self.best_psi), nat.ptr(self.peak), nat.ptr(self.peak_y), nat.ptr(self.peak_x),
                  nat.ptr(self.zscore))
-        nat.call("gisapr_score_sum_batch", st, nat.ptr(job.local_ptr), nat.ptr(self.peak), np_, self.n_cand,
+        nat.call("gisapr_score_sum_batch", st, nat.ptr(job.local_ptr), nat.ptr(self.peak), np_, n_act,
                  nat.ptr(self.totals))
         mark("records")
 
@@ -416,6 +435,24 @@ class BatchScoringJob:
         for c, p in enumerate(poses):
             self.poses_host[c].copy_(self.models[self.model_of[c]].pose_tensor(p))
         self.poses_dev.copy_(self.poses_host, non_blocking=True)
+
+    def score_active(self, poses, stream=None) -> np.ndarray:
+        """Scores of up to n_cand poses in one eager launch sequence on
+        ``stream`` (default: the batch stream); slots past len(poses) are not
+        computed. Blocks until the scores are on the host."""
+        k = len(poses)
+        if not 0 < k <= self.n_cand:
+            raise ValueError(f"expected 1..{self.n_cand} poses, got {k}")
+        st = stream if stream is not None else self.stream
+        for c, p in enumerate(poses):
+            self.poses_host[c].copy_(self.models[self.model_of[c]].pose_tensor(p))
+        with torch.cuda.stream(st):
+            self.poses_dev[:k].copy_(self.poses_host[:k], non_blocking=True)
+            self.enqueue(n_active=k)
+            self.totals_host[:k].copy_(self.totals[:k], non_blocking=True)
+        st.synchronize()
+        self.check_status()
+        return self.totals_host[:k].numpy().copy()
 
     def score_batch(self, poses) -> np.ndarray:
         """Scores of len(poses) == n_cand poses, in slot order."""

@@ -1,0 +1,115 @@
+"""Scheduling and admission of the request loop, with a fake executor (CPU)."""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+from gisapr_gb300.serving import ScoringServer, job_footprint_bytes
+
+
+class FakeServer(ScoringServer):
+    """Scores are a pure function of (job, pose); each batch takes a few ms."""
+
+    def __init__(self, *a, delay=0.003, **k):
+        self.delay = delay
+        self.ran = []  # (job_id, n) per batch
+        self.built = []
+        self.lock2 = threading.Lock()
+        super().__init__(*a, device="cpu", **k)
+
+    def _make_stream(self):
+        return None
+
+    def _run(self, j, poses, stream):
+        if j.job is None:
+            j.job = j.factory()
+            with self.lock2:
+                self.built.append(j.job_id)
+        time.sleep(self.delay)
+        with self.lock2:
+            self.ran.append((j.job_id, len(poses)))
+        return poses.sum(axis=1) * j.job
+
+
+def poses_of(seed, n):
+    return np.random.default_rng(seed).normal(size=(n, 6))
+
+
+def test_results_follow_requests_and_batches_merge():
+    with FakeServer(max_batch=16, n_workers=1, delay=0.02) as srv:
+        srv.register("a", lambda: 2.0, 10)
+        srv.register("b", lambda: 3.0, 10)
+        reqs = [(("a", "b")[i % 2], poses_of(i, 1 + i % 5)) for i in range(24)]
+        futs = [srv.submit(j, p) for j, p in reqs]
+        srv.drain(timeout=30)
+        for (j, p), f in zip(reqs, futs):
+            np.testing.assert_array_equal(f.result(), p.sum(axis=1) * (2.0 if j == "a" else 3.0))
+        st = srv.stats()
+        assert st.requests == 24 and st.candidates == sum(len(p) for _, p in reqs)
+        assert st.batches < 24  # requests queued behind a running batch share the next one
+        assert all(n <= 16 for _, n in srv.ran)
+        assert st.latency_ms_p99 >= st.latency_ms_p50 > 0
+
+
+def test_large_request_is_split_and_joined():
+    with FakeServer(max_batch=8, n_workers=2) as srv:
+        srv.register("a", lambda: 1.5, 10)
+        p = poses_of(3, 21)
+        f = srv.submit("a", p)
+        np.testing.assert_array_equal(f.result(timeout=30), p.sum(axis=1) * 1.5)
+        assert sorted(n for _, n in srv.ran) == [5, 8, 8]
+
+
+def test_admission_by_footprint_waits_for_retired_jobs():
+    with FakeServer(hbm_cap_bytes=100, max_batch=8, n_workers=2) as srv:
+        srv.register("a", lambda: 1.0, 60)
+        srv.register("b", lambda: 2.0, 60)  # does not fit next to a
+        srv.register("c", lambda: 3.0, 30)  # fits, but admission keeps registration order
+        assert srv.is_admitted("a") and not srv.is_admitted("b") and not srv.is_admitted("c")
+        assert srv.memory_in_use() == 60
+        fa = srv.submit("a", poses_of(1, 3))
+        fb = srv.submit("b", poses_of(2, 3))
+        fa.result(timeout=30)
+        time.sleep(0.05)
+        assert not fb.done()  # b is queued until a retires
+        srv.retire("a")
+        np.testing.assert_array_equal(fb.result(timeout=30), poses_of(2, 3).sum(axis=1) * 2.0)
+        assert srv.is_admitted("b") and srv.is_admitted("c")
+        assert srv.memory_in_use() == 90
+        assert srv.built == ["a", "b"]
+
+
+def test_concurrent_drivers_and_errors():
+    with FakeServer(max_batch=32, n_workers=3, delay=0.001) as srv:
+        for k in range(4):
+            srv.register(f"j{k}", (lambda k=k: float(k + 1)), 1)
+        out = {}
+
+        def driver(d):
+            for i in range(15):
+                jid = f"j{(d + i) % 4}"
+                p = poses_of(100 * d + i, 1 + (i % 7))
+                out[(d, i)] = (jid, p, srv.submit(jid, p))
+
+        threads = [threading.Thread(target=driver, args=(d,)) for d in range(5)]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+        srv.drain(timeout=30)
+        for jid, p, f in out.values():
+            np.testing.assert_array_equal(f.result(), p.sum(axis=1) * float(int(jid[1:]) + 1))
+        with pytest.raises(ValueError):
+            srv.submit("missing", poses_of(0, 1))
+        with pytest.raises(ValueError):
+            srv.submit("j0", np.zeros((0, 6)))
+        with pytest.raises(ValueError):
+            srv.register("huge", lambda: 1.0, 10 ** 15)
+
+
+def test_footprint_estimate_counts_spectra_and_banks():
+    base = job_footprint_bytes(128, 128, 5000, 3, 768, 64)
+    assert base > 5000 * 3 * 128 * 65 * 8 + 64 * 768 * 128 * 65 * 8
+    assert job_footprint_bytes(128, 128, 5000, 3, 768, 64, precision="fp16x3") > base
+    assert job_footprint_bytes(128, 128, 10000, 3, 768, 64) > base

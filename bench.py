@@ -138,14 +138,15 @@ def job_records(job):
                            float(r.defocus_angle[i])) for i in range(len(r.rot))]
 
 
-def run_batched(job, dens, gen, precision, n_batch, K, W, device, barrier):
+def run_batched(job, dens, gen, precision, n_batch, K, W, device, barrier, tc_chunk=128):
     """Time K graph-replayed generations of n_batch candidates (device events on
     the batch stream), then K end-to-end generations (poses from the host,
     scores and per-particle peaks back)."""
     import torch
     from gisapr_gb300.engine import BatchScoringJob
     model_of = [i % len(dens) for i in range(n_batch)]
-    bj = BatchScoringJob(job, n_batch, models=dens, model_of=model_of, precision=precision)
+    bj = BatchScoringJob(job, n_batch, models=dens, model_of=model_of, precision=precision,
+                         tc_chunk=min(tc_chunk, 128))
     for k in range(W):
         bj.score_batch(gen[k])
     barrier()
@@ -448,8 +449,17 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
         dens = [MovedChainDensity(m.pdb_text, "A", spec.box, spec.apix, spec.res, device, from_text=True)
                 for m in models]
         gen = [syn.candidate_poses(args.batch, args.seed + 1000 + 31 * k + rank, 5.0, 3.0) for k in range(K + W)]
+        # launch shapes from the autotuner (cluster size of the plain correlation,
+        # candidates per tensor-core launch), timed on this job
+        from gisapr_gb300.autotune import Autotuner
+        t_tune = time.perf_counter()
+        tuned = Autotuner(trials=1).tune(job, n_cand=args.batch, precision="fp16x3")
+        autotune = {"corr_cluster": tuned.corr_cluster, "tc_chunk": tuned.tc_chunk,
+                    "correlate_ms": tuned.times_ms, "tune_s": time.perf_counter() - t_tune}
         for precision in args.precisions.split(","):
-            batched[precision] = run_batched(job, dens, gen, precision, args.batch, K, W, device, barrier)
+            batched[precision] = run_batched(job, dens, gen, precision, args.batch, K, W, device, barrier,
+                                             tc_chunk=tuned.tc_chunk)
+            batched[precision]["autotune"] = autotune
     tl = [elapsed, e2e_elapsed]
     for b in batched.values():
         tl += [b["elapsed_s"], b["e2e_elapsed_s"]]

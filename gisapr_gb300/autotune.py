@@ -1,0 +1,139 @@
+"""Launch-shape autotuner for batched scoring.
+
+Two choices decide the correlation's speed for a given box, crop, psi count
+and particle set, and the best value depends on the GPU:
+
+* the thread-block cluster size of the plain FP32 correlation (CTAs that
+  split one particle's packed columns; each holds its columns of every psi
+  spectrum in shared memory), 1..8;
+* the candidates per tensor-core launch: a 128-row MMA tile holds
+  128 // ceil8(candidates) whole directions, so the chunk size sets how many
+  directions share a tile and how many tiles a particle needs.
+
+``Autotuner.tune`` times the batched correlation stage (CUDA events, best of
+a few runs on the job's own data) for every valid value, keeps the fastest,
+and caches the result per (GPU, size, crop, psi count, particle count
+bucket, batch size) in a JSON file. The reference has no autotuner (its
+launch shapes are fixed in the torch code); these choices change launch
+shapes only, not the algorithm.
+"""
+from __future__ import annotations
+
+import json
+import math
+import os
+from dataclasses import asdict, dataclass, field
+from pathlib import Path
+from typing import Dict, Optional, Sequence
+
+from . import _native as nat
+
+__all__ = ["Autotuner", "TuneResult", "default_cache_path"]
+
+CLUSTER_CHOICES = (1, 2, 3, 4, 5, 6, 8)
+CHUNK_CHOICES = (16, 32, 64, 128)
+SMEM_LIMIT = 227 * 1024
+
+
+def default_cache_path() -> Path:
+    env = os.environ.get("GISAPR_TUNING_CACHE")
+    if env:
+        return Path(env)
+    return Path.home() / ".cache" / "gisapr_gb300" / "tuning.json"
+
+
+def plain_smem_bytes(n: int, n_psi: int, crop: int, cluster: int) -> int:
+    """Shared memory of one CTA of the plain correlation (matches the kernel's carve-up)."""
+    h = n // 2 + 1
+    cw = -(-h // cluster)
+    k_group, k_local = 4, 16
+    return (n_psi * n * cw * 8 + k_group * n_psi * crop * cw * 8 + (n // 16) * crop * 8 + cw * crop * 8
+            + k_local * n_psi * crop * crop * 4)
+
+
+@dataclass
+class TuneResult:
+    key: str
+    corr_cluster: int
+    tc_chunk: int
+    times_ms: Dict[str, float] = field(default_factory=dict)
+
+    def apply(self) -> None:
+        """Make the cluster size the default of every native context."""
+        nat.set_default_tuning(nat.TUNE_CORR_CLUSTER, self.corr_cluster)
+
+
+class Autotuner:
+    def __init__(self, cache_path: Optional[os.PathLike] = None, trials: int = 2):
+        self.cache_path = Path(cache_path) if cache_path else default_cache_path()
+        self.trials = int(trials)
+
+    @staticmethod
+    def key(job, n_cand: int) -> str:
+        import torch
+        name = torch.cuda.get_device_name(job.device).replace("|", "/")
+        bucket = 2 ** int(round(math.log2(max(1, len(job.records)))))
+        return f"{name}|n={job.cfg.new_box}|crop={job.cfg.crop}|psi={job.n_psi}|particles~{bucket}|cand={n_cand}"
+
+    def _load(self) -> dict:
+        try:
+            return json.loads(self.cache_path.read_text())
+        except (OSError, ValueError):
+            return {}
+
+    def _save(self, data: dict) -> None:
+        try:
+            self.cache_path.parent.mkdir(parents=True, exist_ok=True)
+            tmp = self.cache_path.with_suffix(".tmp")
+            tmp.write_text(json.dumps(data, indent=1, sort_keys=True))
+            os.replace(tmp, self.cache_path)
+        except OSError:
+            pass  # a read-only home only loses the cache
+
+    def _time_correlate(self, job, n_cand: int, precision: str, poses, tc_chunk: int = 128) -> float:
+        from .engine import BatchScoringJob
+        bj = BatchScoringJob(job, n_cand, use_graph=False, precision=precision, tc_chunk=tc_chunk)
+        bj.stage_ms(poses)  # warm-up: plans, tables, launch attributes
+        best = min(bj.stage_ms(poses)["correlate"] for _ in range(self.trials))
+        bj.check_status()
+        del bj
+        return best
+
+    def tune(self, job, n_cand: int = 64, precision: str = "fp16x3", force: bool = False,
+             clusters: Sequence[int] = CLUSTER_CHOICES, chunks: Sequence[int] = CHUNK_CHOICES) -> TuneResult:
+        """Pick the cluster size (plain path) and, unless precision is
+        "fp32", the tensor-core chunk size for batches of n_cand candidates."""
+        from . import synthetic as syn
+        key = self.key(job, n_cand) + f"|{precision}"
+        cache = self._load()
+        if not force and key in cache:
+            r = TuneResult(**cache[key])
+            r.apply()
+            return r
+        poses = list(syn.candidate_poses(n_cand, 1234, 5.0, 3.0))
+        nb, crop, n_psi = job.cfg.new_box, job.cfg.crop, job.n_psi
+        times: Dict[str, float] = {}
+        best_k, best_t = 0, math.inf
+        ctx = nat.Context.for_device(job.device)
+        for k in clusters:
+            if plain_smem_bytes(nb, n_psi, crop, k) > SMEM_LIMIT or k > nb // 2 + 1:
+                continue
+            nat.call("gisapr_set_tuning", ctx.handle, nat.TUNE_CORR_CLUSTER, k)
+            t = self._time_correlate(job, n_cand, "fp32", poses)
+            times[f"plain_cluster_{k}"] = t
+            if t < best_t:
+                best_k, best_t = k, t
+        nat.call("gisapr_set_tuning", ctx.handle, nat.TUNE_CORR_CLUSTER, best_k)
+        best_c = min(128, n_cand)
+        if precision != "fp32":
+            best_ct = math.inf
+            for c in sorted({c for c in chunks if c < n_cand} | {min(n_cand, 128)}):
+                t = self._time_correlate(job, n_cand, precision, poses, tc_chunk=c)
+                times[f"tc_chunk_{c}"] = t
+                if t < best_ct:
+                    best_c, best_ct = c, t
+        r = TuneResult(key=key, corr_cluster=best_k, tc_chunk=best_c, times_ms=times)
+        cache[key] = asdict(r)
+        self._save(cache)
+        r.apply()
+        return r

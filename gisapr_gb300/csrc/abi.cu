@@ -47,10 +47,10 @@ cudaError_t launch_prepare_particles(cudaStream_t, const float*, int, int, const
                                      const float*, const float*, float2*, float2*, int,
                                      const float2*, int, int);
 int correlate_cluster_size(int n);
-size_t correlate_smem_bytes(int n, int n_psi, int crop);
+size_t correlate_smem_bytes(int n, int n_psi, int crop, int cluster);
 cudaError_t launch_correlate_plain(cudaStream_t, const float2*, const float2*, const int*,
                                    const int*, int, int, int, int, const float2*, const float2*,
-                                   float*, int*, int*, int, long long, int);
+                                   float*, int*, int*, int, long long, int, int);
 cudaError_t launch_particle_results(cudaStream_t, const int*, const float*, const int*, const int*,
                                     int, int, int*, int*, float*, int*, int*, float*, int);
 cudaError_t launch_score_sum(cudaStream_t, const int*, const float*, int, double*, int);
@@ -119,6 +119,7 @@ struct gisapr_context {
   std::map<std::pair<int, int>, CorrTables> corr;      // (n, crop) -> twiddles
   DeviceBuffer atoms, bin_counts, bin_lists, proj_scratch, prep_scratch;
   int sm_count = 152;
+  int tune_corr_cluster = 0;  // CTAs per particle in the plain correlation (0: default)
 };
 
 namespace {
@@ -484,7 +485,7 @@ int gisapr_correlate_batch(gisapr_ctx ctx, void* stream, const float* bank, long
     return fail(GISAPR_ERR_UNSUPPORTED, "correlation size must be a multiple of 16 in [32, 256]");
   if (crop < 2 || crop > 16 || crop % 2 != 0 || crop > n)
     return fail(GISAPR_ERR_UNSUPPORTED, "crop must be even, 2..16 and <= n");
-  const size_t smem = correlate_smem_bytes(n, n_psi, crop);
+  const size_t smem = correlate_smem_bytes(n, n_psi, crop, ctx->tune_corr_cluster);
   if (smem > 227 * 1024)
     return fail(GISAPR_ERR_UNSUPPORTED, "too many psi angles for the shared-memory particle slice");
   int rc = set_device(ctx);
@@ -495,7 +496,8 @@ int gisapr_correlate_batch(gisapr_ctx ctx, void* stream, const float* bank, long
   if (nnz < 0) return fail(GISAPR_ERR_ARGUMENT, "nnz < 0");
   GISAPR_CHECK_CUDA(launch_correlate_plain((cudaStream_t)stream, (const float2*)bank, (const float2*)stack,
                                            local_ptr, local_idx, n_particles, n_psi, n, crop, t.outer, t.col,
-                                           out_score, out_y, out_x, n_cand, bank_stride, nnz),
+                                           out_score, out_y, out_x, n_cand, bank_stride, nnz,
+                                           ctx->tune_corr_cluster),
                     "correlate");
   return GISAPR_OK;
 }
@@ -512,7 +514,7 @@ int gisapr_correlate(gisapr_ctx ctx, void* stream, const float* bank, const floa
     return fail(GISAPR_ERR_UNSUPPORTED, "correlation size must be a multiple of 16 in [32, 256]");
   if (crop < 2 || crop > 16 || crop % 2 != 0 || crop > n)
     return fail(GISAPR_ERR_UNSUPPORTED, "crop must be even, 2..16 and <= n");
-  const size_t smem = correlate_smem_bytes(n, n_psi, crop);
+  const size_t smem = correlate_smem_bytes(n, n_psi, crop, ctx->tune_corr_cluster);
   if (smem > 227 * 1024)
     return fail(GISAPR_ERR_UNSUPPORTED, "too many psi angles for the shared-memory particle slice");
   int rc = set_device(ctx);
@@ -522,9 +524,32 @@ int gisapr_correlate(gisapr_ctx ctx, void* stream, const float* bank, const floa
   if (rc) return rc;
   GISAPR_CHECK_CUDA(launch_correlate_plain((cudaStream_t)stream, (const float2*)bank, (const float2*)stack,
                                            local_ptr, local_idx, n_particles, n_psi, n, crop, t.outer, t.col,
-                                           out_score, out_y, out_x, 1, 0, 0),
+                                           out_score, out_y, out_x, 1, 0, 0, ctx->tune_corr_cluster),
                     "correlate");
   return GISAPR_OK;
+}
+
+int gisapr_set_tuning(gisapr_ctx ctx, int key, int value) {
+  if (!ctx) return fail(GISAPR_ERR_ARGUMENT, "context is NULL");
+  switch (key) {
+    case GISAPR_TUNE_CORR_CLUSTER:
+      if (value < 0 || value > 8) return fail(GISAPR_ERR_ARGUMENT, "correlation cluster size must be 0..8");
+      ctx->tune_corr_cluster = value;
+      return GISAPR_OK;
+    default:
+      return fail(GISAPR_ERR_ARGUMENT, "unknown tuning key " + std::to_string(key));
+  }
+}
+
+int gisapr_get_tuning(gisapr_ctx ctx, int key, int* value) {
+  if (!ctx || !value) return fail(GISAPR_ERR_ARGUMENT, "context or value is NULL");
+  switch (key) {
+    case GISAPR_TUNE_CORR_CLUSTER:
+      *value = ctx->tune_corr_cluster;
+      return GISAPR_OK;
+    default:
+      return fail(GISAPR_ERR_ARGUMENT, "unknown tuning key " + std::to_string(key));
+  }
 }
 
 long long gisapr_tc_bank_bytes(int n_slot, int n) {

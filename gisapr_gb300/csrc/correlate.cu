@@ -250,8 +250,10 @@ int correlate_cluster_size(int n) {
   return k < 1 ? 1 : (k > 8 ? 8 : k);
 }
 
-size_t correlate_smem_bytes(int n, int n_psi, int crop) {
-  const int H = n / 2 + 1, K = correlate_cluster_size(n), cwmax = (H + K - 1) / K, M = n / 16;
+// cluster: CTAs per particle (0: the default for n)
+size_t correlate_smem_bytes(int n, int n_psi, int crop, int cluster) {
+  const int H = n / 2 + 1, K = cluster > 0 ? cluster : correlate_cluster_size(n), cwmax = (H + K - 1) / K,
+            M = n / 16;
   size_t b = (size_t)n_psi * n * cwmax * sizeof(float2);
   b += (size_t)kGroup * n_psi * crop * cwmax * sizeof(float2);
   b += (size_t)M * crop * sizeof(float2) + (size_t)cwmax * crop * sizeof(float2);
@@ -287,15 +289,15 @@ cudaError_t launch_correlate_plain(cudaStream_t st, const float2* bank, const fl
                                    const int* local_ptr, const int* local_idx, int n_particles,
                                    int n_psi, int n, int crop, const float2* tw_outer,
                                    const float2* tw_col, float* out_score, int* out_y, int* out_x,
-                                   int n_cand, long long bank_stride, int nnz) {
+                                   int n_cand, long long bank_stride, int nnz, int cluster) {
   if (n_particles <= 0 || n_cand <= 0) return cudaSuccess;
   CorrParams P;
   P.n_cand = n_cand; P.bank_stride = bank_stride; P.nnz = nnz;
   P.bank = bank; P.stack = stack; P.local_ptr = local_ptr; P.local_idx = local_idx;
   P.tw_outer = tw_outer; P.tw_col = tw_col; P.out_score = out_score; P.out_y = out_y;
   P.out_x = out_x; P.n_particles = n_particles; P.n_psi = n_psi; P.n = n;
-  P.cluster = correlate_cluster_size(n);
-  const size_t smem = correlate_smem_bytes(n, n_psi, crop);
+  P.cluster = cluster > 0 ? cluster : correlate_cluster_size(n);
+  const size_t smem = correlate_smem_bytes(n, n_psi, crop, P.cluster);
   switch (crop) {
     case 2: return launch_c<2>(P, smem, st);
     case 4: return launch_c<4>(P, smem, st);

@@ -253,10 +253,14 @@ class BatchScoringJob:
     PRECISIONS = ("fp32", "fp16x3", "fp16")
 
     def __init__(self, job: ScoringJob, n_cand: int, models: Optional[Sequence] = None,
-                 model_of: Optional[Sequence[int]] = None, use_graph: bool = True, precision: str = "fp32"):
+                 model_of: Optional[Sequence[int]] = None, use_graph: bool = True, precision: str = "fp32",
+                 tc_chunk: int = 128):
         if precision not in self.PRECISIONS:
             raise ValueError(f"precision must be one of {self.PRECISIONS}, got {precision!r}")
         self.precision = precision
+        if not 1 <= int(tc_chunk) <= self.TC_MAX_CAND:
+            raise ValueError(f"tc_chunk must be in 1..{self.TC_MAX_CAND}")
+        self.tc_chunk = int(tc_chunk)
         self.job = job
         self.n_cand = int(n_cand)
         self.models = list(models) if models else [job.density]
@@ -295,13 +299,14 @@ class BatchScoringJob:
     def _setup_tensor_path(self, n_needed: int) -> None:
         """fp16 hi/lo bank scratch, direction-sorted work lists and status word.
 
-        Batches of more than 128 candidates run as equal chunks, one
-        tensor-core launch each (the tile shape depends on the chunk size)."""
+        Batches of more than ``tc_chunk`` (at most 128) candidates run as
+        equal chunks, one tensor-core launch each (the tile shape depends on
+        the chunk size; the autotuner picks tc_chunk)."""
         job = self.job
         lib = nat.load()
         nb = job.cfg.new_box
         self.n_slot = n_needed
-        n_chunks = -(-self.n_cand // self.TC_MAX_CAND)
+        n_chunks = -(-self.n_cand // self.tc_chunk)
         size = -(-self.n_cand // n_chunks)
         self.tc_chunks = [(c0, min(size, self.n_cand - c0)) for c0 in range(0, self.n_cand, size)]
         per_cand = int(lib.gisapr_tc_bank_bytes(n_needed, nb))
@@ -332,7 +337,7 @@ class BatchScoringJob:
     def _chunks(self, n_active: int):
         if n_active == self.n_cand:
             return self.tc_chunks
-        n_chunks = -(-n_active // self.TC_MAX_CAND)
+        n_chunks = -(-n_active // self.tc_chunk)
         size = -(-n_active // n_chunks)
         return [(c0, min(size, n_active - c0)) for c0 in range(0, n_active, size)]
 

@@ -38,7 +38,7 @@ SIGNATURES = {
     "gisapr_tc_bank_bytes": [_i, _i],
     "gisapr_set_tuning": [_p, _i, _i],
     "gisapr_get_tuning": [_p, _i, _p],
-    "gisapr_tc_plan_work": [_p, _p, _i, _i, _i, _p, _i, _p],
+    "gisapr_tc_plan_work": [_p, _p, _i, _i, _i, _i, _p, _i, _p],
     "gisapr_correlate_tc_batch": [_p, _p, _p, C.c_longlong, _i, _i, _p, _p, _p, _p, _p, _i, _i, _i, _i, _i, _i,
                                   _p, _p, _p, _p],
 }

@@ -58,7 +58,7 @@ int correlate_tc_max_psi();
 int correlate_tc_max_n();
 size_t correlate_tc_smem_bytes(int n, int crop);
 long long correlate_tc_bank_halves(int n_slot, int n);
-int correlate_tc_plan(const int*, const int*, int, int, int, int*, int);
+int correlate_tc_plan(const int*, const int*, int, int, int, int, int*, int);
 cudaError_t launch_bank_to_fp16(cudaStream_t, const float2*, long long, int, int, int, void*);
 int correlate_tc_max_cand();
 cudaError_t launch_correlate_tc(cudaStream_t, const void*, int, const float2*, const int*, const int*, const int*,
@@ -558,7 +558,7 @@ long long gisapr_tc_bank_bytes(int n_slot, int n) {
 }
 
 int gisapr_tc_plan_work(const int* local_ptr, const int* local_idx, int n_particles, int n_cand, int n_psi,
-                        int* work, int max_work, int* n_work) {
+                        int crop, int* work, int max_work, int* n_work) {
   if (!n_work) return fail(GISAPR_ERR_ARGUMENT, "n_work is NULL");
   *n_work = 0;
   if (n_particles < 0 || n_cand <= 0 || n_psi <= 0)
@@ -569,10 +569,12 @@ int gisapr_tc_plan_work(const int* local_ptr, const int* local_idx, int n_partic
   if (!local_ptr || !local_idx) return fail(GISAPR_ERR_ARGUMENT, "a required pointer is NULL");
   for (int b = 0; b < n_particles; ++b)
     if (local_ptr[b + 1] < local_ptr[b]) return fail(GISAPR_ERR_ARGUMENT, "local_ptr must be non-decreasing");
-  const int count = correlate_tc_plan(local_ptr, local_idx, n_particles, n_cand, n_psi, nullptr, 0);
+  if (crop < 2 || crop > 14 || crop % 2 != 0)
+    return fail(GISAPR_ERR_UNSUPPORTED, "tensor-core correlation takes an even crop in 2..14");
+  const int count = correlate_tc_plan(local_ptr, local_idx, n_particles, n_cand, n_psi, crop, nullptr, 0);
   if (work != nullptr) {
     if (max_work < count) return fail(GISAPR_ERR_ARGUMENT, "work holds fewer than the planned items");
-    correlate_tc_plan(local_ptr, local_idx, n_particles, n_cand, n_psi, work, max_work);
+    correlate_tc_plan(local_ptr, local_idx, n_particles, n_cand, n_psi, crop, work, max_work);
   }
   *n_work = count;
   return GISAPR_OK;
@@ -591,10 +593,10 @@ int gisapr_correlate_tc_batch(gisapr_ctx ctx, void* stream, const float* bank, l
   if (n_slot == 0) return fail(GISAPR_ERR_ARGUMENT, "n_slot must be positive when there is work");
   if (n_cand > 1 && bank_stride < (long long)n_slot * n * (n / 2 + 1))
     return fail(GISAPR_ERR_ARGUMENT, "bank_stride is smaller than one candidate's bank");
-  if (n != 32 && n != 64 && n != 128)
-    return fail(GISAPR_ERR_UNSUPPORTED, "tensor-core correlation takes n in {32, 64, 128}");
-  if (crop < 2 || crop > 12 || crop % 2 != 0 || crop > n)
-    return fail(GISAPR_ERR_UNSUPPORTED, "tensor-core correlation takes an even crop in 2..12");
+  if (n != 32 && n != 64 && n != 128 && n != 256)
+    return fail(GISAPR_ERR_UNSUPPORTED, "tensor-core correlation takes n in {32, 64, 128, 256}");
+  if (crop < 2 || crop > 14 || crop % 2 != 0 || crop > n || (n == 256 && crop < 10))
+    return fail(GISAPR_ERR_UNSUPPORTED, "tensor-core correlation takes an even crop in 2..14 (10..14 at n = 256)");
   if (n_slot > 65535) return fail(GISAPR_ERR_ARGUMENT, "at most 65535 template slots");
   if (n_cand > correlate_tc_max_cand())
     return fail(GISAPR_ERR_ARGUMENT, "at most 128 candidates per tensor-core call");

@@ -45,9 +45,15 @@ namespace {
 
 constexpr int kTcThreads = 512;   // 16 warps in four warpgroups (roles below)
 constexpr int kTcM = 128;         // rows per tile (TMEM lanes)
-constexpr int kTcPsi = 3;         // psi angles per particle held by a tile
-constexpr int kTcMaxN = 128;      // K = 2n <= 256, in steps of 64 (32 rows r)
-constexpr int kTcStages = 4;      // shared-memory ring of K steps
+constexpr int kTcPsi = 3;         // psi angles per particle a tile holds at most
+constexpr int kTcMaxN = 256;      // K = 2n <= 512, in steps of 64 (32 rows r)
+constexpr int kTcStages = 4;      // shared-memory ring of K steps (at most)
+
+// psi angles per tile: three up to crop 12; at crop 14 two, so that the MMA
+// accumulators and the stage-2 rows kept in TMEM fit its 512 columns.
+__host__ __device__ constexpr int tc_psi_group(int C) { return C <= 12 ? 3 : 2; }
+// shared-memory stages: four, three at n = 256 (larger particle columns and tables)
+__host__ __device__ constexpr int tc_stages(int N) { return N >= 256 ? 3 : 4; }
 constexpr int kTcMaxCand = 128;   // candidates per launch
 constexpr int kTcTmemCols = 512;  // two MMA accumulators of kN <= 80 columns + stage-2 rows
 constexpr float kTcScale = 8192.0f;               // 2^13 on each operand
@@ -58,7 +64,7 @@ constexpr unsigned kWaitLimit = 1u << 24;         // bounded mbarrier spin
 // every tcgen05.ld starts on an 8-column boundary.
 __host__ __device__ constexpr int tc_psi_stride(int C) { return ((2 * C + 7) / 8) * 8; }
 // MMA N: all psi angles, rounded up to a multiple of 16.
-__host__ __device__ constexpr int tc_n(int C) { return ((kTcPsi * tc_psi_stride(C) + 15) / 16) * 16; }
+__host__ __device__ constexpr int tc_n(int C) { return ((tc_psi_group(C) * tc_psi_stride(C) + 15) / 16) * 16; }
 
 struct TcParams {
   const __half* tbank;    // [n_slot][H][2 halves][2 parts][n/8][n_cand][8], scaled
@@ -184,20 +190,20 @@ __device__ __forceinline__ void stage2_row(float (&a)[C], float zr, float zi, ui
 // TMEM load / store of one accumulator row (C 32-bit columns)
 template <int C>
 __device__ __forceinline__ void tmem_ld_row(float (&a)[C], uint32_t ta) {
-  static_assert(C == 12 || C == 10 || C == 8 || C == 6 || C == 4 || C == 2, "even crop up to 12");
+  static_assert(C % 2 == 0 && C >= 2 && C <= 14, "even crop up to 14");
   uint32_t* r = reinterpret_cast<uint32_t*>(a);
   if constexpr (C >= 8) {
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                  : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
                  : "r"(ta));
   }
-  if constexpr (C == 12 || C == 4) {
-    constexpr int o = C - 4;
+  if constexpr (C == 12 || C == 4 || C == 14) {
+    constexpr int o = C == 14 ? 8 : C - 4;
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
                  : "=r"(r[o]), "=r"(r[o + 1]), "=r"(r[o + 2]), "=r"(r[o + 3])
                  : "r"(ta + o));
   }
-  if constexpr (C == 10 || C == 6 || C == 2) {
+  if constexpr (C == 10 || C == 6 || C == 2 || C == 14) {
     constexpr int o = C - 2;
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0,%1}, [%2];" : "=r"(r[o]), "=r"(r[o + 1]) : "r"(ta + o));
   }
@@ -215,12 +221,12 @@ __device__ __forceinline__ void tmem_st_row(const float (&a)[C], uint32_t ta) {
     asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(ta), "r"(r[0]),
                  "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]));
   }
-  if constexpr (C == 12 || C == 4) {
-    constexpr int o = C - 4;
+  if constexpr (C == 12 || C == 4 || C == 14) {
+    constexpr int o = C == 14 ? 8 : C - 4;
     asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(ta + o), "r"(r[o]),
                  "r"(r[o + 1]), "r"(r[o + 2]), "r"(r[o + 3]));
   }
-  if constexpr (C == 10 || C == 6 || C == 2) {
+  if constexpr (C == 10 || C == 6 || C == 2 || C == 14) {
     constexpr int o = C - 2;
     asm volatile("tcgen05.st.sync.aligned.32x32b.x2.b32 [%0], {%1,%2};" ::"r"(ta + o), "r"(r[o]), "r"(r[o + 1]));
   }
@@ -295,12 +301,12 @@ struct TcItem {
   int e0, a0, nd, psi0, g_psi;
 };
 
-__device__ __forceinline__ TcItem tc_item(const TcParams& P, int wi, int n, int H) {
-  const int n_groups = (P.n_psi + kTcPsi - 1) / kTcPsi;
+__device__ __forceinline__ TcItem tc_item(const TcParams& P, int wi, int n, int H, int psi_group) {
+  const int n_groups = (P.n_psi + psi_group - 1) / psi_group;
   const int b = P.work[2 * wi], tile = P.work[2 * wi + 1] / n_groups;
   TcItem it;
-  it.psi0 = (P.work[2 * wi + 1] - tile * n_groups) * kTcPsi;
-  it.g_psi = min(kTcPsi, P.n_psi - it.psi0);
+  it.psi0 = (P.work[2 * wi + 1] - tile * n_groups) * psi_group;
+  it.g_psi = min(psi_group, P.n_psi - it.psi0);
   it.e0 = P.local_ptr[b];
   const int d = P.local_ptr[b + 1] - it.e0;
   it.a0 = tile * P.dpt;
@@ -332,12 +338,13 @@ constexpr int kTcBuilders = 64;  // threads of warps 2-3
 template <int C, int N>
 __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  static_assert(C % 2 == 0 && C <= 12, "even crop up to 12");
+  static_assert(C % 2 == 0 && C <= 14, "even crop up to 14");
   static_assert(kTcThreads == 512, "four warpgroups");
+  static_assert(2 * tc_n(C) + tc_psi_group(C) * (C - tc_reg_rows<C>()) * C <= kTcTmemCols, "TMEM columns");
   constexpr int kN = tc_n(C);
   constexpr int kPS = tc_psi_stride(C);
   constexpr int h = C / 2;
-  constexpr int S = kTcStages;
+  constexpr int S = tc_stages(N);
   constexpr int NQ = N / 32;               // K steps per column: 32 rows r (64 K) each
   constexpr int n = N, H = N / 2 + 1;
   constexpr uint32_t a_part = kTcM * 128;  // bytes of A (hi or lo) per stage: 128 rows x 128 B
@@ -435,7 +442,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
       for (int s = 0; s < S; ++s) zeroed[s] = 0;
       bool ok = true;
       for (int wi = blockIdx.x; wi < P.n_work && ok; wi += gridDim.x) {
-        const TcItem it = tc_item(P, wi, n, H);
+        const TcItem it = tc_item(P, wi, n, H, tc_psi_group(C));
         const int used = it.nd * nc8;
         int slot = 0;
         if (lane < parts * it.nd) slot = P.local_idx[it.e0 + it.a0 + lane % it.nd];
@@ -482,7 +489,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
       uint32_t g = 0;
       bool ok = true;
       for (int wi = blockIdx.x; wi < P.n_work; wi += gridDim.x) {
-        const TcItem it = tc_item(P, wi, n, H);
+        const TcItem it = tc_item(P, wi, n, H, tc_psi_group(C));
         const int g_psi = it.g_psi;
         // columns 0 and 1 of this particle; later columns arrive by cp.async two
         // columns ahead (one group per column and thread)
@@ -569,7 +576,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
     uint32_t tuse[2] = {0, 0};
     bool ok = true;
     for (int wi = blockIdx.x; wi < P.n_work && ok; wi += gridDim.x) {
-      const bool active = my_psi < tc_item(P, wi, n, H).g_psi;  // warp-uniform; the rest is re-read at the end
+      const bool active = my_psi < tc_item(P, wi, n, H, tc_psi_group(C)).g_psi;  // warp-uniform; the rest is re-read at the end
       float acc[RR][C];  // [crop row][slot]
 #pragma unroll
       for (int y = 0; y < RR; ++y)
@@ -647,7 +654,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
           }
         }
       }
-      const TcItem it = tc_item(P, wi, n, H);
+      const TcItem it = tc_item(P, wi, n, H, tc_psi_group(C));
       const int dl = my_row / nc8, cand = my_row - dl * nc8;
       if (active && dl < it.nd && cand < n_cand) {
         const size_t o = (size_t)cand * P.nnz * P.n_psi + (size_t)(it.e0 + it.a0 + dl) * P.n_psi + it.psi0 + my_psi;
@@ -680,31 +687,38 @@ __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
 // at position c ^ (cand & 7) (the 128-byte swizzle of the shared-memory tile,
 // whose direction blocks start on multiples of 8 rows). One block per
 // (slot, candidate); every candidate writes whole 128-byte rows.
-__global__ void bank_to_fp16(const float2* __restrict__ bank, long long bank_stride, int n, int n_cand,
+__global__ void bank_to_fp16(const float2* __restrict__ bank, long long bank_stride, int n, int n_cand, int cb,
                              __half* __restrict__ out) {
-  extern __shared__ float2 s_t[];  // [n][H]
+  extern __shared__ float2 s_t[];  // [n][cb]: columns [c0, c0 + cb) of the template
   const int H = n / 2 + 1, nq = n / 32;
   const int slot = blockIdx.x, cand = blockIdx.y;
   const float2* src = bank + (size_t)cand * (size_t)bank_stride + (size_t)slot * n * H;
-  for (int t = threadIdx.x; t < n * H; t += blockDim.x) s_t[t] = src[t];
-  __syncthreads();
-  // one task per (col, step, chunk): 8 consecutive k -> hi and lo 16-byte chunks
-  for (int t = threadIdx.x; t < H * nq * 8; t += blockDim.x) {
-    const int c = t & 7, qq = (t >> 3) % nq, col = t / (8 * nq);
-    const bool imag = c >= 4;
-    const int r0 = qq * 32 + (c & 3) * 8;
-    float v[8];
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      const float2 z = s_t[(r0 + i) * H + col];
-      v[i] = (imag ? z.y : z.x) * kTcScale;
+  for (int c0 = 0; c0 < H; c0 += cb) {
+    const int w = min(cb, H - c0);
+    __syncthreads();
+    for (int t = threadIdx.x; t < n * w; t += blockDim.x) {
+      const int r = t / w, c = t - r * w;
+      s_t[r * cb + c] = src[(size_t)r * H + c0 + c];
     }
-    uint4 hi, lo;
-    split8(v, hi, lo);
-    const size_t row = (((size_t)slot * H + col) * nq + qq) * 2;  // part 0 row block
-    const int pos = c ^ (cand & 7);
-    *reinterpret_cast<uint4*>(out + ((row * n_cand + cand) * 8 + pos) * 8) = hi;
-    *reinterpret_cast<uint4*>(out + (((row + 1) * n_cand + cand) * 8 + pos) * 8) = lo;
+    __syncthreads();
+    // one task per (col, step, chunk): 8 consecutive k -> hi and lo 16-byte chunks
+    for (int t = threadIdx.x; t < w * nq * 8; t += blockDim.x) {
+      const int c = t & 7, qq = (t >> 3) % nq, cl = t / (8 * nq), col = c0 + cl;
+      const bool imag = c >= 4;
+      const int r0 = qq * 32 + (c & 3) * 8;
+      float v[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const float2 z = s_t[(r0 + i) * cb + cl];
+        v[i] = (imag ? z.y : z.x) * kTcScale;
+      }
+      uint4 hi, lo;
+      split8(v, hi, lo);
+      const size_t row = (((size_t)slot * H + col) * nq + qq) * 2;  // part 0 row block
+      const int pos = c ^ (cand & 7);
+      *reinterpret_cast<uint4*>(out + ((row * n_cand + cand) * 8 + pos) * 8) = hi;
+      *reinterpret_cast<uint4*>(out + (((row + 1) * n_cand + cand) * 8 + pos) * 8) = lo;
+    }
   }
 }
 
@@ -727,6 +741,9 @@ cudaError_t launch_tc_c(const TcParams& P, size_t smem, int grid, cudaStream_t s
     case 32: return launch_tc_cn<C, 32>(P, smem, grid, st);
     case 64: return launch_tc_cn<C, 64>(P, smem, grid, st);
     case 128: return launch_tc_cn<C, 128>(P, smem, grid, st);
+    case 256:
+      if constexpr (C >= 10) return launch_tc_cn<C, 256>(P, smem, grid, st);
+      return cudaErrorInvalidValue;
     default: return cudaErrorInvalidValue;
   }
 }
@@ -739,8 +756,8 @@ int correlate_tc_max_cand() { return kTcMaxCand; }
 
 size_t correlate_tc_smem_bytes(int n, int crop) {
   const size_t stage = 2 * (size_t)kTcM * 128 + 2 * (size_t)tc_n(crop) * 128;
-  return kTcStages * stage + 3 * (size_t)kTcPsi * n * sizeof(float2) + (size_t)n * sizeof(float2) +
-         (size_t)(n / 2 + 1) * tc_tw_entries(crop) * sizeof(float) + (3 * kTcStages + 4) * 8 + 8;
+  return tc_stages(n) * stage + 3 * (size_t)kTcPsi * n * sizeof(float2) + (size_t)n * sizeof(float2) +
+         (size_t)(n / 2 + 1) * tc_tw_entries(crop) * sizeof(float) + (3 * tc_stages(n) + 4) * 8 + 8;
 }
 
 // halves in the fp16 hi/lo bank copy of one candidate
@@ -759,10 +776,11 @@ int correlate_tc_dirs_per_tile(int n_cand) {
 // so CTAs running at the same time read the same template columns. A tile
 // holds 128 / n_cand whole directions (n_cand <= 128). Host arrays; returns
 // the item count.
-int correlate_tc_plan(const int* local_ptr, const int* local_idx, int n_particles, int n_cand, int n_psi,
+int correlate_tc_plan(const int* local_ptr, const int* local_idx, int n_particles, int n_cand, int n_psi, int crop,
                       int* work, int max_work) {
   struct Item { int key, b, tile; };
-  const int n_groups = (n_psi + kTcPsi - 1) / kTcPsi;
+  const int pg = tc_psi_group(crop);
+  const int n_groups = (n_psi + pg - 1) / pg;
   const int dpt = correlate_tc_dirs_per_tile(n_cand);
   std::vector<Item> items;
   for (int b = 0; b < n_particles; ++b) {
@@ -785,14 +803,15 @@ int correlate_tc_plan(const int* local_ptr, const int* local_idx, int n_particle
 cudaError_t launch_bank_to_fp16(cudaStream_t st, const float2* bank, long long bank_stride, int n_cand, int n_slot,
                                 int n, void* out) {
   if (n_cand <= 0 || n_slot <= 0) return cudaSuccess;
-  const size_t smem = (size_t)n * (n / 2 + 1) * sizeof(float2);
+  const int cb = std::min(n / 2 + 1, 128 * 1024 / (int)(n * sizeof(float2)));  // columns per staged block
+  const size_t smem = (size_t)n * cb * sizeof(float2);
   static size_t set_smem = 0;
   if (set_smem < smem) {
     cudaError_t e = cudaFuncSetAttribute(bank_to_fp16, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     set_smem = smem;
   }
-  bank_to_fp16<<<dim3(n_slot, n_cand), 256, smem, st>>>(bank, bank_stride, n, n_cand, (__half*)out);
+  bank_to_fp16<<<dim3(n_slot, n_cand), 256, smem, st>>>(bank, bank_stride, n, n_cand, cb, (__half*)out);
   return cudaGetLastError();
 }
 
@@ -829,6 +848,7 @@ cudaError_t launch_correlate_tc(cudaStream_t st, const void* tbank, int n_cand, 
     case 8: return launch_tc_c<8>(P, smem, grid, st);
     case 10: return launch_tc_c<10>(P, smem, grid, st);
     case 12: return launch_tc_c<12>(P, smem, grid, st);
+    case 14: return launch_tc_c<14>(P, smem, grid, st);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -327,10 +327,11 @@ class BatchScoringJob:
             ptr, idx = self._host_map
             np_ = len(job.records)
             count = C.c_int(0)
-            nat.call("gisapr_tc_plan_work", idx_ptr(ptr), idx_ptr(idx), np_, cc, job.n_psi, None, 0, C.byref(count))
+            nat.call("gisapr_tc_plan_work", idx_ptr(ptr), idx_ptr(idx), np_, cc, job.n_psi, job.cfg.crop, None, 0,
+                     C.byref(count))
             work = np.zeros((max(1, count.value), 2), dtype=np.int32)
-            nat.call("gisapr_tc_plan_work", idx_ptr(ptr), idx_ptr(idx), np_, cc, job.n_psi, idx_ptr(work),
-                     work.shape[0], C.byref(count))
+            nat.call("gisapr_tc_plan_work", idx_ptr(ptr), idx_ptr(idx), np_, cc, job.n_psi, job.cfg.crop,
+                     idx_ptr(work), work.shape[0], C.byref(count))
             self.tc_plans[cc] = (torch.from_numpy(work).to(job.device), count.value)
         return self.tc_plans[cc]
 

@@ -197,17 +197,19 @@ int gisapr_get_tuning(gisapr_ctx ctx, int key, int* value);
  *     rewritten on every call (fp16 hi/lo copy of the banks);
  *   work, n_work: device copy of the list made by gisapr_tc_plan_work
  *     (host arrays in, host array out: [n_work][2] (particle, tile of 128
- *     rows * psi groups + group of three psi angles), sorted by direction;
- *     work == NULL only counts; n_psi must match the correlation call);
+ *     rows * psi groups + group of psi angles: three, two at crop 14),
+ *     sorted by direction; work == NULL only counts; n_psi and crop must
+ *     match the correlation call);
  *   status: device int, set to 1 if an on-chip barrier wait ran out (the
  *     outputs are then incomplete); the caller zeroes it.
- * Sizes: n in {32, 64, 128}, crop even in 2..12, n_cand <= 128 per call (the
+ * Sizes: n in {32, 64, 128, 256}, crop even in 2..14 (10..14 at n = 256),
+ * n_cand <= 128 per call (the
  * work list is planned for that n_cand: a tile holds 128 / ceil8(n_cand)
  * whole directions).
  */
 long long gisapr_tc_bank_bytes(int n_slot, int n);
 int gisapr_tc_plan_work(const int* local_ptr, const int* local_idx, int n_particles, int n_cand, int n_psi,
-                        int* work, int max_work, int* n_work);
+                        int crop, int* work, int max_work, int* n_work);
 int gisapr_correlate_tc_batch(gisapr_ctx ctx, void* stream, const float* bank, long long bank_stride, int n_cand,
                               int n_slot, void* tbank, const float* stack, const int* local_ptr,
                               const int* local_idx, const int* work, int n_work, int nnz, int n_psi, int n, int crop,

@@ -65,22 +65,24 @@ def test_tensor_core_work_plan_on_host(native_lib):
     ptr = np.concatenate([[0], np.cumsum(counts)]).astype(np.int32)
     idx = np.concatenate([np.sort(rng.choice(50, size=c, replace=False)) for c in counts]).astype(np.int32)
     vp = lambda a: C.c_void_p(a.ctypes.data)
-    for n_cand, n_psi in ((1, 1), (5, 3), (64, 3), (128, 5), (48, 7), (100, 2)):
-        groups = -(-n_psi // 3)
+    for n_cand, n_psi, crop in ((1, 1, 12), (5, 3, 12), (64, 3, 12), (128, 5, 10), (48, 7, 8), (100, 2, 12),
+                                (64, 3, 14), (7, 5, 14)):
+        groups = -(-n_psi // (3 if crop <= 12 else 2))
         dpt = 128 // (-(-n_cand // 8) * 8)  # rows per direction rounded up to 8
         n = C.c_int(-1)
-        assert lib.gisapr_tc_plan_work(vp(ptr), vp(idx), 40, n_cand, n_psi, None, 0, C.byref(n)) == 0
+        assert lib.gisapr_tc_plan_work(vp(ptr), vp(idx), 40, n_cand, n_psi, crop, None, 0, C.byref(n)) == 0
         want = sum(-(-int(c) // dpt) for c in counts) * groups
         assert n.value == want
         work = np.zeros((max(1, want), 2), np.int32)
-        assert lib.gisapr_tc_plan_work(vp(ptr), vp(idx), 40, n_cand, n_psi, vp(work), want, C.byref(n)) == 0
+        assert lib.gisapr_tc_plan_work(vp(ptr), vp(idx), 40, n_cand, n_psi, crop, vp(work), want, C.byref(n)) == 0
         pairs = {(int(b), int(t)) for b, t in work[:want]}
         assert len(pairs) == want
         keys = [int(idx[ptr[b] + (t // groups) * dpt]) for b, t in work[:want]]
         assert keys == sorted(keys)
         if want > 1:
-            assert lib.gisapr_tc_plan_work(vp(ptr), vp(idx), 40, n_cand, n_psi, vp(work), want - 1,
+            assert lib.gisapr_tc_plan_work(vp(ptr), vp(idx), 40, n_cand, n_psi, crop, vp(work), want - 1,
                                            C.byref(n)) == 1
     n = C.c_int(0)
-    assert lib.gisapr_tc_plan_work(vp(ptr), vp(idx), 40, 129, 3, None, 0, C.byref(n)) == 1
+    assert lib.gisapr_tc_plan_work(vp(ptr), vp(idx), 40, 129, 3, 12, None, 0, C.byref(n)) == 1
+    assert lib.gisapr_tc_plan_work(vp(ptr), vp(idx), 40, 8, 3, 16, None, 0, C.byref(n)) == 4
     assert lib.gisapr_tc_bank_bytes(760, 128) == 760 * 65 * 2 * 256 * 2

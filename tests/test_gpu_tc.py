@@ -178,7 +178,7 @@ def test_tensor_path_rejects_unsupported_sizes(golden32):
     st = nat.stream_of(DEV)
     buf = torch.zeros(1 << 20, dtype=torch.uint8, device=DEV)
     p = nat.ptr(buf)
-    for n, crop, n_psi in [(256, 12, 3), (128, 14, 3), (96, 12, 3)]:
+    for n, crop, n_psi in [(512, 12, 3), (128, 16, 3), (96, 12, 3), (256, 8, 3)]:
         with pytest.raises(ValueError):
             nat.call("gisapr_correlate_tc_batch", ctx, st, p, 0, 1, 1, p, p, p, p, p, 1, 1, n_psi, n, crop, 1,
                      p, p, p, p)
@@ -186,3 +186,17 @@ def test_tensor_path_rejects_unsupported_sizes(golden32):
         nat.call("gisapr_correlate_tc_batch", ctx, st, p, 1 << 10, 129, 1, p, p, p, p, p, 1, 1, 3, 128, 12, 1,
                  p, p, p, p)
     _ = C
+
+
+def test_split_box256_crop14_matches_plain():
+    """The box-256 precision configuration (crop 14, psi groups of two) on a
+    small particle set: tensor-core split maps against the plain FP32 maps."""
+    spec = syn.WORKLOADS["box256_20kp"]
+    data = syn.make_job(spec, seed=3, device=DEV, n_particles=24)
+    job = ScoringJob(_cfg(spec), data.model.pdb_text, model_angles_from_lists(data.model_rot, data.model_tilt),
+                     records_from_job(data), data.images, fsc_values=data.fsc, device=DEV)
+    assert job.cfg.crop == 14 and job.cfg.new_box == 256
+    poses = list(syn.candidate_poses(3, 41, 5.0, 3.0))
+    plain, tc, want, got, err = _compare_to_plain(job, poses, "fp16x3", SPLIT_MAP_REL)
+    np.testing.assert_allclose(got, want, rtol=1e-6)
+    assert int(tc.tc_status.item()) == 0

@@ -49,8 +49,10 @@ def parse_args():
     ap.add_argument("--particles", type=int, default=0, help="override the particle count (tests only)")
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-sample", type=int, default=48, help="particles and templates in the CPU sample")
+    ap.add_argument("--cpu-sample", type=int, default=400, help="particles and templates in the CPU sample")
     ap.add_argument("--batch", type=int, default=64, help="candidates per batched generation (0: skip)")
+    ap.add_argument("--precision-particles", type=int, default=64,
+                    help="particles of the box-256 precision comparison (0: skip it)")
     ap.add_argument("--serve-requests", type=int, default=40,
                     help="requests in the serving stream (0: skip the serving measurement)")
     ap.add_argument("--precisions", default="fp32,fp16x3",
@@ -266,6 +268,47 @@ def run_reference(args):
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def run_precision(args, device):
+    """Box-256 precision configuration (crop 14, psi step 3.75, local 6 deg)
+    on a small particle set: the tensor-core forms against the plain FP32
+    batched path, per candidate score and per particle argmax (direction,
+    psi, shift). The FP64 comparison of the same forms is in the test suite
+    (tests/test_gpu_tc.py)."""
+    import numpy as np
+    from gisapr_gb300 import synthetic as syn
+    from gisapr_gb300.engine import BatchScoringJob, JobConfig, ScoringJob
+    from gisapr_gb300.tables import model_angles_from_lists
+    spec = syn.WORKLOADS["box256_20kp"]
+    n_part = args.precision_particles
+    data = syn.make_job(spec, seed=args.seed + 77, device=str(device), n_particles=n_part)
+    cfg = JobConfig(box=spec.box, apix=spec.apix, crop=spec.crop, psi_step=spec.psi_step,
+                    local_range=spec.local_range, mask_edge=spec.mask_edge, kk=spec.kk)
+    job = ScoringJob(cfg, data.model.pdb_text, model_angles_from_lists(data.model_rot, data.model_tilt),
+                     job_records(data), data.images, fsc_values=data.fsc, device=device)
+    poses = list(syn.candidate_poses(8, args.seed + 78, 5.0, 3.0))
+    runs = {}
+    for prec in ("fp32", "fp16x3", "fp16"):
+        bj = BatchScoringJob(job, len(poses), use_graph=False, precision=prec)
+        scores = bj.score_active(poses)
+        runs[prec] = (scores, bj.score_buf.cpu().numpy(),
+                      np.stack([t.cpu().numpy() for t in (bj.best_entry, bj.best_psi, bj.peak_y, bj.peak_x)], -1),
+                      bj.stage_ms(poses)["correlate"])
+        del bj
+    ref_scores, ref_maps, ref_arg, _ = runs["fp32"]
+    out = {"workload": f"box256_20kp shapes, {n_part} particles, {len(poses)} candidates",
+           "box": spec.box, "crop": spec.crop, "directions": len(data.model_rot),
+           "maps_per_candidate": job.nnz * job.n_psi}
+    for prec in ("fp16x3", "fp16"):
+        sc, maps, arg, ms = runs[prec]
+        valid = ref_arg[..., 0] >= 0
+        agree = np.all(arg == ref_arg, axis=-1)[valid]
+        out[prec] = {"score_max_rel_err_vs_fp32": float(np.max(np.abs(sc / ref_scores - 1.0))),
+                     "map_max_err_rel_to_scale": float(np.max(np.abs(maps - ref_maps)) / np.max(np.abs(ref_maps))),
+                     "argmax_agreement_vs_fp32": float(np.mean(agree)),
+                     "correlate_ms": ms, "plain_correlate_ms": runs["fp32"][3]}
+    return out
 
 
 SERVE_JOBS = (("box64_small", 2000), ("box128_5kp", 1000), ("box128_5kp", 2500))  # (workload, particles)
@@ -521,6 +564,8 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
         line["batched"] = batched
     if world == 1 and args.serve_requests > 0:
         line["serving"] = run_serving(args, device)
+    if world == 1 and args.precision_particles > 0:
+        line["precision"] = run_precision(args, device)
     if world == 1 and not args.no_cpu_baseline:
         cb = cpu_baseline(spec, data, poses[W], args.cpu_sample)
         line["cpu_baseline"] = {

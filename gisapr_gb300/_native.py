@@ -36,8 +36,8 @@ SIGNATURES = {
     "gisapr_particle_results_batch": [_p, _p, _p, _p, _p, _i, _i, _i, _p, _p, _p, _p, _p, _p],
     "gisapr_score_sum_batch": [_p, _p, _p, _i, _i, _p],
     "gisapr_tc_bank_bytes": [_i, _i],
-    "gisapr_set_tuning": [_p, _i, _i],
-    "gisapr_get_tuning": [_p, _i, _p],
+    "gisapr_set_tuning": [_p, _i, _i, _i],
+    "gisapr_get_tuning": [_p, _i, _i, _p],
     "gisapr_tc_plan_work": [_p, _p, _i, _i, _i, _i, _p, _i, _p],
     "gisapr_correlate_tc_batch": [_p, _p, _p, C.c_longlong, _i, _i, _p, _p, _p, _p, _p, _i, _i, _i, _i, _i, _i,
                                   _p, _p, _p, _p],
@@ -99,16 +99,17 @@ def stream_of(device) -> C.c_void_p:
 
 TUNE_CORR_CLUSTER = 1  # gisapr_set_tuning keys (include/gisapr_gb300.h)
 
-# Process-wide launch-shape settings applied to every native context at
-# creation (and to this thread's contexts when changed); set by the autotuner.
+# Process-wide launch-shape settings, (key, size) -> value, applied to every
+# native context at creation (and to this thread's contexts when changed);
+# set by the autotuner.
 DEFAULT_TUNING: dict = {}
 
 
-def set_default_tuning(key: int, value: int) -> None:
-    DEFAULT_TUNING[int(key)] = int(value)
+def set_default_tuning(key: int, size: int, value: int) -> None:
+    DEFAULT_TUNING[(int(key), int(size))] = int(value)
     cache = getattr(Context._per_thread, "ctx", None) or {}
     for ctx in cache.values():
-        call("gisapr_set_tuning", ctx.handle, int(key), int(value))
+        call("gisapr_set_tuning", ctx.handle, int(key), int(size), int(value))
 
 
 class Context:
@@ -121,8 +122,8 @@ class Context:
         h = C.c_void_p()
         call("gisapr_context_create", self.device_index, C.byref(h))
         self.handle = h
-        for key, value in DEFAULT_TUNING.items():
-            call("gisapr_set_tuning", h, key, value)
+        for (key, size), value in DEFAULT_TUNING.items():
+            call("gisapr_set_tuning", h, key, size, value)
 
     def __del__(self):
         h = getattr(self, "handle", None)

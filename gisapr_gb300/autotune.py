@@ -54,13 +54,14 @@ def plain_smem_bytes(n: int, n_psi: int, crop: int, cluster: int) -> int:
 @dataclass
 class TuneResult:
     key: str
+    size: int
     corr_cluster: int
     tc_chunk: int
     times_ms: Dict[str, float] = field(default_factory=dict)
 
     def apply(self) -> None:
-        """Make the cluster size the default of every native context."""
-        nat.set_default_tuning(nat.TUNE_CORR_CLUSTER, self.corr_cluster)
+        """Make the cluster size the default of every native context at this size."""
+        nat.set_default_tuning(nat.TUNE_CORR_CLUSTER, self.size, self.corr_cluster)
 
 
 class Autotuner:
@@ -118,12 +119,12 @@ class Autotuner:
         for k in clusters:
             if plain_smem_bytes(nb, n_psi, crop, k) > SMEM_LIMIT or k > nb // 2 + 1:
                 continue
-            nat.call("gisapr_set_tuning", ctx.handle, nat.TUNE_CORR_CLUSTER, k)
+            nat.call("gisapr_set_tuning", ctx.handle, nat.TUNE_CORR_CLUSTER, nb, k)
             t = self._time_correlate(job, n_cand, "fp32", poses)
             times[f"plain_cluster_{k}"] = t
             if t < best_t:
                 best_k, best_t = k, t
-        nat.call("gisapr_set_tuning", ctx.handle, nat.TUNE_CORR_CLUSTER, best_k)
+        nat.call("gisapr_set_tuning", ctx.handle, nat.TUNE_CORR_CLUSTER, nb, best_k)
         best_c = min(128, n_cand)
         if precision != "fp32":
             best_ct = math.inf
@@ -132,7 +133,7 @@ class Autotuner:
                 times[f"tc_chunk_{c}"] = t
                 if t < best_ct:
                     best_c, best_ct = c, t
-        r = TuneResult(key=key, corr_cluster=best_k, tc_chunk=best_c, times_ms=times)
+        r = TuneResult(key=key, size=nb, corr_cluster=best_k, tc_chunk=best_c, times_ms=times)
         cache[key] = asdict(r)
         self._save(cache)
         r.apply()

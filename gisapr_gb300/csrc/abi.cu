@@ -119,7 +119,7 @@ struct gisapr_context {
   std::map<std::pair<int, int>, CorrTables> corr;      // (n, crop) -> twiddles
   DeviceBuffer atoms, bin_counts, bin_lists, proj_scratch, prep_scratch;
   int sm_count = 152;
-  int tune_corr_cluster = 0;  // CTAs per particle in the plain correlation (0: default)
+  std::map<int, int> tune_corr_cluster;  // n -> CTAs per particle in the plain correlation
 };
 
 namespace {
@@ -249,6 +249,11 @@ int get_corr_tables(gisapr_ctx ctx, int n, int crop, CorrTables* out) {
   ctx->corr[key] = t;
   *out = t;
   return GISAPR_OK;
+}
+
+int tuned_cluster(gisapr_ctx ctx, int n) {
+  auto it = ctx->tune_corr_cluster.find(n);
+  return it == ctx->tune_corr_cluster.end() ? 0 : it->second;
 }
 
 int check_box(int box) {
@@ -485,7 +490,8 @@ int gisapr_correlate_batch(gisapr_ctx ctx, void* stream, const float* bank, long
     return fail(GISAPR_ERR_UNSUPPORTED, "correlation size must be a multiple of 16 in [32, 256]");
   if (crop < 2 || crop > 16 || crop % 2 != 0 || crop > n)
     return fail(GISAPR_ERR_UNSUPPORTED, "crop must be even, 2..16 and <= n");
-  const size_t smem = correlate_smem_bytes(n, n_psi, crop, ctx->tune_corr_cluster);
+  const int cluster = tuned_cluster(ctx, n);
+  const size_t smem = correlate_smem_bytes(n, n_psi, crop, cluster);
   if (smem > 227 * 1024)
     return fail(GISAPR_ERR_UNSUPPORTED, "too many psi angles for the shared-memory particle slice");
   int rc = set_device(ctx);
@@ -496,8 +502,7 @@ int gisapr_correlate_batch(gisapr_ctx ctx, void* stream, const float* bank, long
   if (nnz < 0) return fail(GISAPR_ERR_ARGUMENT, "nnz < 0");
   GISAPR_CHECK_CUDA(launch_correlate_plain((cudaStream_t)stream, (const float2*)bank, (const float2*)stack,
                                            local_ptr, local_idx, n_particles, n_psi, n, crop, t.outer, t.col,
-                                           out_score, out_y, out_x, n_cand, bank_stride, nnz,
-                                           ctx->tune_corr_cluster),
+                                           out_score, out_y, out_x, n_cand, bank_stride, nnz, cluster),
                     "correlate");
   return GISAPR_OK;
 }
@@ -514,7 +519,8 @@ int gisapr_correlate(gisapr_ctx ctx, void* stream, const float* bank, const floa
     return fail(GISAPR_ERR_UNSUPPORTED, "correlation size must be a multiple of 16 in [32, 256]");
   if (crop < 2 || crop > 16 || crop % 2 != 0 || crop > n)
     return fail(GISAPR_ERR_UNSUPPORTED, "crop must be even, 2..16 and <= n");
-  const size_t smem = correlate_smem_bytes(n, n_psi, crop, ctx->tune_corr_cluster);
+  const int cluster = tuned_cluster(ctx, n);
+  const size_t smem = correlate_smem_bytes(n, n_psi, crop, cluster);
   if (smem > 227 * 1024)
     return fail(GISAPR_ERR_UNSUPPORTED, "too many psi angles for the shared-memory particle slice");
   int rc = set_device(ctx);
@@ -524,29 +530,34 @@ int gisapr_correlate(gisapr_ctx ctx, void* stream, const float* bank, const floa
   if (rc) return rc;
   GISAPR_CHECK_CUDA(launch_correlate_plain((cudaStream_t)stream, (const float2*)bank, (const float2*)stack,
                                            local_ptr, local_idx, n_particles, n_psi, n, crop, t.outer, t.col,
-                                           out_score, out_y, out_x, 1, 0, 0, ctx->tune_corr_cluster),
+                                           out_score, out_y, out_x, 1, 0, 0, cluster),
                     "correlate");
   return GISAPR_OK;
 }
 
-int gisapr_set_tuning(gisapr_ctx ctx, int key, int value) {
+int gisapr_set_tuning(gisapr_ctx ctx, int key, int size, int value) {
   if (!ctx) return fail(GISAPR_ERR_ARGUMENT, "context is NULL");
   switch (key) {
     case GISAPR_TUNE_CORR_CLUSTER:
       if (value < 0 || value > 8) return fail(GISAPR_ERR_ARGUMENT, "correlation cluster size must be 0..8");
-      ctx->tune_corr_cluster = value;
+      if (size < 32 || size > 256 || size % 16 != 0)
+        return fail(GISAPR_ERR_ARGUMENT, "correlation size must be a multiple of 16 in [32, 256]");
+      if (value == 0) ctx->tune_corr_cluster.erase(size);
+      else ctx->tune_corr_cluster[size] = value;
       return GISAPR_OK;
     default:
       return fail(GISAPR_ERR_ARGUMENT, "unknown tuning key " + std::to_string(key));
   }
 }
 
-int gisapr_get_tuning(gisapr_ctx ctx, int key, int* value) {
+int gisapr_get_tuning(gisapr_ctx ctx, int key, int size, int* value) {
   if (!ctx || !value) return fail(GISAPR_ERR_ARGUMENT, "context or value is NULL");
   switch (key) {
-    case GISAPR_TUNE_CORR_CLUSTER:
-      *value = ctx->tune_corr_cluster;
+    case GISAPR_TUNE_CORR_CLUSTER: {
+      auto it = ctx->tune_corr_cluster.find(size);
+      *value = it == ctx->tune_corr_cluster.end() ? 0 : it->second;
       return GISAPR_OK;
+    }
     default:
       return fail(GISAPR_ERR_ARGUMENT, "unknown tuning key " + std::to_string(key));
   }

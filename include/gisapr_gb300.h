@@ -173,16 +173,16 @@ int gisapr_correlate_batch(gisapr_ctx ctx, void* stream, const float* bank, long
                            int nnz, int n_psi, int n, int crop, float* out_score, int* out_y, int* out_x);
 
 /*
- * Launch-shape knobs of a context, chosen by the autotuner
- * (gisapr_gb300/autotune.py); no counterpart in the reference.
+ * Launch-shape knobs of a context per transform size, chosen by the
+ * autotuner (gisapr_gb300/autotune.py); no counterpart in the reference.
  *   GISAPR_TUNE_CORR_CLUSTER: CTAs per particle (thread-block cluster size,
- *     1..8; 0 = the default for the size) of gisapr_correlate and
- *     gisapr_correlate_batch. Results do not depend on it beyond float32
- *     summation order of the cluster's partial maps.
+ *     1..8; 0 = the default) of gisapr_correlate and gisapr_correlate_batch
+ *     at correlation size ``size``. Results do not depend on it beyond
+ *     float32 summation order of the cluster's partial maps.
  */
 enum { GISAPR_TUNE_CORR_CLUSTER = 1 };
-int gisapr_set_tuning(gisapr_ctx ctx, int key, int value);
-int gisapr_get_tuning(gisapr_ctx ctx, int key, int* value);
+int gisapr_set_tuning(gisapr_ctx ctx, int key, int size, int value);
+int gisapr_get_tuning(gisapr_ctx ctx, int key, int size, int* value);
 
 /*
  * Tensor-core form of gisapr_correlate_batch (tcgen05 MMA, FP32 accumulate),

@@ -52,11 +52,11 @@ def test_tune_caches_and_keeps_scores(golden32, tmp_path):
         # every cluster size gives the same maps up to float32 summation order
         ctx = nat.Context.for_device(DEV)
         for k in (1, 2, 3):
-            nat.call("gisapr_set_tuning", ctx.handle, nat.TUNE_CORR_CLUSTER, k)
+            nat.call("gisapr_set_tuning", ctx.handle, nat.TUNE_CORR_CLUSTER, 32, k)
             np.testing.assert_allclose(BatchScoringJob(job, 8, use_graph=False).score_active(poses), ref, rtol=1e-6)
         with pytest.raises(ValueError):
-            nat.call("gisapr_set_tuning", ctx.handle, nat.TUNE_CORR_CLUSTER, 9)
+            nat.call("gisapr_set_tuning", ctx.handle, nat.TUNE_CORR_CLUSTER, 32, 9)
         with pytest.raises(ValueError):
-            nat.call("gisapr_set_tuning", ctx.handle, 77, 1)
+            nat.call("gisapr_set_tuning", ctx.handle, 77, 32, 1)
     finally:
-        nat.set_default_tuning(nat.TUNE_CORR_CLUSTER, 0)
+        nat.set_default_tuning(nat.TUNE_CORR_CLUSTER, 32, 0)

@@ -51,6 +51,7 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=400, help="particles and templates in the CPU sample")
     ap.add_argument("--batch", type=int, default=64, help="candidates per batched generation (0: skip)")
+    ap.add_argument("--no-autotune", action="store_true", help="default launch shapes (no tuning runs)")
     ap.add_argument("--precision-particles", type=int, default=64,
                     help="particles of the box-256 precision comparison (0: skip it)")
     ap.add_argument("--serve-requests", type=int, default=40,
@@ -496,12 +497,16 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
         # candidates per tensor-core launch), timed on this job
         from gisapr_gb300.autotune import Autotuner
         t_tune = time.perf_counter()
-        tuned = Autotuner(trials=1).tune(job, n_cand=args.batch, precision="fp16x3")
-        autotune = {"corr_cluster": tuned.corr_cluster, "tc_chunk": tuned.tc_chunk,
-                    "correlate_ms": tuned.times_ms, "tune_s": time.perf_counter() - t_tune}
+        if args.no_autotune:
+            tuned = None
+            autotune = {"corr_cluster": "default", "tc_chunk": min(args.batch, 128)}
+        else:
+            tuned = Autotuner(trials=1).tune(job, n_cand=args.batch, precision="fp16x3")
+            autotune = {"corr_cluster": tuned.corr_cluster, "tc_chunk": tuned.tc_chunk,
+                        "correlate_ms": tuned.times_ms, "tune_s": time.perf_counter() - t_tune}
         for precision in args.precisions.split(","):
             batched[precision] = run_batched(job, dens, gen, precision, args.batch, K, W, device, barrier,
-                                             tc_chunk=tuned.tc_chunk)
+                                             tc_chunk=tuned.tc_chunk if tuned else 128)
             batched[precision]["autotune"] = autotune
     tl = [elapsed, e2e_elapsed]
     for b in batched.values():

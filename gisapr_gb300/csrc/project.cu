@@ -597,7 +597,7 @@ __device__ void build_one_smem(const ProjParams& P, int dir, int slot, float2* Z
     constexpr int CPR = pass_a_cols<N>();
     const StageLines<N> S{stage_all + warp * (2 * CPR * plane_ld(N))};
     for (int c0 = warp * CPR; c0 < W; c0 += kSmemWarps * CPR) {
-#pragma unroll 2
+#pragma unroll 4
       for (int idx = lane; idx < CPR * m; idx += 32) {
         const int cl = idx / m, r = idx % m;  // r: standard-order row of the 2N grid
         const int c = c0 + cl;
@@ -687,17 +687,21 @@ __device__ void build_one_smem(const ProjParams& P, int dir, int slot, float2* Z
   for (int c0 = warp * G; c0 < HC; c0 += kSmemWarps * G)
     warp_fft<N, -1>(ColLines<N>{Z, c0}, min(G, HC - c0), tw);
   __syncthreads();
+  // radial |F| sums: float32 per lane (the reference sums in float32 with
+  // scatter_add_), float64 across the warp
   for (int b = warp; b < P.n_bins; b += kSmemWarps) {
-    double acc = 0.0;
-    for (int e = P.bin_ptr[b] + lane; e < P.bin_ptr[b + 1]; e += 32) {
-      const int idx = P.bin_list[e];
+    float acc = 0.f;
+    const int e1 = P.bin_ptr[b + 1];
+#pragma unroll 4
+    for (int e = P.bin_ptr[b] + lane; e < e1; e += 32) {
+      const int idx = __ldg(P.bin_list + e);
       const int r = idx / HC, kx = idx - r * HC;
       const float2 f = Z(r, kx);
-      const double a = (double)hypotf(f.x, f.y);
-      acc += (kx == 0 || kx == N / 2) ? a : 2.0 * a;
+      const float a = hypotf(f.x, f.y);
+      acc += (kx == 0 || kx == N / 2) ? a : 2.0f * a;
     }
-    acc = warp_sum_d(acc);
-    if (lane == 0) s_div[b] = (b == 0) ? 1.0f : (float)((double)P.bin_count[b] / acc);
+    const double accd = warp_sum_d((double)acc);
+    if (lane == 0) s_div[b] = (b == 0) ? 1.0f : (float)((double)P.bin_count[b] / accd);
   }
   __syncthreads();
 
@@ -717,7 +721,7 @@ __device__ void build_one_smem(const ProjParams& P, int dir, int slot, float2* Z
 
   // ---- pass E: inverse row transform (real part), plane-fit sums
   const float scale_e = (float)(1.0 / ((double)N * (double)N));
-  double sz = 0.0, sxz = 0.0, syz = 0.0;
+  float fz = 0.f, fxz = 0.f, fyz = 0.f;  // float32 partial sums, float64 across the block
   for (int r0 = warp * G; r0 < N; r0 += kSmemWarps * G) {
     const RowLines<N> RL{Z, r0};
     // Hermitian extension of each row: position N-k takes conj(G(k)); only
@@ -735,14 +739,14 @@ __device__ void build_one_smem(const ProjParams& P, int dir, int slot, float2* Z
       const int i = r0 + g;
       const float w = RL.at(g, j).x * scale_e;
       RL.at(g, j) = make_float2(w, 0.f);
-      sz += (double)w;
-      sxz += (double)i * (double)w;
-      syz += (double)j * (double)w;
+      fz += w;
+      fxz = fmaf((float)i, w, fxz);
+      fyz = fmaf((float)j, w, fyz);
     }
   }
-  sz = block_sum_d(sz, red);
-  sxz = block_sum_d(sxz, red);
-  syz = block_sum_d(syz, red);
+  const double sz = block_sum_d((double)fz, red);
+  const double sxz = block_sum_d((double)fxz, red);
+  const double syz = block_sum_d((double)fyz, red);
   if (threadIdx.x == 0) {
     const double n = (double)N, n2 = n * n;
     const double s1 = n * (n - 1.0) / 2.0 * n;
@@ -764,16 +768,18 @@ __device__ void build_one_smem(const ProjParams& P, int dir, int slot, float2* Z
     s_coef[3] = (sz - c0 * s1 - c1 * s1 - c2 * n2) / n2;
   }
   __syncthreads();
-  const double pc0 = s_coef[0], pc1 = s_coef[1], pc2 = s_coef[2], mean = s_coef[3];
-  double sv = 0.0;
+  // plane and mean removal in float32 (the reference's precision), variance
+  // summed in float32 per thread and float64 across the block
+  const float fp0 = (float)s_coef[0], fp1 = (float)s_coef[1], fpc = (float)(s_coef[2] + s_coef[3]);
+  float fsv = 0.f;
   for (int t = threadIdx.x; t < N * N; t += blockDim.x) {
     const int i = t / N, j = t - i * N;
-    const double v = (double)Z(i, j).x - (pc0 * i + pc1 * j + pc2) - mean;
-    sv += v * v;
+    const float v = Z(i, j).x - fmaf(fp0, (float)i, fmaf(fp1, (float)j, fpc));
+    fsv = fmaf(v, v, fsv);
   }
-  sv = block_sum_d(sv, red);
+  const double sv = block_sum_d((double)fsv, red);
   const double sd = sqrt(sv / ((double)N * (double)N));
-  const double inv_sd = sd > 1e-12 ? 1.0 / sd : 1.0;
+  const float inv_sd = sd > 1e-12 ? (float)(1.0 / sd) : 1.0f;
 
   // ---- pass F: normalise, mask, forward row FFT
   for (int r0 = warp * G; r0 < N; r0 += kSmemWarps * G) {
@@ -782,8 +788,8 @@ __device__ void build_one_smem(const ProjParams& P, int dir, int slot, float2* Z
     for (int t = 0; t < 16; ++t) {
       const int idx = lane + 32 * t, g = idx / N, j = idx % N;
       const int i = r0 + g;
-      float f = (float)(((double)RL.at(g, j).x - (pc0 * i + pc1 * j + pc2) - mean) * inv_sd);
-      if (P.mask != nullptr) f *= P.mask[i * N + j];
+      float f = (RL.at(g, j).x - fmaf(fp0, (float)i, fmaf(fp1, (float)j, fpc))) * inv_sd;
+      if (P.mask != nullptr) f *= __ldg(P.mask + i * N + j);
       RL.at(g, j) = make_float2(f, 0.f);
     }
     __syncwarp();
@@ -794,8 +800,8 @@ __device__ void build_one_smem(const ProjParams& P, int dir, int slot, float2* Z
   for (int c0 = warp * G; c0 < HC; c0 += kSmemWarps * G)
     warp_fft<N, -1>(ColLines<N>{Z, c0}, min(G, HC - c0), tw);
   __syncthreads();
-  // crop + pack + FSC, L2 norm, pre-shifted write
-  double ss = 0.0;
+  // crop + pack + FSC, L2 norm (float32 per thread, float64 across the block), pre-shifted write
+  float fss = 0.f;
   for (int t = threadIdx.x; t < nb * H; t += blockDim.x) {
     const int r = t / H, c = t - r * H;
     const int ky = r < nb / 2 ? r : r - nb;
@@ -803,10 +809,10 @@ __device__ void build_one_smem(const ProjParams& P, int dir, int slot, float2* Z
     if (c < nb / 2) f = Z((ky + N) % N, c);
     else if (nb == N) f = Z((ky + N) % N, N / 2);
     else f = cconj(Z((-ky + N) % N, nb / 2));
-    f = cscale(f, P.fsc[t]);
-    ss += (double)f.x * f.x + (double)f.y * f.y;
+    f = cscale(f, __ldg(P.fsc + t));
+    fss = fmaf(f.x, f.x, fmaf(f.y, f.y, fss));
   }
-  ss = block_sum_d(ss, red);
+  const double ss = block_sum_d((double)fss, red);
   const float inv_norm = (float)(1.0 / sqrt(ss));
   float2* out = P.bank + (size_t)slot * nb * H;
   for (int t = threadIdx.x; t < nb * H; t += blockDim.x) {

@@ -48,6 +48,7 @@ struct ProjParams {
   const int* out_slot;      // output row in bank for each build index (null => dirs[i])
   float2* scratch;          // per-CTA scratch
   size_t scratch_stride;    // complex elements per CTA
+  const float2* slices;     // [n_build][N+1][2N] gathered slices, even rows then odd rows (or null)
   int N;
   int nb;
 };
@@ -404,6 +405,9 @@ __global__ void __launch_bounds__(kThreads) project_templates(ProjParams P) {
 
 }  // namespace
 
+// complex elements of the gathered slices of n_build templates (fast path)
+size_t project_slice_elems(int N, int n_build) { return (size_t)n_build * (N + 1) * 2 * N; }
+
 size_t project_scratch_elems(int N, int nb) {
   return (size_t)N * (N + 1) + (size_t)nb * (nb / 2 + 1);
 }
@@ -425,7 +429,7 @@ cudaError_t launch_project_templates(cudaStream_t st, const float2* spectrum, co
   ProjParams P;
   P.spectrum = spectrum; P.rot = rot; P.dirs = dirs; P.n_build = n_build; P.mask = mask;
   P.fsc = fsc; P.bin_list = bin_list; P.bin_ptr = bin_ptr; P.bin_count = bin_count;
-  P.n_bins = n_bins; P.tw = tw; P.bank = bank; P.out_slot = out_slot; P.scratch = scratch;
+  P.n_bins = n_bins; P.tw = tw; P.bank = bank; P.out_slot = out_slot; P.scratch = scratch; P.slices = nullptr;
   P.scratch_stride = project_scratch_elems(N, nb); P.N = N; P.nb = nb;
   const size_t smem = project_smem_bytes(N, n_bins);
   static size_t set_smem = 0;
@@ -455,11 +459,13 @@ namespace {
 constexpr int kSmemThreads = 384;
 constexpr int kSmemWarps = kSmemThreads / 32;
 
-// Columns a warp gathers per pass-A round (both row parities of each column
-// form one FFT line); at N = 128 one column, so that sixteen warps' staging
-// lines fit next to the plane.
+// Columns a warp transforms per pass-A round: G = 32 / (N/16) lines, two
+// per column (even and odd rows of the 2N grid). The even line of column c
+// is transformed in place in plane column c (which then receives the
+// column's output); only the odd lines need staging.
 template <int N>
-__host__ __device__ constexpr int pass_a_cols() { return N == 128 ? 1 : 16 / (N / 16); }
+__host__ __device__ constexpr int pass_a_cols() { return 16 / (N / 16); }
+
 
 // Row stride (complex elements) of the padded shared-memory plane: holds the
 // N + 1 columns plus one spare slot per 8, chosen by a bank-conflict search.
@@ -534,6 +540,39 @@ struct StageLines {  // staging lines of one warp, same padding along the line
   __device__ __forceinline__ float2& at(int g, int k) const { return p[g * plane_ld(N) + k + (k >> 3)]; }
 };
 
+// The value of the central slice at row r (standard order of the 2N grid)
+// and column c: the reference's float32 coordinates, border-clamped
+// trilinear sample, conjugated where the rotated x is negative.
+template <int N>
+__device__ __forceinline__ float2 slice_value(const float2* __restrict__ spectrum, const float* __restrict__ R,
+                                              int r, int c) {
+  constexpr int m = 2 * N;
+  const float inv_m = (float)(1.0 / (double)m);
+  const int kys = (r + N) % m;
+  const float gy = __fmul_rn((float)(kys - N), inv_m);
+  const float gx = __fmul_rn((float)c, inv_m);
+  float rx = __fadd_rn(__fmul_rn(R[0], gx), __fmul_rn(R[1], gy));
+  float ry = __fadd_rn(__fmul_rn(R[3], gx), __fmul_rn(R[4], gy));
+  float rz = __fadd_rn(__fmul_rn(R[6], gx), __fmul_rn(R[7], gy));
+  const bool conj = rx < 0.0f;
+  if (conj) { rx = -rx; ry = -ry; rz = -rz; }
+  const float cz = __fadd_rn(__fmul_rn(rz, (float)m), (float)(m / 2));
+  const float cy = __fadd_rn(__fmul_rn(ry, (float)m), (float)(m / 2));
+  const float cx = __fmul_rn(rx, (float)m);
+  float2 v = sample_slice<N>(spectrum, cz, cy, cx);
+  if (conj) v.y = -v.y;
+  return v;
+}
+
+// Lines of pass A: line 2q is plane column c0 + q, line 2q + 1 staging line q.
+template <int N>
+struct PassALines {
+  Plane<N> pl; int c0; float2* st;
+  __device__ __forceinline__ float2& at(int g, int k) const {
+    return (g & 1) ? st[(g >> 1) * plane_ld(N) + k + (k >> 3)] : pl(k, c0 + (g >> 1));
+  }
+};
+
 // In-place four-step FFT of ``nlines`` (<= 32 / (N/16)) lines, natural order
 // in and out: a 16-point register codelet over n1, twiddles, then N/16-point
 // codelets over n2 (N = 16 * (N/16)). One warp, warp barriers only.
@@ -579,56 +618,56 @@ __device__ __forceinline__ void warp_fft(const Lines& L, int nlines, const float
 }
 
 template <int N>
-__device__ void build_one_smem(const ProjParams& P, int dir, int slot, float2* Zs, float2* stage_all,
+__device__ void build_one_smem(const ProjParams& P, int b_index, int slot, float2* Zs, float2* stage_all,
                                const float2* tw, float* s_div, double* red, double* s_coef) {
   constexpr int m = 2 * N, W = N + 1, HC = N / 2 + 1, L2 = N / 16, G = 32 / L2;
   const Plane<N> Z{Zs};
   const int nb = P.nb, H = nb / 2 + 1;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const float* R = P.rot + (size_t)dir * 9;
-  const float R00 = R[0], R01 = R[1], R10 = R[3], R11 = R[4], R20 = R[6], R21 = R[7];
-  const float inv_m = (float)(1.0 / (double)m);
 
-  // ---- pass A: gather + pruned row inverse. A warp round takes CPR = 16/L2
-  // columns: both parities of each column form G = 2*CPR lines of N samples
-  // in the warp's staging area, one warp FFT transforms them, and the
-  // even/odd pair combines into the N centred rows of the 2N-point inverse.
+  // ---- pass A: pruned row inverse of the gathered slice. A warp round takes
+  // CPR = 16/L2 columns (G = 2*CPR lines of N: even rows in the plane column,
+  // odd rows staged), one warp FFT transforms them, and each even/odd pair
+  // combines into the N centred rows of the 2N-point inverse, written back
+  // into the column (output row (k + N/2) mod N takes frequency k).
   {
     constexpr int CPR = pass_a_cols<N>();
-    const StageLines<N> S{stage_all + warp * (2 * CPR * plane_ld(N))};
+    float2* st = stage_all + warp * (CPR * plane_ld(N));
+    const float2* sl = P.slices + (size_t)b_index * W * m;
     for (int c0 = warp * CPR; c0 < W; c0 += kSmemWarps * CPR) {
-#pragma unroll 4
-      for (int idx = lane; idx < CPR * m; idx += 32) {
-        const int cl = idx / m, r = idx % m;  // r: standard-order row of the 2N grid
-        const int c = c0 + cl;
-        float2 v = make_float2(0.f, 0.f);
-        if (c < W) {
-          const int kys = (r + N) % m;
-          const float gy = __fmul_rn((float)(kys - N), inv_m);
-          const float gx = __fmul_rn((float)c, inv_m);
-          float rx = __fadd_rn(__fmul_rn(R00, gx), __fmul_rn(R01, gy));
-          float ry = __fadd_rn(__fmul_rn(R10, gx), __fmul_rn(R11, gy));
-          float rz = __fadd_rn(__fmul_rn(R20, gx), __fmul_rn(R21, gy));
-          const bool conj = rx < 0.0f;
-          if (conj) { rx = -rx; ry = -ry; rz = -rz; }
-          const float cz = __fadd_rn(__fmul_rn(rz, (float)m), (float)(m / 2));
-          const float cy = __fadd_rn(__fmul_rn(ry, (float)m), (float)(m / 2));
-          const float cx = __fmul_rn(rx, (float)m);
-          v = sample_slice<N>(P.spectrum, cz, cy, cx);
-          if (conj) v.y = -v.y;
-        }
-        S.at(cl * 2 + (r & 1), r >> 1) = v;
+      const int nc = min(CPR, W - c0);
+      const PassALines<N> L{Z, c0, st};
+      for (int idx = lane; idx < nc * m; idx += 32) {
+        const int cl = idx / m, i = idx - cl * m;  // i < N: even row 2i, else odd row 2(i-N)+1
+        L.at(cl * 2 + (i >= N), i < N ? i : i - N) = __ldg(sl + (size_t)(c0 + cl) * m + i);
       }
       __syncwarp();
-      warp_fft<N, 1>(S, 2 * CPR, tw);
-      for (int idx = lane; idx < CPR * N; idx += 32) {
-        const int cl = idx / N, k = idx % N;
-        const int c = c0 + cl;
-        if (c < W) {
-          const int u = k < N / 2 ? k : k - N;
-          const float2 a0 = S.at(cl * 2, k), a1 = S.at(cl * 2 + 1, k);
-          Z(u + N / 2, c) = cadd(a0, cmul(tw_pos(tw, u, m), a1));
+      warp_fft<N, 1>(L, 2 * nc, tw);
+      constexpr int KPL = N / 32;  // frequencies per lane and column
+      if constexpr (KPL >= 2) {
+        // frequency k = lane + 32 t lands on row k + N/2 = lane + 32 (t + KPL/2)
+        // (mod N): the same lane, so each lane swaps its pairs in place
+        for (int cl = 0; cl < nc; ++cl) {
+#pragma unroll
+          for (int t = 0; t < KPL / 2; ++t) {
+            const int k0 = lane + 32 * t, k1 = k0 + N / 2;
+            const float2 o0 = cadd(L.at(cl * 2, k0), cmul(tw_pos(tw, k0, m), L.at(cl * 2 + 1, k0)));
+            const float2 o1 = cadd(L.at(cl * 2, k1), cmul(tw_pos(tw, k1 - N, m), L.at(cl * 2 + 1, k1)));
+            Z(k1, c0 + cl) = o0;
+            Z(k0, c0 + cl) = o1;
+          }
         }
+      } else {
+        float2 out[CPR];
+#pragma unroll
+        for (int cl = 0; cl < CPR; ++cl) {
+          const int k = lane, u = k < N / 2 ? k : k - N;
+          if (cl < nc) out[cl] = cadd(L.at(cl * 2, k), cmul(tw_pos(tw, u, m), L.at(cl * 2 + 1, k)));
+        }
+        __syncwarp();
+#pragma unroll
+        for (int cl = 0; cl < CPR; ++cl)
+          if (cl < nc) Z((lane + N / 2) % N, c0 + cl) = out[cl];
       }
       __syncwarp();
     }
@@ -829,13 +868,26 @@ __device__ void build_one_smem(const ProjParams& P, int dir, int slot, float2* Z
   __syncthreads();
 }
 
+// Slice gather for pass A: one block per (column, template), thread r
+// samples row r of the 2N grid and stores it at r/2 (even r) or N + r/2
+// (odd r) of the column, the order pass A reads. High occupancy hides the
+// L2 latency of the trilinear taps.
+template <int N>
+__global__ void __launch_bounds__(2 * N) gather_slices(ProjParams P, float2* __restrict__ slices) {
+  constexpr int m = 2 * N, W = N + 1;
+  const int c = blockIdx.x, b = blockIdx.y, r = threadIdx.x;
+  const float* R = P.rot + (size_t)P.dirs[b] * 9;
+  const float2 v = slice_value<N>(P.spectrum, R, r, c);
+  slices[((size_t)b * W + c) * m + ((r & 1) ? N + (r >> 1) : (r >> 1))] = v;
+}
+
 template <int N>
 __global__ void __launch_bounds__(kSmemThreads, 1) project_templates_smem(ProjParams P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int L2 = N / 16;
   float2* Zs = reinterpret_cast<float2*>(smem_raw);
   float2* stage = Zs + plane_rows(N) * plane_ld(N);
-  float2* s_tw = stage + kSmemWarps * (2 * pass_a_cols<N>()) * plane_ld(N);
+  float2* s_tw = stage + kSmemWarps * pass_a_cols<N>() * plane_ld(N);
   double* red = reinterpret_cast<double*>(s_tw + kMaxFftLen / 2);
   double* s_coef = red + 32;
   float* s_div = reinterpret_cast<float*>(s_coef + 8);
@@ -844,7 +896,7 @@ __global__ void __launch_bounds__(kSmemThreads, 1) project_templates_smem(ProjPa
   for (int b = blockIdx.x; b < P.n_build; b += gridDim.x) {
     const int dir = P.dirs[b];
     const int slot = P.out_slot ? P.out_slot[b] : dir;
-    build_one_smem<N>(P, dir, slot, Zs, stage, s_tw, s_div, red, s_coef);
+    build_one_smem<N>(P, b, slot, Zs, stage, s_tw, s_div, red, s_coef);
   }
 }
 
@@ -852,13 +904,17 @@ __global__ void __launch_bounds__(kSmemThreads, 1) project_templates_smem(ProjPa
 
 size_t project_smem_bytes_fast(int N, int n_bins) {
   const int L2 = N / 16;
-  const int cpr = N == 128 ? 1 : 16 / L2;
-  return (size_t)plane_rows(N) * plane_ld(N) * sizeof(float2) + (size_t)kSmemWarps * (2 * cpr) * plane_ld(N) * sizeof(float2) +
+  const int cpr = 16 / L2;
+  return (size_t)plane_rows(N) * plane_ld(N) * sizeof(float2) + (size_t)kSmemWarps * cpr * plane_ld(N) * sizeof(float2) +
          (kMaxFftLen / 2) * sizeof(float2) + 40 * sizeof(double) + (size_t)(n_bins + 4) * sizeof(float);
 }
 
 template <int N>
-static cudaError_t launch_fast(const ProjParams& P, int grid, cudaStream_t st) {
+static cudaError_t launch_fast(ProjParams P, int grid, float2* slices, cudaStream_t st) {
+  gather_slices<N><<<dim3(N + 1, P.n_build), 2 * N, 0, st>>>(P, slices);
+  cudaError_t e0 = cudaGetLastError();
+  if (e0 != cudaSuccess) return e0;
+  P.slices = slices;
   const size_t smem = project_smem_bytes_fast(N, P.n_bins);
   static size_t set_smem = 0;  // attribute set once per size, never inside a stream capture
   if (set_smem < smem) {
@@ -875,17 +931,19 @@ cudaError_t launch_project_templates_fast(cudaStream_t st, const float2* spectru
                                           const int* dirs, int n_build, const int* out_slot,
                                           const float* mask, const float* fsc, const int* bin_list,
                                           const int* bin_ptr, const float* bin_count, int n_bins,
-                                          const float2* tw, float2* bank, int grid, int N, int nb) {
+                                          const float2* tw, float2* bank, int grid, int N, int nb,
+                                          float2* slices) {
   if (n_build <= 0) return cudaSuccess;
+  if (n_build > 65535) return cudaErrorInvalidValue;
   ProjParams P;
   P.spectrum = spectrum; P.rot = rot; P.dirs = dirs; P.n_build = n_build; P.mask = mask;
   P.fsc = fsc; P.bin_list = bin_list; P.bin_ptr = bin_ptr; P.bin_count = bin_count;
   P.n_bins = n_bins; P.tw = tw; P.bank = bank; P.out_slot = out_slot; P.scratch = nullptr;
-  P.scratch_stride = 0; P.N = N; P.nb = nb;
+  P.scratch_stride = 0; P.N = N; P.nb = nb; P.slices = nullptr;
   switch (N) {
-    case 32: return launch_fast<32>(P, grid, st);
-    case 64: return launch_fast<64>(P, grid, st);
-    case 128: return launch_fast<128>(P, grid, st);
+    case 32: return launch_fast<32>(P, grid, slices, st);
+    case 64: return launch_fast<64>(P, grid, slices, st);
+    case 128: return launch_fast<128>(P, grid, slices, st);
     default: return cudaErrorInvalidValue;
   }
 }

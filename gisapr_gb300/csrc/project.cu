@@ -619,7 +619,8 @@ __device__ __forceinline__ void warp_fft(const Lines& L, int nlines, const float
 
 template <int N>
 __device__ void build_one_smem(const ProjParams& P, int b_index, int slot, float2* Zs, float2* stage_all,
-                               const float2* tw, float* s_div, double* red, double* s_coef) {
+                               const float2* tw, float* s_div, double* red, double* s_coef,
+                               const unsigned short* s_bins, const int* s_bptr) {
   constexpr int m = 2 * N, W = N + 1, HC = N / 2 + 1, L2 = N / 16, G = 32 / L2;
   const Plane<N> Z{Zs};
   const int nb = P.nb, H = nb / 2 + 1;
@@ -730,10 +731,10 @@ __device__ void build_one_smem(const ProjParams& P, int b_index, int slot, float
   // scatter_add_), float64 across the warp
   for (int b = warp; b < P.n_bins; b += kSmemWarps) {
     float acc = 0.f;
-    const int e1 = P.bin_ptr[b + 1];
+    const int e1 = s_bptr[b + 1];
 #pragma unroll 4
-    for (int e = P.bin_ptr[b] + lane; e < e1; e += 32) {
-      const int idx = __ldg(P.bin_list + e);
+    for (int e = s_bptr[b] + lane; e < e1; e += 32) {
+      const int idx = s_bins[e];
       const int r = idx / HC, kx = idx - r * HC;
       const float2 f = Z(r, kx);
       const float a = hypotf(f.x, f.y);
@@ -839,39 +840,42 @@ __device__ void build_one_smem(const ProjParams& P, int b_index, int slot, float
   for (int c0 = warp * G; c0 < HC; c0 += kSmemWarps * G)
     warp_fft<N, -1>(ColLines<N>{Z, c0}, min(G, HC - c0), tw);
   __syncthreads();
-  // crop + pack + FSC, L2 norm (float32 per thread, float64 across the block), pre-shifted write
+  // crop + pack + FSC, L2 norm (float32 per thread, float64 across the block),
+  // pre-shifted write; each thread keeps its packed values in registers
+  // between the norm and the write
+  constexpr int KP = (N * (N / 2 + 1) + kSmemThreads - 1) / kSmemThreads;
+  float2 fv[KP];
   float fss = 0.f;
-  for (int t = threadIdx.x; t < nb * H; t += blockDim.x) {
-    const int r = t / H, c = t - r * H;
-    const int ky = r < nb / 2 ? r : r - nb;
-    float2 f;
-    if (c < nb / 2) f = Z((ky + N) % N, c);
-    else if (nb == N) f = Z((ky + N) % N, N / 2);
-    else f = cconj(Z((-ky + N) % N, nb / 2));
-    f = cscale(f, __ldg(P.fsc + t));
-    fss = fmaf(f.x, f.x, fmaf(f.y, f.y, fss));
+#pragma unroll
+  for (int q = 0; q < KP; ++q) {
+    const int t = threadIdx.x + q * kSmemThreads;
+    fv[q] = make_float2(0.f, 0.f);
+    if (t < nb * H) {
+      const int r = t / H, c = t - r * H;
+      const int ky = r < nb / 2 ? r : r - nb;
+      float2 f;
+      if (c < nb / 2) f = Z((ky + N) % N, c);
+      else if (nb == N) f = Z((ky + N) % N, N / 2);
+      else f = cconj(Z((-ky + N) % N, nb / 2));
+      fv[q] = cscale(f, __ldg(P.fsc + t));
+      fss = fmaf(fv[q].x, fv[q].x, fmaf(fv[q].y, fv[q].y, fss));
+    }
   }
   const double ss = block_sum_d((double)fss, red);
   const float inv_norm = (float)(1.0 / sqrt(ss));
   float2* out = P.bank + (size_t)slot * nb * H;
-  for (int t = threadIdx.x; t < nb * H; t += blockDim.x) {
-    const int r = t / H, c = t - r * H;
-    const int ky = r < nb / 2 ? r : r - nb;
-    float2 f;
-    if (c < nb / 2) f = Z((ky + N) % N, c);
-    else if (nb == N) f = Z((ky + N) % N, N / 2);
-    else f = cconj(Z((-ky + N) % N, nb / 2));
-    f = cscale(f, P.fsc[t]);
-    const int rs = (r + nb / 2) % nb, cs = (c + H / 2) % H;
-    out[(size_t)rs * H + cs] = cscale(f, inv_norm);
+#pragma unroll
+  for (int q = 0; q < KP; ++q) {
+    const int t = threadIdx.x + q * kSmemThreads;
+    if (t < nb * H) {
+      const int r = t / H, c = t - r * H;
+      const int rs = (r + nb / 2) % nb, cs = (c + H / 2) % H;
+      out[(size_t)rs * H + cs] = cscale(fv[q], inv_norm);
+    }
   }
   __syncthreads();
 }
 
-// Slice gather for pass A: one block per (column, template), thread r
-// samples row r of the 2N grid and stores it at r/2 (even r) or N + r/2
-// (odd r) of the column, the order pass A reads. High occupancy hides the
-// L2 latency of the trilinear taps.
 template <int N>
 __global__ void __launch_bounds__(2 * N) gather_slices(ProjParams P, float2* __restrict__ slices) {
   constexpr int m = 2 * N, W = N + 1;
@@ -891,12 +895,16 @@ __global__ void __launch_bounds__(kSmemThreads, 1) project_templates_smem(ProjPa
   double* red = reinterpret_cast<double*>(s_tw + kMaxFftLen / 2);
   double* s_coef = red + 32;
   float* s_div = reinterpret_cast<float*>(s_coef + 8);
+  int* s_bptr = reinterpret_cast<int*>(s_div + P.n_bins + 4);              // [n_bins + 1]
+  unsigned short* s_bins = reinterpret_cast<unsigned short*>(s_bptr + P.n_bins + 1);  // [N (N/2 + 1)]
   for (int t = threadIdx.x; t < kMaxFftLen / 2; t += blockDim.x) s_tw[t] = P.tw[t];
+  for (int t = threadIdx.x; t <= P.n_bins; t += blockDim.x) s_bptr[t] = P.bin_ptr[t];
+  for (int t = threadIdx.x; t < N * (N / 2 + 1); t += blockDim.x) s_bins[t] = (unsigned short)P.bin_list[t];
   __syncthreads();
   for (int b = blockIdx.x; b < P.n_build; b += gridDim.x) {
     const int dir = P.dirs[b];
     const int slot = P.out_slot ? P.out_slot[b] : dir;
-    build_one_smem<N>(P, b, slot, Zs, stage, s_tw, s_div, red, s_coef);
+    build_one_smem<N>(P, b, slot, Zs, stage, s_tw, s_div, red, s_coef, s_bins, s_bptr);
   }
 }
 
@@ -906,7 +914,8 @@ size_t project_smem_bytes_fast(int N, int n_bins) {
   const int L2 = N / 16;
   const int cpr = 16 / L2;
   return (size_t)plane_rows(N) * plane_ld(N) * sizeof(float2) + (size_t)kSmemWarps * cpr * plane_ld(N) * sizeof(float2) +
-         (kMaxFftLen / 2) * sizeof(float2) + 40 * sizeof(double) + (size_t)(n_bins + 4) * sizeof(float);
+         (kMaxFftLen / 2) * sizeof(float2) + 40 * sizeof(double) + (size_t)(n_bins + 4) * sizeof(float) +
+         (size_t)(n_bins + 1) * sizeof(int) + (size_t)N * (N / 2 + 1) * sizeof(unsigned short);
 }
 
 template <int N>

@@ -427,7 +427,8 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
     device = torch.device("cuda", local_rank)
     torch.cuda.set_device(device)
     t_setup = time.perf_counter()
-    spec, data, models = make_workload(args.workload, args.seed + rank, str(device), args.particles,
+    from gisapr_gb300.replicas import replica_seed
+    spec, data, models = make_workload(args.workload, replica_seed(args.seed, rank), str(device), args.particles,
                                        with_models=True)
     t_data = time.perf_counter() - t_setup
     cfg = JobConfig(box=spec.box, apix=spec.apix, crop=spec.crop, psi_step=spec.psi_step,
@@ -511,26 +512,25 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
     tl = [elapsed, e2e_elapsed]
     for b in batched.values():
         tl += [b["elapsed_s"], b["e2e_elapsed_s"]]
-    times = torch.tensor(tl, dtype=torch.float64, device=device)
-    if world > 1:
-        torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
-    elapsed, e2e_elapsed = float(times[0]), float(times[1])
+    from gisapr_gb300.replicas import job_rate, max_over_ranks
+    times = max_over_ranks(tl, device=device)  # the slowest replica's times
+    elapsed, e2e_elapsed = times[0], times[1]
     for i, b in enumerate(batched.values()):
-        b["value"] = world * K * args.batch / float(times[2 + 2 * i])
+        b["value"] = job_rate(world, K * args.batch, times[2 + 2 * i])
         b["unit"] = UNIT
-        b["e2e"] = {"value": world * K * args.batch / float(times[3 + 2 * i]), "unit": UNIT,
+        b["e2e"] = {"value": job_rate(world, K * args.batch, times[3 + 2 * i]), "unit": UNIT,
                     "h2d_bytes_per_step": b.pop("e2e_h2d_bytes_per_step"),
                     "d2h_bytes_per_step": b.pop("e2e_d2h_bytes_per_step")}
         b.pop("elapsed_s")
         b.pop("e2e_elapsed_s")
-        b["vs_plain_single"] = b["value"] / (world * K / elapsed)
+        b["vs_plain_single"] = b["value"] / job_rate(world, K, elapsed)
     if "fp32" in batched:
         for b in batched.values():
             b["vs_plain_batched"] = b["value"] / batched["fp32"]["value"]
     if rank != 0:
         return
-    value = world * K / elapsed
-    e2e_value = world * K / e2e_elapsed
+    value = job_rate(world, K, elapsed)
+    e2e_value = job_rate(world, K, e2e_elapsed)
     hbm_peak, bf16_peak, peak_kind = load_peaks()
     maps = job.nnz * job.n_psi
     flops = correlation_flops(cfg.new_box, maps)

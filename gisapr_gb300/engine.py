@@ -60,9 +60,15 @@ class JobConfig:
 class ScoringJob:
     """One refinement job (model + particles) resident on one CUDA device."""
 
-    def __init__(self, cfg: JobConfig, pdb_text: str, angles: ModelAngles,
+    def __init__(self, cfg: JobConfig, pdb_text: Optional[str], angles: ModelAngles,
                  records: Sequence[ParticleRecord], images, fsc_values=None, has_ctf: bool = True,
-                 device="cuda"):
+                 device="cuda", local: Optional[Sequence[Sequence[int]]] = None,
+                 fsc_map: Optional[np.ndarray] = None):
+        """``pdb_text`` None makes a job without a model: densities are then
+        given per call (score_volume). ``local`` (one direction list per
+        record) replaces the lists built from the local range; ``fsc_map`` (the
+        centred new_box x new_box map of read_fsc_map) replaces
+        ``fsc_values``."""
         t0 = time.perf_counter()
         self.cfg = cfg
         self.device = torch.device(device)
@@ -78,30 +84,24 @@ class ScoringJob:
         new_apix = n / nb * cfg.apix
         self.trans_scale = cfg.apix / new_apix
         # local direction lists -> compact template bank + CSR
-        if cfg.do_local_search:
-            entries = build_local_orientation_entries(self.records, angles.rot, angles.tilt, cfg.local_range)
-            local = [e[1:] for e in entries]
-        else:
-            local = [list(range(len(angles.rot))) for _ in self.records]
-        self.local = local
-        needed = sorted({k for l in local for k in l})
-        self.needed = needed
-        slot = {d: i for i, d in enumerate(needed)}
-        ptr = np.zeros(len(local) + 1, dtype=np.int32)
-        ptr[1:] = np.cumsum([len(l) for l in local])
-        idx = np.asarray([slot[k] for l in local for k in l], dtype=np.int32)
-        self.local_ptr = torch.from_numpy(ptr).to(dev)
-        self.local_idx = torch.from_numpy(idx if len(idx) else np.zeros(1, np.int32)).to(dev)
-        self.nnz = int(ptr[-1])
-        self.needed_dirs = torch.tensor(needed if needed else [0], dtype=torch.int32, device=dev)
-        self.needed_slots = torch.arange(max(1, len(needed)), dtype=torch.int32, device=dev)
+        if local is None:
+            if cfg.do_local_search:
+                entries = build_local_orientation_entries(self.records, angles.rot, angles.tilt, cfg.local_range)
+                local = [e[1:] for e in entries]
+            else:
+                local = [list(range(len(angles.rot))) for _ in self.records]
+        self._set_lists(local)
         # mask and FSC
         mask_radius = cfg.mask_radius if cfg.mask_radius is not None else int(round(0.43 * n))
         mask_np = generate_soft_mask((n, n), mask_radius, cfg.mask_edge)
         self.mask = None if cfg.discard_mask else torch.from_numpy(mask_np).to(dev)
-        fsc = np.ones(n, np.float32) if fsc_values is None else np.asarray(fsc_values, np.float32)
-        self.packed_fsc = torch.from_numpy(np.ascontiguousarray(
-            centered_to_packed_np(expand_radial_values(fsc, nb)))).to(dev)
+        if fsc_map is None:
+            fsc = np.ones(n, np.float32) if fsc_values is None else np.asarray(fsc_values, np.float32)
+            fsc_map = expand_radial_values(fsc, nb)
+        fsc_map = np.asarray(fsc_map, dtype=np.float32)
+        if fsc_map.shape != (nb, nb):
+            raise ValueError(f"FSC map must be {nb}x{nb}, got {fsc_map.shape}")
+        self.packed_fsc = torch.from_numpy(np.ascontiguousarray(centered_to_packed_np(fsc_map))).to(dev)
         # psi sampling
         self.psi_meta = [psi_sampling_for_record(r.psi, cfg.psi_step, cfg.do_local_search, cfg.local_range)
                          for r in self.records]
@@ -119,14 +119,11 @@ class ScoringJob:
         self.stack = preparer.prepare_batch(imgs, torch.from_numpy(psi_index), ctf)
         del imgs, ctf
         # model
-        self.density = MovedChainDensity(pdb_text, cfg.chain_id, n, cfg.apix, cfg.resolution, dev,
-                                         include_hetatm=cfg.include_hetatm, from_text=True)
+        self.density = None if pdb_text is None else MovedChainDensity(
+            pdb_text, cfg.chain_id, n, cfg.apix, cfg.resolution, dev, include_hetatm=cfg.include_hetatm,
+            from_text=True)
         self.projector = IntegratedProjector(dev, n, nb, self.layout, self.mask, self.packed_fsc)
-        self.bank = torch.empty((max(1, len(needed)), nb, nb // 2 + 1), dtype=torch.complex64, device=dev)
-        m = max(1, self.nnz) * self.n_psi
-        self.score_buf = torch.empty(m, dtype=torch.float32, device=dev)
-        self.y_buf = torch.empty(m, dtype=torch.int32, device=dev)
-        self.x_buf = torch.empty(m, dtype=torch.int32, device=dev)
+        self._alloc_search_buffers()
         np_ = len(self.records)
         self.best_entry = torch.empty(np_, dtype=torch.int32, device=dev)
         self.best_psi = torch.empty(np_, dtype=torch.int32, device=dev)
@@ -141,6 +138,43 @@ class ScoringJob:
         torch.cuda.synchronize(dev)
         self.setup_s = time.perf_counter() - t0
 
+    def _set_lists(self, local: Sequence[Sequence[int]]) -> None:
+        """Direction lists (one per record) -> needed directions and CSR arrays."""
+        if len(local) != len(self.records):
+            raise ValueError("local needs one direction list per particle record")
+        n_dirs = len(self.angles.rot)
+        local = [[int(k) for k in l] for l in local]
+        if any(k < 0 or k >= n_dirs for l in local for k in l):
+            raise ValueError("a local direction index is outside the angle table")
+        dev = self.device
+        self.local = local
+        needed = sorted({k for l in local for k in l})
+        self.needed = needed
+        slot = {d: i for i, d in enumerate(needed)}
+        ptr = np.zeros(len(local) + 1, dtype=np.int32)
+        ptr[1:] = np.cumsum([len(l) for l in local])
+        idx = np.asarray([slot[k] for l in local for k in l], dtype=np.int32)
+        self.local_ptr = torch.from_numpy(ptr).to(dev)
+        self.local_idx = torch.from_numpy(idx if len(idx) else np.zeros(1, np.int32)).to(dev)
+        self.nnz = int(ptr[-1])
+        self.needed_dirs = torch.tensor(needed if needed else [0], dtype=torch.int32, device=dev)
+        self.needed_slots = torch.arange(max(1, len(needed)), dtype=torch.int32, device=dev)
+
+    def _alloc_search_buffers(self) -> None:
+        nb, dev = self.cfg.new_box, self.device
+        self.bank = torch.empty((max(1, len(self.needed)), nb, nb // 2 + 1), dtype=torch.complex64, device=dev)
+        m = max(1, self.nnz) * self.n_psi
+        self.score_buf = torch.empty(m, dtype=torch.float32, device=dev)
+        self.y_buf = torch.empty(m, dtype=torch.int32, device=dev)
+        self.x_buf = torch.empty(m, dtype=torch.int32, device=dev)
+
+    def set_local(self, local: Sequence[Sequence[int]]) -> None:
+        """Replace the per-particle direction lists; the prepared particle
+        spectra stay resident. Batches built on this job before the call
+        must be rebuilt."""
+        self._set_lists(local)
+        self._alloc_search_buffers()
+
     # ------------------------------------------------------------------
     # launches of this engine per scored candidate (cuFFT's own kernels not counted)
     KERNELS_PER_CANDIDATE = 6
@@ -152,10 +186,24 @@ class ScoringJob:
         [rot(9), shift(3)] float64 on the device. The score lands in
         self.total. ``stage_events`` (stage -> list) collects a pair of CUDA
         events around each stage when given."""
-        dev = self.device
-        ctx = nat.Context.for_device(dev).handle
-        st = nat.stream_of(dev)
+        if self.density is None:
+            raise ValueError("this job has no model; score densities with score_volume")
+        mark = self._marker(stage_events)
+        mark("density", False)
+        self.density.generate(None, out=write_volume, write_padded=True, pose_device=pose_device)
+        mark("density", True)
+        self._enqueue_search(None, mark)
 
+    def enqueue_volume(self, volume: torch.Tensor, stage_events: Optional[Dict[str, list]] = None) -> None:
+        """Enqueue the search of one given density ([box]^3 float32 on the
+        job's device) on the current stream; the score lands in self.total."""
+        n = int(self.cfg.box)
+        if volume.shape != (n, n, n) or volume.dtype != torch.float32 or volume.device != self.device:
+            raise ValueError(f"density must be a float32 [{n}]^3 tensor on {self.device}")
+        self._enqueue_search(volume.contiguous(), self._marker(stage_events))
+
+    @staticmethod
+    def _marker(stage_events):
         def mark(stage, end):
             if stage_events is None:
                 return
@@ -165,12 +213,15 @@ class ScoringJob:
                 stage_events[stage][-1].append(ev)
             else:
                 stage_events.setdefault(stage, []).append([ev])
+        return mark
 
-        mark("density", False)
-        self.density.generate(None, out=write_volume, write_padded=True, pose_device=pose_device)
-        mark("density", True)
+    def _enqueue_search(self, volume: Optional[torch.Tensor], mark) -> None:
+        """Volume spectrum (of ``volume``, or of the padded input the splat
+        wrote), templates, correlation, per-particle records and score sum."""
+        ctx = nat.Context.for_device(self.device).handle
+        st = nat.stream_of(self.device)
         mark("volume_fft", False)
-        self.projector.volume_spectrum(None)
+        self.projector.volume_spectrum(volume)
         mark("volume_fft", True)
         mark("templates", False)
         if self.needed:
@@ -202,6 +253,16 @@ class ScoringJob:
     def score_many(self, poses) -> np.ndarray:
         return np.asarray([self.score(p) for p in poses], dtype=np.float64)
 
+    def score_volume(self, volume) -> float:
+        """sum_i exp(rawCC_i / 1024) of one given density (array or tensor, [box]^3)."""
+        if not torch.is_tensor(volume):
+            volume = torch.from_numpy(np.ascontiguousarray(volume, dtype=np.float32))
+        volume = volume.to(self.device, torch.float32)
+        self.enqueue_volume(volume)
+        self.total_host.copy_(self.total, non_blocking=True)
+        torch.cuda.current_stream(self.device).synchronize()
+        return float(self.total_host[0])
+
     # ------------------------------------------------------------------
     def particle_results(self) -> Dict[str, np.ndarray]:
         """Per-particle arrays of the last scored pose."""
@@ -212,7 +273,11 @@ class ScoringJob:
     def result_records(self) -> List[List[object]]:
         """The search text records of the last scored pose, in particle order
         (v606:1494-1516), skipping particles without directions."""
-        r = self.particle_results()
+        return self.format_results(self.particle_results())
+
+    def format_results(self, r: Dict[str, np.ndarray]) -> List[List[object]]:
+        """Text records from per-particle arrays (best_entry, best_psi, peak,
+        peak_y, peak_x, zscore), in particle order."""
         rows = []
         ptr = self.local_ptr.cpu().numpy()
         for i, rec in enumerate(self.records):
@@ -263,6 +328,8 @@ class BatchScoringJob:
         self.tc_chunk = int(tc_chunk)
         self.job = job
         self.n_cand = int(n_cand)
+        if not models and job.density is None:
+            raise ValueError("a job without a model needs the batch's models")
         self.models = list(models) if models else [job.density]
         self.model_of = list(model_of) if model_of is not None else [i % len(self.models) for i in range(self.n_cand)]
         if len(self.model_of) != self.n_cand:
@@ -459,6 +526,19 @@ class BatchScoringJob:
         st.synchronize()
         self.check_status()
         return self.totals_host[:k].numpy().copy()
+
+    def slot_results(self, n_slots: Optional[int] = None) -> List[Dict[str, np.ndarray]]:
+        """Per-particle arrays of each of the first n_slots slots of the last batch."""
+        k = self.n_cand if n_slots is None else int(n_slots)
+        cols = dict(best_entry=self.best_entry, best_psi=self.best_psi, peak=self.peak, peak_y=self.peak_y,
+                    peak_x=self.peak_x, zscore=self.zscore)
+        host = {name: t[:k].cpu().numpy() for name, t in cols.items()}
+        return [{name: a[c] for name, a in host.items()} for c in range(k)]
+
+    def search_texts(self, n_slots: Optional[int] = None) -> List[str]:
+        """The search text of each of the first n_slots slots of the last batch."""
+        return ["".join(str(row) + "\n" for row in self.job.format_results(r))
+                for r in self.slot_results(n_slots)]
 
     def score_batch(self, poses) -> np.ndarray:
         """Scores of len(poses) == n_cand poses, in slot order."""

@@ -46,3 +46,74 @@ def argmax_agrees(scores_a, scores_b, idx_a, idx_b, tie_rel=TIE_REL) -> bool:
         return True
     va, vb = float(scores_b[idx_a]), float(scores_b[idx_b])
     return abs(va - vb) <= tie_rel * max(abs(vb), 1e-30)
+
+
+# ---------------------------------------------------------------------------
+# Input files of the file-based search (angle STAR, particle STAR + stack,
+# FSC text, model MRC), written from fixture arrays.
+# ---------------------------------------------------------------------------
+
+
+def write_angle_star(path, rot, tilt) -> None:
+    with open(path, "w") as f:
+        f.write("\ndata_\n\nloop_\n_rlnAngleRot #1\n_rlnAngleTilt #2\n_rlnAnglePsi #3\n")
+        for r, t in zip(rot, tilt):
+            f.write(f"{float(r)!r}\t{float(t)!r}\t0.0\n")
+
+
+def write_particle_star(path, stack_name, line, rot, tilt, psi, dfu, dfv, dfa) -> None:
+    """One row per particle, placed at its STAR line index (blank lines pad)."""
+    header = ("\ndata_\n\nloop_\n_rlnImageName #1\n_rlnAngleRot #2\n_rlnAngleTilt #3\n"
+              "_rlnAnglePsi #4\n_rlnDefocusU #5\n_rlnDefocusV #6\n_rlnDefocusAngle #7\n")
+    with open(path, "w") as f:
+        f.write(header)
+        n = header.count("\n")
+        if int(line[0]) < n:
+            raise ValueError("first particle line index falls inside the header")
+        for i in range(len(rot)):
+            while n < int(line[i]):
+                f.write("\n")
+                n += 1
+            vals = [float(v[i]) for v in (rot, tilt, psi, dfu, dfv, dfa)]
+            f.write(f"{i + 1:06d}@{stack_name}\t" + "\t".join(repr(v) for v in vals) + "\n")
+            n += 1
+
+
+def write_search_inputs(tmp, g, volume=None, extra=()):
+    """Files of the box-32 fixture's search under ``tmp`` and the parsed
+    search arguments (local search with the fixture's settings)."""
+    from pathlib import Path
+    from gisapr_gb300.mrc import write_mrc
+    from gisapr_gb300.standalone import create_search_parser
+    tmp = Path(tmp)
+    spec = syn.WORKLOADS[str(g["spec_name"])]
+    write_angle_star(tmp / "angles.star", g["model_rot"], g["model_tilt"])
+    write_mrc(tmp / "stack.mrcs", np.asarray(g["images"], dtype=np.float32), spec.apix)
+    write_particle_star(tmp / "particles.star", str(tmp / "stack.mrcs"), g["rec_line"], g["rec_rot"],
+                        g["rec_tilt"], g["rec_psi"], g["rec_dfu"], g["rec_dfv"], g["rec_dfa"])
+    with open(tmp / "fsc.txt", "w") as f:
+        for k, v in enumerate(np.asarray(g["fsc"], dtype=np.float64)):
+            f.write(f"{k} {float(v)!r}\n")
+    write_mrc(tmp / "model.mrc", np.asarray(g["density"] if volume is None else volume, np.float32), spec.apix)
+    (tmp / "model.pdb").write_text(str(g["pdb_text"]))
+    argv = ["--i", "unused", "--p", str(tmp / "particles.star"), "--FSC", str(tmp / "fsc.txt"),
+            "--o", str(tmp / "search.txt"), "--kk", repr(spec.kk), "--oriboxsize", str(spec.box),
+            "--newboxsize", str(spec.new_box), "--apix", repr(spec.apix), "--maskRadius", str(spec.mask_radius),
+            "--maskEdge", str(spec.mask_edge), "--psiStep", repr(spec.psi_step), "--doLocalSearch",
+            "--localRange", repr(spec.local_range), "--ang", str(tmp / "angles.star"),
+            "--mrc", str(tmp / "model.mrc"), "--ccgCropSize", str(spec.crop), *extra]
+    return create_search_parser().parse_args(argv)
+
+
+def parse_search_text(path_or_text):
+    """Records of a search text: a list of (cc, psi, raw) record triples."""
+    import ast
+    import os
+    text = path_or_text
+    if os.path.exists(str(path_or_text)):
+        with open(path_or_text) as f:
+            text = f.read()
+    rows = [ast.literal_eval(line) for line in text.splitlines() if line.strip()]
+    if len(rows) % 3:
+        raise ValueError("a search text holds three records per particle")
+    return [tuple(rows[i:i + 3]) for i in range(0, len(rows), 3)]

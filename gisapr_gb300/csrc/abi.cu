@@ -55,6 +55,11 @@ cudaError_t launch_correlate_plain(cudaStream_t, const float2*, const float2*, c
 cudaError_t launch_particle_results(cudaStream_t, const int*, const float*, const int*, const int*,
                                     int, int, int*, int*, float*, int*, int*, float*, int);
 cudaError_t launch_score_sum(cudaStream_t, const int*, const float*, int, double*, int);
+size_t edt_smem_bytes(int box);
+cudaError_t launch_restraint_edt(cudaStream_t, const float*, float, unsigned char*, int*, int*, int);
+cudaError_t launch_restraint_init(cudaStream_t, int*, int);
+cudaError_t launch_restraint_reduce(cudaStream_t, float*, const unsigned char*, const int*, int, const int*,
+                                    const int*, float, int*, int);
 int correlate_tc_max_psi();
 int correlate_tc_max_n();
 size_t correlate_tc_smem_bytes(int n, int crop);
@@ -668,6 +673,42 @@ int gisapr_score_sum_batch(void* stream, const int* local_ptr, const float* peak
 
 int gisapr_score_sum(void* stream, const int* local_ptr, const float* peak, int n_particles, double* out) {
   return gisapr_score_sum_batch(stream, local_ptr, peak, n_particles, 1, out);
+}
+
+int gisapr_restraint_edt(gisapr_ctx ctx, void* stream, const float* density, int box, float threshold,
+                         unsigned char* mask, int* d2, int* scratch) {
+  if (!ctx) return fail(GISAPR_ERR_ARGUMENT, "context is NULL");
+  if (!density || !mask || !d2 || !scratch) return fail(GISAPR_ERR_ARGUMENT, "a required pointer is NULL");
+  if (box < 1 || box > 1024) return fail(GISAPR_ERR_ARGUMENT, "box must be in [1, 1024]");
+  if (!std::isfinite(threshold)) return fail(GISAPR_ERR_ARGUMENT, "threshold must be finite");
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  GISAPR_CHECK_CUDA(launch_restraint_edt((cudaStream_t)stream, density, threshold, mask, d2, scratch, box),
+                    "restraint_edt");
+  return GISAPR_OK;
+}
+
+int gisapr_restraint_init(void* stream, int* out, int n) {
+  if (n < 0 || (n > 0 && !out)) return fail(GISAPR_ERR_ARGUMENT, "bad arguments");
+  if (n == 0) return GISAPR_OK;
+  GISAPR_CHECK_CUDA(launch_restraint_init((cudaStream_t)stream, out, n), "restraint_init");
+  return GISAPR_OK;
+}
+
+int gisapr_restraint_eval(gisapr_ctx ctx, void* stream, float* volume, const unsigned char* mask, const int* d2,
+                          int box, const int* bounds, float threshold, int* out) {
+  if (!ctx) return fail(GISAPR_ERR_ARGUMENT, "context is NULL");
+  if (!volume || !mask || !d2 || !bounds || !out) return fail(GISAPR_ERR_ARGUMENT, "a required pointer is NULL");
+  if (box < 1 || box > 1024) return fail(GISAPR_ERR_ARGUMENT, "box must be in [1, 1024]");
+  for (int a = 0; a < 3; ++a)
+    if (bounds[a] < 0 || bounds[3 + a] > box || bounds[a] > bounds[3 + a])
+      return fail(GISAPR_ERR_ARGUMENT, "bounds must satisfy 0 <= lo <= hi <= box on every axis");
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  GISAPR_CHECK_CUDA(launch_restraint_reduce((cudaStream_t)stream, volume, mask, d2, box, bounds, bounds + 3,
+                                            threshold, out, ctx->sm_count),
+                    "restraint_reduce");
+  return GISAPR_OK;
 }
 
 }  // extern "C"

@@ -243,6 +243,32 @@ int gisapr_score_sum(void* stream, const int* local_ptr, const float* peak, int 
 int gisapr_score_sum_batch(void* stream, const int* local_ptr, const float* peak, int n_particles, int n_cand,
                            double* out);
 
+/*
+ * Geometric restraint (func_check_boundary_for_testing_v8.py:62-126,
+ * GeometryRestraint). gisapr_restraint_edt thresholds the main-body density
+ * [box]^3 (voxel > threshold) into mask (u8) and writes d2: per voxel the
+ * exact squared Euclidean distance, in voxels, to the nearest mask voxel
+ * (scipy distance_transform_edt(~mask) squared; 2^29 where the mask is
+ * empty). scratch: box^3 ints. Replaces GeometryRestraint.__init__'s mask
+ * and distance transform (v8:83-94).
+ */
+int gisapr_restraint_edt(gisapr_ctx ctx, void* stream, const float* density, int box, float threshold,
+                         unsigned char* mask, int* d2, int* scratch);
+
+/* out[3 * i + 0..2] = {0, INT_MAX, 0} for i < n (the reduction identities). */
+int gisapr_restraint_init(void* stream, int* out, int n);
+
+/*
+ * One candidate (v8:96-126): over the half-open voxel box bounds = {z0, y0,
+ * x0, z1, y1, x1} (host memory) of the chain density in volume (the moved chain splatted
+ * with gisapr_deposit onto zeros), adds to out[0] the voxels above threshold
+ * where mask is set (overlap), lowers out[1] to the minimum d2 of voxels
+ * above threshold and sets out[2] if there is any. Every voxel read is reset
+ * to zero, so volume is all-zero again when the chain lay inside bounds.
+ */
+int gisapr_restraint_eval(gisapr_ctx ctx, void* stream, float* volume, const unsigned char* mask, const int* d2,
+                          int box, const int* bounds, float threshold, int* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -42,6 +42,7 @@ SIGNATURES = {
     "gisapr_correlate_tc_batch": [_p, _p, _p, C.c_longlong, _i, _i, _p, _p, _p, _p, _p, _i, _i, _i, _i, _i, _i,
                                   _p, _p, _p, _p],
     "gisapr_restraint_edt": [_p, _p, _p, _i, _f, _p, _p, _p],
+    "gisapr_ingest_stack": [_p, _p, _p, _i, _i, _i, _p, _i, _i, _i, _p, _p, _p, _i, _p, _p, _p],
     "gisapr_restraint_init": [_p, _p, _i],
     "gisapr_restraint_eval": [_p, _p, _p, _p, _p, _i, _p, _f, _p],
 }

@@ -60,6 +60,12 @@ cudaError_t launch_restraint_edt(cudaStream_t, const float*, float, unsigned cha
 cudaError_t launch_restraint_init(cudaStream_t, int*, int);
 cudaError_t launch_restraint_reduce(cudaStream_t, float*, const unsigned char*, const int*, int, const int*,
                                     const int*, float, int*, int);
+cudaError_t launch_ingest_load(cudaStream_t, const float*, int, int, int, const int*, int, int, double2*, int);
+cudaError_t launch_ingest_spectrum_divide(cudaStream_t, double2*, int, int, const int*, const int*, const double*,
+                                          int);
+cudaError_t launch_ingest_normalize(cudaStream_t, double2*, int, int, int, double);
+cudaError_t launch_ingest_scale_mask(cudaStream_t, double2*, int, int, const double*, double, int, int);
+cudaError_t launch_ingest_store(cudaStream_t, const double2*, int, int, double, float*, int);
 int correlate_tc_max_psi();
 int correlate_tc_max_n();
 size_t correlate_tc_smem_bytes(int n, int crop);
@@ -673,6 +679,73 @@ int gisapr_score_sum_batch(void* stream, const int* local_ptr, const float* peak
 
 int gisapr_score_sum(void* stream, const int* local_ptr, const float* peak, int n_particles, double* out) {
   return gisapr_score_sum_batch(stream, local_ptr, peak, n_particles, 1, out);
+}
+
+int gisapr_ingest_stack(gisapr_ctx ctx, void* stream, const float* images, int n, int h, int w, const int* shifts,
+                        int ch, int cw, int flags, const int* bin_ptr, const int* bin_pix, const double* bin_count,
+                        int n_bins, const double* highpass_mask, double* work, float* out) {
+  if (!ctx) return fail(GISAPR_ERR_ARGUMENT, "context is NULL");
+  if (n < 0 || h < 1 || w < 1) return fail(GISAPR_ERR_ARGUMENT, "n < 0 or an image side < 1");
+  if (ch < 1 || cw < 1 || ch > h || cw > w)
+    return fail(GISAPR_ERR_ARGUMENT, "the crop must be at least 1 and at most the image size on both axes");
+  if (flags & ~7) return fail(GISAPR_ERR_ARGUMENT, "unknown flag bits");
+  if ((flags & 1) && (!bin_ptr || !bin_pix || !bin_count || n_bins < 1 || n_bins > 8192))
+    return fail(GISAPR_ERR_ARGUMENT, "whitening needs the radial bin tables (1..8192 bins)");
+  if ((flags & 4) && !highpass_mask) return fail(GISAPR_ERR_ARGUMENT, "the high-pass mask is NULL");
+  if (n == 0) return GISAPR_OK;
+  if (!images || !work || !out) return fail(GISAPR_ERR_ARGUMENT, "a required pointer is NULL");
+  if ((long long)ch * cw > (1LL << 26)) return fail(GISAPR_ERR_ARGUMENT, "crop too large");
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int pixels = ch * cw;
+  double2* wk = (double2*)work;
+  GISAPR_CHECK_CUDA(launch_ingest_load(st, images, n, h, w, shifts, ch, cw, wk, ctx->sm_count), "ingest_load");
+  cufftHandle plan = 0;
+  if (flags & 5) {
+    int dims[2] = {ch, cw};
+    cufftResult r = cufftPlanMany(&plan, 2, dims, nullptr, 1, 0, nullptr, 1, 0, CUFFT_Z2Z, n);
+    if (r != CUFFT_SUCCESS) return fail(GISAPR_ERR_CUFFT, "cufftPlanMany(Z2Z) failed with code " + std::to_string((int)r));
+    cufftSetStream(plan, st);
+  }
+  auto run = [&]() -> int {
+    const double inv = 1.0 / (double)pixels;
+    double scale = 1.0;  // pending factor of the values in work
+    if (flags & 1) {
+      cufftResult r = cufftExecZ2Z(plan, (cufftDoubleComplex*)wk, (cufftDoubleComplex*)wk, CUFFT_FORWARD);
+      if (r != CUFFT_SUCCESS) return fail(GISAPR_ERR_CUFFT, "cufftExecZ2Z failed");
+      GISAPR_CHECK_CUDA(launch_ingest_spectrum_divide(st, wk, n, pixels, bin_ptr, bin_pix, bin_count, n_bins),
+                        "ingest_spectrum_divide");
+      r = cufftExecZ2Z(plan, (cufftDoubleComplex*)wk, (cufftDoubleComplex*)wk, CUFFT_INVERSE);
+      if (r != CUFFT_SUCCESS) return fail(GISAPR_ERR_CUFFT, "cufftExecZ2Z failed");
+      scale = inv;
+    }
+    if (flags & 2) {
+      GISAPR_CHECK_CUDA(launch_ingest_normalize(st, wk, n, ch, cw, scale), "ingest_normalize");
+      scale = 1.0;
+    }
+    if (flags & 4) {
+      if (scale != 1.0)  // the real image of the preceding inverse transform
+        GISAPR_CHECK_CUDA(launch_ingest_scale_mask(st, wk, n, pixels, nullptr, scale, 1, ctx->sm_count),
+                          "ingest_scale");
+      cufftResult r = cufftExecZ2Z(plan, (cufftDoubleComplex*)wk, (cufftDoubleComplex*)wk, CUFFT_FORWARD);
+      if (r != CUFFT_SUCCESS) return fail(GISAPR_ERR_CUFFT, "cufftExecZ2Z failed");
+      GISAPR_CHECK_CUDA(launch_ingest_scale_mask(st, wk, n, pixels, highpass_mask, 1.0, 0, ctx->sm_count),
+                        "ingest_mask");
+      r = cufftExecZ2Z(plan, (cufftDoubleComplex*)wk, (cufftDoubleComplex*)wk, CUFFT_INVERSE);
+      if (r != CUFFT_SUCCESS) return fail(GISAPR_ERR_CUFFT, "cufftExecZ2Z failed");
+      scale = inv;
+    }
+    GISAPR_CHECK_CUDA(launch_ingest_store(st, wk, n, pixels, scale, out, ctx->sm_count), "ingest_store");
+    return GISAPR_OK;
+  };
+  rc = run();
+  if (plan) {
+    // the plan's work area may be in use until the stream reaches this point
+    cudaStreamSynchronize(st);
+    cufftDestroy(plan);
+  }
+  return rc;
 }
 
 int gisapr_restraint_edt(gisapr_ctx ctx, void* stream, const float* density, int box, float threshold,

@@ -244,6 +244,24 @@ int gisapr_score_sum_batch(void* stream, const int* local_ptr, const float* peak
                            double* out);
 
 /*
+ * Particle stack preparation (read_star_shift_crop_and_generate_new_star_v5.py:
+ * 9-29, 42-134, 183-237), in float64. images: n float32 [h][w] images;
+ * shifts: per image the integer shift {x, y} (the reference rounds
+ * rlnOrigin/apix with floor(v + 0.5)), or NULL for none; the shifted image
+ * (zero fill) is cropped to the centred ch x cw window, then flags select:
+ * 1 = divide by the radial mean amplitude spectrum (getSpectrum_divideBy
+ * Spectrum; bin tables: CSR bin_ptr[n_bins + 1] / bin_pix of row-major pixel
+ * indices of the unshifted transform grid per bin round(centred radius),
+ * bin_count = pixels per bin), 2 = least-squares plane removal and mean/sigma
+ * normalisation (normalize), 4 = high-pass by highpass_mask (ch*cw doubles,
+ * unshifted order). work: n*ch*cw*2 doubles; out: n float32 ch x cw images.
+ * Every pointer but shifts is device memory.
+ */
+int gisapr_ingest_stack(gisapr_ctx ctx, void* stream, const float* images, int n, int h, int w, const int* shifts,
+                        int ch, int cw, int flags, const int* bin_ptr, const int* bin_pix, const double* bin_count,
+                        int n_bins, const double* highpass_mask, double* work, float* out);
+
+/*
  * Geometric restraint (func_check_boundary_for_testing_v8.py:62-126,
  * GeometryRestraint). gisapr_restraint_edt thresholds the main-body density
  * [box]^3 (voxel > threshold) into mask (u8) and writes d2: per voxel the

@@ -526,19 +526,26 @@ __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
               const float2* pp = sp + s * n + r0;
               // rows of psi s: per crop-row pair (Re y, Re y+1, Im y, Im y+1)
               const int jr = s * kPS + 4 * (yi >> 1) + (yi & 1), ji = jr + 2;
+              // the eight products of the step, once for both parts
+              float ur[8], ui[8];
+              {
+                float2 tw = tw0;
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                  const float2 u = cmul(pp[i], tw);
+                  ur[i] = u.x;
+                  ui[i] = u.y;
+                  tw = cmul(tw, step);
+                }
+              }
 #pragma unroll
               for (int part = 0; part < 2; ++part) {
                 // part 0: Re U -> Re-Z row first half, Im-Z row second half;
                 // part 1: Im U -> Im-Z row first half, -Im U in the Re-Z row second half
-                float2 tw = tw0;
                 uint32_t hw[4], lw[4];
 #pragma unroll
                 for (int i = 0; i < 4; ++i) {
-                  const float2 u0 = cmul(pp[2 * i], tw);
-                  tw = cmul(tw, step);
-                  const float2 u1 = cmul(pp[2 * i + 1], tw);
-                  tw = cmul(tw, step);
-                  const float a = part ? u0.y : u0.x, b = part ? u1.y : u1.x;
+                  const float a = part ? ui[2 * i] : ur[2 * i], b = part ? ui[2 * i + 1] : ur[2 * i + 1];
                   const __half2 hv = __floats2half2_rn(a, b);
                   const float2 hf = __half22float2(hv);
                   const __half2 lv = __floats2half2_rn(a - hf.x, b - hf.y);

@@ -35,7 +35,7 @@ cudaError_t launch_project_templates(cudaStream_t, const float2*, const float*, 
                                      const int*, const float*, const float*, const int*, const int*,
                                      const float*, int, const float2*, float2*, float2*, int, int,
                                      int);
-size_t project_smem_bytes_fast(int N, int n_bins);
+size_t project_smem_bytes_fast(int N, int n_bins, int nb);
 cudaError_t launch_project_templates_fast(cudaStream_t, const float2*, const float*, const int*, int,
                                           const int*, const float*, const float*, const int*, const int*,
                                           const float*, int, const float2*, float2*, int, int, int, float2*);
@@ -434,7 +434,7 @@ int gisapr_project_templates(gisapr_ctx ctx, void* stream, const float* spectrum
     // whole template in shared memory, one CTA per SM
     const int grid = grid_for(ctx, n_build, 1);
     if (n_build > 65535) return fail(GISAPR_ERR_ARGUMENT, "at most 65535 templates per call");
-    rc = ensure(ctx->proj_slices, project_slice_elems(box, n_build) * sizeof(float2), "cudaMalloc(slices)");
+    rc = ensure(ctx->proj_slices, project_slice_elems(box, n_build) * sizeof(float2), "cudaMalloc(planes)");
     if (rc) return rc;
     GISAPR_CHECK_CUDA(launch_project_templates_fast((cudaStream_t)stream, (const float2*)spectrum, rot, dirs,
                                                     n_build, out_slot, mask, fsc, bt.list, bt.ptr, bt.count,

@@ -48,7 +48,7 @@ struct ProjParams {
   const int* out_slot;      // output row in bank for each build index (null => dirs[i])
   float2* scratch;          // per-CTA scratch
   size_t scratch_stride;    // complex elements per CTA
-  const float2* slices;     // [n_build][N+1][2N] gathered slices, even rows then odd rows (or null)
+  const float2* planes;     // [n_build][N][plane_ld(N)] pass-A planes of the shared-memory path (or null)
   int N;
   int nb;
 };
@@ -405,8 +405,11 @@ __global__ void __launch_bounds__(kThreads) project_templates(ProjParams P) {
 
 }  // namespace
 
-// complex elements of the gathered slices of n_build templates (fast path)
-size_t project_slice_elems(int N, int n_build) { return (size_t)n_build * (N + 1) * 2 * N; }
+// complex elements of the pass-A planes of n_build templates (shared-memory
+// path, N <= 128): N rows of plane_ld(N) each
+size_t project_slice_elems(int N, int n_build) {
+  return (size_t)n_build * N * (N == 128 ? 150 : (N == 64 ? 74 : 38));
+}
 
 size_t project_scratch_elems(int N, int nb) {
   return (size_t)N * (N + 1) + (size_t)nb * (nb / 2 + 1);
@@ -429,7 +432,7 @@ cudaError_t launch_project_templates(cudaStream_t st, const float2* spectrum, co
   ProjParams P;
   P.spectrum = spectrum; P.rot = rot; P.dirs = dirs; P.n_build = n_build; P.mask = mask;
   P.fsc = fsc; P.bin_list = bin_list; P.bin_ptr = bin_ptr; P.bin_count = bin_count;
-  P.n_bins = n_bins; P.tw = tw; P.bank = bank; P.out_slot = out_slot; P.scratch = scratch; P.slices = nullptr;
+  P.n_bins = n_bins; P.tw = tw; P.bank = bank; P.out_slot = out_slot; P.scratch = scratch; P.planes = nullptr;
   P.scratch_stride = project_scratch_elems(N, nb); P.N = N; P.nb = nb;
   const size_t smem = project_smem_bytes(N, n_bins);
   static size_t set_smem = 0;
@@ -564,15 +567,6 @@ __device__ __forceinline__ float2 slice_value(const float2* __restrict__ spectru
   return v;
 }
 
-// Lines of pass A: line 2q is plane column c0 + q, line 2q + 1 staging line q.
-template <int N>
-struct PassALines {
-  Plane<N> pl; int c0; float2* st;
-  __device__ __forceinline__ float2& at(int g, int k) const {
-    return (g & 1) ? st[(g >> 1) * plane_ld(N) + k + (k >> 3)] : pl(k, c0 + (g >> 1));
-  }
-};
-
 // In-place four-step FFT of ``nlines`` (<= 32 / (N/16)) lines, natural order
 // in and out: a 16-point register codelet over n1, twiddles, then N/16-point
 // codelets over n2 (N = 16 * (N/16)). One warp, warp barriers only.
@@ -617,65 +611,103 @@ __device__ __forceinline__ void warp_fft(const Lines& L, int nlines, const float
   __syncwarp();
 }
 
+// Lines of the paired row passes: line q is plane row r0 + 2q, which holds
+// z = a + i b for the real rows a = r0 + 2q and b = r0 + 2q + 1.
 template <int N>
-__device__ void build_one_smem(const ProjParams& P, int b_index, int slot, float2* Zs, float2* stage_all,
-                               const float2* tw, float* s_div, double* red, double* s_coef,
-                               const unsigned short* s_bins, const int* s_bptr) {
-  constexpr int m = 2 * N, W = N + 1, HC = N / 2 + 1, L2 = N / 16, G = 32 / L2;
+struct PairLines {
+  Plane<N> pl; int r0;
+  __device__ __forceinline__ float2& at(int g, int k) const { return pl(r0 + 2 * g, k); }
+};
+
+// After a forward FFT of the paired lines of rows r0 .. r0 + 2G - 1, split
+// each line into the half spectra of its two real rows (k in [0, N/2]):
+// A(k) = (Z(k) + conj Z(N-k)) / 2 into the first row, B(k) = (Z(k) -
+// conj Z(N-k)) / 2i into the second. A task (q, k) reads positions k and
+// N-k of its line and writes position k of both rows; no other task reads
+// those, so the split runs in place without a barrier.
+template <int N>
+__device__ __forceinline__ void pair_split(const Plane<N>& Z, int r0, int lane) {
+  constexpr int HC = N / 2 + 1, G = 32 / (N / 16);
+  for (int idx = lane; idx < G * HC; idx += 32) {
+    const int q = idx / HC, k = idx - q * HC;
+    const int i1 = r0 + 2 * q;
+    const float2 zk = Z(i1, k), zn = Z(i1, (N - k) & (N - 1));
+    Z(i1, k) = make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
+    Z(i1 + 1, k) = make_float2(0.5f * (zk.y + zn.y), 0.5f * (zn.x - zk.x));
+  }
+}
+
+// Deterministic float32 block sums (xor tree inside each warp, warps added
+// in index order). ``scratch`` holds kSmemWarps entries; two uses of the
+// same scratch must be separated by a block barrier.
+__device__ __forceinline__ float4 block_sum_f4(float4 v, float4* scratch) {
+  v.x = warp_sum(v.x); v.y = warp_sum(v.y); v.z = warp_sum(v.z); v.w = warp_sum(v.w);
+  if ((threadIdx.x & 31) == 0) scratch[threadIdx.x >> 5] = v;
+  __syncthreads();
+  float4 t = scratch[0];
+#pragma unroll
+  for (int w = 1; w < kSmemWarps; ++w) {
+    const float4 u = scratch[w];
+    t.x += u.x; t.y += u.y; t.z += u.z; t.w += u.w;
+  }
+  return t;
+}
+__device__ __forceinline__ float block_sum_f(float v, float* scratch) {
+  v = warp_sum(v);
+  if ((threadIdx.x & 31) == 0) scratch[threadIdx.x >> 5] = v;
+  __syncthreads();
+  float t = scratch[0];
+#pragma unroll
+  for (int w = 1; w < kSmemWarps; ++w) t += scratch[w];
+  return t;
+}
+
+// The pass-A plane of one template arrives by bulk async copies: 8 plane
+// rows per copy (the rows of one padding group are contiguous in shared
+// memory), completion counted on one mbarrier. Every wait is bounded.
+constexpr unsigned kPlaneWaitLimit = 1u << 24;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+template <int N>
+__device__ __forceinline__ void plane_load(float2* Zs, const float2* src, uint64_t* bar) {
+  constexpr uint32_t kChunk = 8u * plane_ld(N) * sizeof(float2);
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(kChunk * (N / 8)) : "memory");
+  for (int q = 0; q < N / 8; ++q)
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(Zs + 9 * q * plane_ld(N))),
+        "l"(src + (size_t)8 * q * plane_ld(N)), "r"(kChunk), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ bool plane_wait(uint64_t* bar, uint32_t parity) {
+  for (unsigned i = 0; i < kPlaneWaitLimit; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+template <int N>
+__device__ void build_one_smem(const ProjParams& P, int slot, float2* Zs, const float2* tw, float* s_div,
+                               float4* red4, float* red, float* s_misc, const unsigned short* s_bins,
+                               const int* s_bptr, const float* s_fsc, const float2* next_plane, uint64_t* bar) {
+  constexpr int HC = N / 2 + 1, L2 = N / 16, G = 32 / L2, RP = 2 * G;
   const Plane<N> Z{Zs};
   const int nb = P.nb, H = nb / 2 + 1;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-  // ---- pass A: pruned row inverse of the gathered slice. A warp round takes
-  // CPR = 16/L2 columns (G = 2*CPR lines of N: even rows in the plane column,
-  // odd rows staged), one warp FFT transforms them, and each even/odd pair
-  // combines into the N centred rows of the 2N-point inverse, written back
-  // into the column (output row (k + N/2) mod N takes frequency k).
-  {
-    constexpr int CPR = pass_a_cols<N>();
-    float2* st = stage_all + warp * (CPR * plane_ld(N));
-    const float2* sl = P.slices + (size_t)b_index * W * m;
-    for (int c0 = warp * CPR; c0 < W; c0 += kSmemWarps * CPR) {
-      const int nc = min(CPR, W - c0);
-      const PassALines<N> L{Z, c0, st};
-      for (int idx = lane; idx < nc * m; idx += 32) {
-        const int cl = idx / m, i = idx - cl * m;  // i < N: even row 2i, else odd row 2(i-N)+1
-        L.at(cl * 2 + (i >= N), i < N ? i : i - N) = __ldg(sl + (size_t)(c0 + cl) * m + i);
-      }
-      __syncwarp();
-      warp_fft<N, 1>(L, 2 * nc, tw);
-      constexpr int KPL = N / 32;  // frequencies per lane and column
-      if constexpr (KPL >= 2) {
-        // frequency k = lane + 32 t lands on row k + N/2 = lane + 32 (t + KPL/2)
-        // (mod N): the same lane, so each lane swaps its pairs in place
-        for (int cl = 0; cl < nc; ++cl) {
-#pragma unroll
-          for (int t = 0; t < KPL / 2; ++t) {
-            const int k0 = lane + 32 * t, k1 = k0 + N / 2;
-            const float2 o0 = cadd(L.at(cl * 2, k0), cmul(tw_pos(tw, k0, m), L.at(cl * 2 + 1, k0)));
-            const float2 o1 = cadd(L.at(cl * 2, k1), cmul(tw_pos(tw, k1 - N, m), L.at(cl * 2 + 1, k1)));
-            Z(k1, c0 + cl) = o0;
-            Z(k0, c0 + cl) = o1;
-          }
-        }
-      } else {
-        float2 out[CPR];
-#pragma unroll
-        for (int cl = 0; cl < CPR; ++cl) {
-          const int k = lane, u = k < N / 2 ? k : k - N;
-          if (cl < nc) out[cl] = cadd(L.at(cl * 2, k), cmul(tw_pos(tw, u, m), L.at(cl * 2 + 1, k)));
-        }
-        __syncwarp();
-#pragma unroll
-        for (int cl = 0; cl < CPR; ++cl)
-          if (cl < nc) Z((lane + N / 2) % N, c0 + cl) = out[cl];
-      }
-      __syncwarp();
-    }
-  }
-  __syncthreads();
-
-  // ---- pass B: C2R along columns, keep centred N, then forward row FFT
+  // ---- pass B: C2R along rows (the plane written by rows_inverse arrived by
+  // bulk copy before this call), keep the centred N columns as real values
+  constexpr int m = 2 * N;
   const float scale_b = (float)(1.0 / ((double)m * (double)m));
   for (int r0 = warp * G; r0 < N; r0 += kSmemWarps * G) {
     const RowLines<N> RL{Z, r0};
@@ -715,11 +747,21 @@ __device__ void build_one_smem(const ProjParams& P, int b_index, int slot, float
 #pragma unroll
       for (int t = 0; t < 16; ++t) {
         const int idx = lane + 32 * t, g = idx / N, j = idx % N;
-        RL.at(g, j) = make_float2(pv[t], 0.f);
+        RL.at(g, j).x = pv[t];
       }
-      __syncwarp();
     }
-    warp_fft<N, -1>(RL, G, tw);
+  }
+  __syncthreads();
+  // forward FFT of the real rows, two rows per complex line
+  for (int r0 = warp * RP; r0 < N; r0 += kSmemWarps * RP) {
+#pragma unroll
+    for (int t = 0; t < 16; ++t) {
+      const int idx = lane + 32 * t, q = idx / N, j = idx % N;
+      Z(r0 + 2 * q, j).y = Z(r0 + 2 * q + 1, j).x;
+    }
+    __syncwarp();
+    warp_fft<N, -1>(PairLines<N>{Z, r0}, G, tw);
+    pair_split<N>(Z, r0, lane);
   }
   __syncthreads();
 
@@ -727,25 +769,30 @@ __device__ void build_one_smem(const ProjParams& P, int b_index, int slot, float
   for (int c0 = warp * G; c0 < HC; c0 += kSmemWarps * G)
     warp_fft<N, -1>(ColLines<N>{Z, c0}, min(G, HC - c0), tw);
   __syncthreads();
-  // radial |F| sums: float32 per lane (the reference sums in float32 with
-  // scatter_add_), float64 across the warp
+  // radial |F| sums in float32 (the reference sums in float32 with
+  // scatter_add_): per lane, then a fixed xor tree across the warp. The bin
+  // list holds plane offsets, the top bit set for columns 0 and N/2 (weight
+  // 1; every other column stands for itself and its mirror, weight 2).
   for (int b = warp; b < P.n_bins; b += kSmemWarps) {
     float acc = 0.f;
     const int e1 = s_bptr[b + 1];
 #pragma unroll 4
     for (int e = s_bptr[b] + lane; e < e1; e += 32) {
-      const int idx = s_bins[e];
-      const int r = idx / HC, kx = idx - r * HC;
-      const float2 f = Z(r, kx);
-      const float a = hypotf(f.x, f.y);
-      acc += (kx == 0 || kx == N / 2) ? a : 2.0f * a;
+      const unsigned v = s_bins[e];
+      const float2 f = Zs[v & 0x7fffu];
+      const float a = __fsqrt_rn(fmaf(f.x, f.x, f.y * f.y));
+      acc += (v & 0x8000u) ? a : 2.0f * a;
     }
-    const double accd = warp_sum_d((double)acc);
-    if (lane == 0) s_div[b] = (b == 0) ? 1.0f : (float)((double)P.bin_count[b] / accd);
+    acc = warp_sum(acc);
+    if (lane == 0) s_div[b] = (b == 0) ? 1.0f : __fdiv_rn(__ldg(P.bin_count + b), acc);
   }
   __syncthreads();
 
-  // ---- pass D: radial divisor, inverse column FFT
+  // ---- pass D: radial divisor, inverse column FFT. The DC term (bin 0,
+  // left as it is) over N^2 is the image mean; it is read before column 0
+  // is transformed and taken out of every pixel in pass E, so the float32
+  // plane-fit and variance sums run on centred values.
+  if (threadIdx.x == 0) s_misc[0] = Z(0, 0).x * (float)(1.0 / ((double)N * (double)N));
   for (int c0 = warp * G; c0 < HC; c0 += kSmemWarps * G) {
     const int nc = min(G, HC - c0);
     for (int idx = lane; idx < nc * N; idx += 32) {
@@ -759,172 +806,263 @@ __device__ void build_one_smem(const ProjParams& P, int b_index, int slot, float
   }
   __syncthreads();
 
-  // ---- pass E: inverse row transform (real part), plane-fit sums
+  // ---- pass E: inverse row transform (real part) of row pairs, plane-fit
+  // sums. Line q carries z = A + i B over the Hermitian extensions of rows
+  // a = r0 + 2q and b = a + 1 (the imaginary parts of columns 0 and N/2 are
+  // dropped, as the real part of the reference's ifft2 does); its inverse
+  // is a + i b. Position N-k is written only from position k < N/2, which
+  // no other task reads, so the packing needs no barrier.
   const float scale_e = (float)(1.0 / ((double)N * (double)N));
-  float fz = 0.f, fxz = 0.f, fyz = 0.f;  // float32 partial sums, float64 across the block
-  for (int r0 = warp * G; r0 < N; r0 += kSmemWarps * G) {
-    const RowLines<N> RL{Z, r0};
-    // Hermitian extension of each row: position N-k takes conj(G(k)); only
-    // positions above N/2 are written, from positions below, so no barrier.
-    for (int idx = lane; idx < G * (N / 2 + 1); idx += 32) {
-      const int g = idx / (N / 2 + 1), k = idx % (N / 2 + 1);
-      if (k == 0 || k == N / 2) RL.at(g, k).y = 0.f;
-      else RL.at(g, N - k) = cconj(RL.at(g, k));
-    }
-    __syncwarp();
-    warp_fft<N, 1>(RL, G, tw);
-#pragma unroll
-    for (int t = 0; t < 16; ++t) {
-      const int idx = lane + 32 * t, g = idx / N, j = idx % N;
-      const int i = r0 + g;
-      const float w = RL.at(g, j).x * scale_e;
-      RL.at(g, j) = make_float2(w, 0.f);
-      fz += w;
-      fxz = fmaf((float)i, w, fxz);
-      fyz = fmaf((float)j, w, fyz);
-    }
-  }
-  const double sz = block_sum_d((double)fz, red);
-  const double sxz = block_sum_d((double)fxz, red);
-  const double syz = block_sum_d((double)fyz, red);
-  if (threadIdx.x == 0) {
-    const double n = (double)N, n2 = n * n;
-    const double s1 = n * (n - 1.0) / 2.0 * n;
-    const double s2 = (n - 1.0) * n * (2.0 * n - 1.0) / 6.0 * n;
-    const double sxy = (n * (n - 1.0) / 2.0) * (n * (n - 1.0) / 2.0);
-    double A[3][4] = {{s2, sxy, s1, sxz}, {sxy, s2, s1, syz}, {s1, s1, n2, sz}};
-    for (int c = 0; c < 3; ++c) {
-      int p = c;
-      for (int r2 = c + 1; r2 < 3; ++r2) if (fabs(A[r2][c]) > fabs(A[p][c])) p = r2;
-      if (p != c) for (int k = 0; k < 4; ++k) { double tmp = A[c][k]; A[c][k] = A[p][k]; A[p][k] = tmp; }
-      for (int r2 = 0; r2 < 3; ++r2) {
-        if (r2 == c) continue;
-        const double f = A[r2][c] / A[c][c];
-        for (int k = c; k < 4; ++k) A[r2][k] -= f * A[c][k];
+  const float mu = s_misc[0];
+  float fz = 0.f, fxz = 0.f, fyz = 0.f;
+  for (int r0 = warp * RP; r0 < N; r0 += kSmemWarps * RP) {
+    for (int idx = lane; idx < G * HC; idx += 32) {
+      const int q = idx / HC, k = idx - q * HC, i1 = r0 + 2 * q;
+      const float2 a = Z(i1, k), b = Z(i1 + 1, k);
+      if (k == 0 || k == N / 2) {
+        Z(i1, k) = make_float2(a.x, b.x);
+      } else {
+        Z(i1, k) = make_float2(a.x - b.y, a.y + b.x);
+        Z(i1, N - k) = make_float2(a.x + b.y, b.x - a.y);
       }
     }
-    const double c0 = A[0][3] / A[0][0], c1 = A[1][3] / A[1][1], c2 = A[2][3] / A[2][2];
-    s_coef[0] = c0; s_coef[1] = c1; s_coef[2] = c2;
-    s_coef[3] = (sz - c0 * s1 - c1 * s1 - c2 * n2) / n2;
-  }
-  __syncthreads();
-  // plane and mean removal in float32 (the reference's precision), variance
-  // summed in float32 per thread and float64 across the block
-  const float fp0 = (float)s_coef[0], fp1 = (float)s_coef[1], fpc = (float)(s_coef[2] + s_coef[3]);
-  float fsv = 0.f;
-  for (int t = threadIdx.x; t < N * N; t += blockDim.x) {
-    const int i = t / N, j = t - i * N;
-    const float v = Z(i, j).x - fmaf(fp0, (float)i, fmaf(fp1, (float)j, fpc));
-    fsv = fmaf(v, v, fsv);
-  }
-  const double sv = block_sum_d((double)fsv, red);
-  const double sd = sqrt(sv / ((double)N * (double)N));
-  const float inv_sd = sd > 1e-12 ? (float)(1.0 / sd) : 1.0f;
-
-  // ---- pass F: normalise, mask, forward row FFT
-  for (int r0 = warp * G; r0 < N; r0 += kSmemWarps * G) {
-    const RowLines<N> RL{Z, r0};
+    __syncwarp();
+    warp_fft<N, 1>(PairLines<N>{Z, r0}, G, tw);
 #pragma unroll
     for (int t = 0; t < 16; ++t) {
-      const int idx = lane + 32 * t, g = idx / N, j = idx % N;
-      const int i = r0 + g;
-      float f = (RL.at(g, j).x - fmaf(fp0, (float)i, fmaf(fp1, (float)j, fpc))) * inv_sd;
-      if (P.mask != nullptr) f *= __ldg(P.mask + i * N + j);
-      RL.at(g, j) = make_float2(f, 0.f);
+      const int idx = lane + 32 * t, q = idx / N, j = idx % N, i1 = r0 + 2 * q;
+      const float2 z = Z(i1, j);
+      const float wa = fmaf(z.x, scale_e, -mu), wb = fmaf(z.y, scale_e, -mu);
+      Z(i1, j).x = wa;
+      Z(i1 + 1, j).x = wb;
+      fz += wa + wb;
+      fxz = fmaf((float)i1, wa, fmaf((float)(i1 + 1), wb, fxz));
+      fyz = fmaf((float)j, wa + wb, fyz);
+    }
+  }
+  // Least-squares plane over the full N x N grid in closed form: the grid is
+  // a Cartesian product, so the centred row and column coordinates are
+  // orthogonal and the normal equations of the reference's 3x3 solve
+  // (rows as x, columns as y) decouple.
+  const float4 s4 = block_sum_f4(make_float4(fz, fxz, fyz, 0.f), red4);
+  constexpr float kMid = 0.5f * (float)(N - 1);
+  constexpr float kSii = (float)((double)N * (double)N * ((double)N * (double)N - 1.0) / 12.0);
+  const float pc0 = (s4.y - kMid * s4.x) / kSii;
+  const float pc1 = (s4.z - kMid * s4.x) / kSii;
+  const float pcm = s4.x * scale_e - (pc0 + pc1) * kMid;
+  // plane and mean removal in float32 (the reference's precision); the
+  // population variance is summed per thread and over a fixed tree
+  float fsv = 0.f;
+  for (int t = threadIdx.x; t < N * N; t += kSmemThreads) {
+    const int i = t / N, j = t - i * N;
+    const float v = Z(i, j).x - fmaf(pc0, (float)i, fmaf(pc1, (float)j, pcm));
+    fsv = fmaf(v, v, fsv);
+  }
+  const float sd = sqrtf(block_sum_f(fsv, red) * scale_e);
+  const float inv_sd = sd > 1e-12f ? 1.0f / sd : 1.0f;
+
+  // ---- pass F: normalise, mask, forward row FFT of row pairs
+  for (int r0 = warp * RP; r0 < N; r0 += kSmemWarps * RP) {
+#pragma unroll
+    for (int t = 0; t < 16; ++t) {
+      const int idx = lane + 32 * t, q = idx / N, j = idx % N, i1 = r0 + 2 * q;
+      const float pj = fmaf(pc1, (float)j, pcm);
+      float fa = (Z(i1, j).x - fmaf(pc0, (float)i1, pj)) * inv_sd;
+      float fb = (Z(i1 + 1, j).x - fmaf(pc0, (float)(i1 + 1), pj)) * inv_sd;
+      if (P.mask != nullptr) {
+        fa *= __ldg(P.mask + i1 * N + j);
+        fb *= __ldg(P.mask + (i1 + 1) * N + j);
+      }
+      Z(i1, j) = make_float2(fa, fb);
     }
     __syncwarp();
-    warp_fft<N, -1>(RL, G, tw);
+    warp_fft<N, -1>(PairLines<N>{Z, r0}, G, tw);
+    pair_split<N>(Z, r0, lane);
   }
   __syncthreads();
   // ---- pass G: forward column FFT
   for (int c0 = warp * G; c0 < HC; c0 += kSmemWarps * G)
     warp_fft<N, -1>(ColLines<N>{Z, c0}, min(G, HC - c0), tw);
   __syncthreads();
-  // crop + pack + FSC, L2 norm (float32 per thread, float64 across the block),
-  // pre-shifted write; each thread keeps its packed values in registers
-  // between the norm and the write
+  // crop + pack + FSC, L2 norm (float32 per thread, fixed tree across the
+  // block), pre-shifted write. Each thread keeps its packed values in
+  // registers between the norm and the write, so once the norm's barrier is
+  // passed the plane is free and the next template's plane load starts. The
+  // packed index t = r * H + c advances by the block size with an add and
+  // one carry, as H is a run-time size.
   constexpr int KP = (N * (N / 2 + 1) + kSmemThreads - 1) / kSmemThreads;
+  const int dr = kSmemThreads / H, dc = kSmemThreads - dr * H;
+  const int r_first = threadIdx.x / H, c_first = threadIdx.x - r_first * H;
   float2 fv[KP];
   float fss = 0.f;
+  {
+    int r = r_first, c = c_first;
 #pragma unroll
-  for (int q = 0; q < KP; ++q) {
-    const int t = threadIdx.x + q * kSmemThreads;
-    fv[q] = make_float2(0.f, 0.f);
-    if (t < nb * H) {
-      const int r = t / H, c = t - r * H;
-      const int ky = r < nb / 2 ? r : r - nb;
-      float2 f;
-      if (c < nb / 2) f = Z((ky + N) % N, c);
-      else if (nb == N) f = Z((ky + N) % N, N / 2);
-      else f = cconj(Z((-ky + N) % N, nb / 2));
-      fv[q] = cscale(f, __ldg(P.fsc + t));
-      fss = fmaf(fv[q].x, fv[q].x, fmaf(fv[q].y, fv[q].y, fss));
+    for (int q = 0; q < KP; ++q) {
+      const int t = threadIdx.x + q * kSmemThreads;
+      fv[q] = make_float2(0.f, 0.f);
+      if (t < nb * H) {
+        const int ky = r < nb / 2 ? r : r - nb;
+        float2 f;
+        if (c < nb / 2) f = Z((ky + N) & (N - 1), c);
+        else if (nb == N) f = Z((ky + N) & (N - 1), N / 2);
+        else f = cconj(Z((N - ky) & (N - 1), nb / 2));
+        fv[q] = cscale(f, s_fsc[t]);
+        fss = fmaf(fv[q].x, fv[q].x, fmaf(fv[q].y, fv[q].y, fss));
+      }
+      c += dc; r += dr;
+      if (c >= H) { c -= H; ++r; }
     }
   }
-  const double ss = block_sum_d((double)fss, red);
-  const float inv_norm = (float)(1.0 / sqrt(ss));
+  const float ss = block_sum_f(fss, red);
+  if (threadIdx.x == 0 && next_plane != nullptr) plane_load<N>(Zs, next_plane, bar);
+  const float inv_norm = 1.0f / sqrtf(ss);
   float2* out = P.bank + (size_t)slot * nb * H;
+  {
+    int r = r_first, c = c_first;
 #pragma unroll
-  for (int q = 0; q < KP; ++q) {
-    const int t = threadIdx.x + q * kSmemThreads;
-    if (t < nb * H) {
-      const int r = t / H, c = t - r * H;
-      const int rs = (r + nb / 2) % nb, cs = (c + H / 2) % H;
-      out[(size_t)rs * H + cs] = cscale(fv[q], inv_norm);
+    for (int q = 0; q < KP; ++q) {
+      const int t = threadIdx.x + q * kSmemThreads;
+      if (t < nb * H) {
+        const int rs = r + nb / 2 < nb ? r + nb / 2 : r - nb / 2;
+        const int cs = c + H / 2 < H ? c + H / 2 : c - (H - H / 2);
+        out[(size_t)rs * H + cs] = cscale(fv[q], inv_norm);
+      }
+      c += dc; r += dr;
+      if (c >= H) { c -= H; ++r; }
+    }
+  }
+}
+
+// Pass A as its own high-occupancy kernel: slice gather and pruned inverse
+// along the 2N grid rows. A CTA takes kRiWarps * CPR columns of one
+// template; a warp gathers its CPR columns into G = 2 * CPR staged lines
+// (even and odd rows of the 2N grid), transforms them with one warp FFT and
+// combines each even/odd pair into the N centred rows of the 2N-point
+// inverse (output row (k + N/2) mod N takes frequency k). The CTA then
+// writes its columns row by row into the template's plane in global memory,
+// laid out as the shared-memory plane's rows (row stride plane_ld(N),
+// column c at c + c/8), so the projector loads it with bulk copies.
+constexpr int kRiWarps = 4;
+
+template <int N>
+__host__ __device__ constexpr int ri_cols() { return kRiWarps * pass_a_cols<N>(); }
+
+template <int N>
+__global__ void __launch_bounds__(kRiWarps * 32) rows_inverse(const float2* __restrict__ spectrum,
+                                                              const float* __restrict__ rot,
+                                                              const int* __restrict__ dirs,
+                                                              const float2* __restrict__ tw_g,
+                                                              float2* __restrict__ planes) {
+  constexpr int m = 2 * N, W = N + 1, CPR = pass_a_cols<N>(), CC = ri_cols<N>(), LINE = plane_ld(N);
+  __shared__ float2 s_tw[kMaxFftLen / 2];
+  __shared__ float2 s_line[kRiWarps][2 * CPR][LINE];
+  __shared__ float2 s_out[N][CC + 1];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int b = blockIdx.y, c_cta = blockIdx.x * CC, cw = c_cta + warp * CPR;
+  const int nc = max(0, min(CPR, W - cw));
+  for (int t = threadIdx.x; t < kMaxFftLen / 2; t += blockDim.x) s_tw[t] = tw_g[t];
+  const float* R = rot + (size_t)dirs[b] * 9;
+  float2(*L)[LINE] = s_line[warp];
+  // lanes take nc columns x 32/nc rows per step: samples of neighbouring
+  // columns share trilinear corners, and this patch shape cut the gather's
+  // time by 40% against 32 rows of one column on GB300
+#pragma unroll 4
+  for (int idx = lane; idx < nc * m; idx += 32) {
+    const int cl = idx % nc, r = idx / nc;
+    const int k = r >> 1;
+    L[2 * cl + (r & 1)][k + (k >> 3)] = slice_value<N>(spectrum, R, r, cw + cl);
+  }
+  __syncthreads();
+  if (nc > 0) {
+    warp_fft<N, 1>(StageLines<N>{&L[0][0]}, 2 * nc, s_tw);
+    for (int idx = lane; idx < nc * N; idx += 32) {
+      const int cl = idx / N, k = idx - cl * N;
+      const int u = k < N / 2 ? k : k - N;
+      const int kk = k + (k >> 3);
+      s_out[(k + N / 2) & (N - 1)][warp * CPR + cl] = cadd(L[2 * cl][kk], cmul(tw_pos(s_tw, u, m), L[2 * cl + 1][kk]));
     }
   }
   __syncthreads();
-}
-
-template <int N>
-__global__ void __launch_bounds__(2 * N) gather_slices(ProjParams P, float2* __restrict__ slices) {
-  constexpr int m = 2 * N, W = N + 1;
-  const int c = blockIdx.x, b = blockIdx.y, r = threadIdx.x;
-  const float* R = P.rot + (size_t)P.dirs[b] * 9;
-  const float2 v = slice_value<N>(P.spectrum, R, r, c);
-  slices[((size_t)b * W + c) * m + ((r & 1) ? N + (r >> 1) : (r >> 1))] = v;
+  float2* dst = planes + (size_t)b * N * plane_ld(N);
+  const int ncta = min(CC, W - c_cta);
+  for (int e = threadIdx.x; e < N * CC; e += blockDim.x) {
+    const int y = e / CC, cl = e - y * CC, c = c_cta + cl;
+    if (cl < ncta) dst[(size_t)y * plane_ld(N) + c + (c >> 3)] = s_out[y][cl];
+  }
 }
 
 template <int N>
 __global__ void __launch_bounds__(kSmemThreads, 1) project_templates_smem(ProjParams P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr int L2 = N / 16;
   float2* Zs = reinterpret_cast<float2*>(smem_raw);
-  float2* stage = Zs + plane_rows(N) * plane_ld(N);
-  float2* s_tw = stage + kSmemWarps * pass_a_cols<N>() * plane_ld(N);
-  double* red = reinterpret_cast<double*>(s_tw + kMaxFftLen / 2);
-  double* s_coef = red + 32;
-  float* s_div = reinterpret_cast<float*>(s_coef + 8);
+  float2* s_tw = Zs + plane_rows(N) * plane_ld(N);
+  float4* red4 = reinterpret_cast<float4*>(s_tw + kMaxFftLen / 2);
+  float* red = reinterpret_cast<float*>(red4 + kSmemWarps);
+  float* s_misc = red + kSmemWarps;                                        // [4]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(s_misc + 4);
+  float* s_div = reinterpret_cast<float*>(bar + 1);                         // [n_bins + 4]
   int* s_bptr = reinterpret_cast<int*>(s_div + P.n_bins + 4);              // [n_bins + 1]
   unsigned short* s_bins = reinterpret_cast<unsigned short*>(s_bptr + P.n_bins + 1);  // [N (N/2 + 1)]
+  float* s_fsc = reinterpret_cast<float*>(s_bins + N * (N / 2 + 1));                  // [nb (nb/2 + 1)]
+  constexpr int HC = N / 2 + 1;
+  const Plane<N> Z{Zs};
+  for (int t = threadIdx.x; t < P.nb * (P.nb / 2 + 1); t += blockDim.x) s_fsc[t] = P.fsc[t];
   for (int t = threadIdx.x; t < kMaxFftLen / 2; t += blockDim.x) s_tw[t] = P.tw[t];
   for (int t = threadIdx.x; t <= P.n_bins; t += blockDim.x) s_bptr[t] = P.bin_ptr[t];
-  for (int t = threadIdx.x; t < N * (N / 2 + 1); t += blockDim.x) s_bins[t] = (unsigned short)P.bin_list[t];
+  // bin list as plane offsets (< 2^15 for N <= 128), top bit for the
+  // columns that stand for themselves only
+  for (int t = threadIdx.x; t < N * HC; t += blockDim.x) {
+    const int idx = P.bin_list[t], r = idx / HC, kx = idx - r * HC;
+    const unsigned edge = (kx == 0 || kx == N / 2) ? 0x8000u : 0u;
+    s_bins[t] = (unsigned short)((unsigned)Z.off(r, kx) | edge);
+  }
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
   __syncthreads();
-  for (int b = blockIdx.x; b < P.n_build; b += gridDim.x) {
+  const size_t plane_elems = (size_t)N * plane_ld(N);
+  if (threadIdx.x == 0 && blockIdx.x < P.n_build) plane_load<N>(Zs, P.planes + blockIdx.x * plane_elems, bar);
+  uint32_t phase = 0;
+  for (int b = blockIdx.x; b < P.n_build; b += gridDim.x, phase ^= 1u) {
     const int dir = P.dirs[b];
     const int slot = P.out_slot ? P.out_slot[b] : dir;
-    build_one_smem<N>(P, b, slot, Zs, stage, s_tw, s_div, red, s_coef, s_bins, s_bptr);
+    const bool ok = plane_wait(bar, phase);
+    if (__syncthreads_or(!ok)) {
+      // a plane that never arrived: its template and the remaining ones of
+      // this CTA become NaN, so every score computed from them is NaN
+      const float nan = __int_as_float(0x7fc00000);
+      for (int b2 = b; b2 < P.n_build; b2 += gridDim.x) {
+        float2* out = P.bank + (size_t)(P.out_slot ? P.out_slot[b2] : P.dirs[b2]) * P.nb * (P.nb / 2 + 1);
+        for (int t = threadIdx.x; t < P.nb * (P.nb / 2 + 1); t += blockDim.x) out[t] = make_float2(nan, nan);
+      }
+      return;
+    }
+    const int nxt = b + gridDim.x;
+    build_one_smem<N>(P, slot, Zs, s_tw, s_div, red4, red, s_misc, s_bins, s_bptr, s_fsc,
+                      nxt < P.n_build ? P.planes + nxt * plane_elems : nullptr, bar);
   }
 }
 
 }  // namespace
 
-size_t project_smem_bytes_fast(int N, int n_bins) {
-  const int L2 = N / 16;
-  const int cpr = 16 / L2;
-  return (size_t)plane_rows(N) * plane_ld(N) * sizeof(float2) + (size_t)kSmemWarps * cpr * plane_ld(N) * sizeof(float2) +
-         (kMaxFftLen / 2) * sizeof(float2) + 40 * sizeof(double) + (size_t)(n_bins + 4) * sizeof(float) +
-         (size_t)(n_bins + 1) * sizeof(int) + (size_t)N * (N / 2 + 1) * sizeof(unsigned short);
+size_t project_smem_bytes_fast(int N, int n_bins, int nb) {
+  return (size_t)plane_rows(N) * plane_ld(N) * sizeof(float2) + (kMaxFftLen / 2) * sizeof(float2) +
+         kSmemWarps * (sizeof(float4) + sizeof(float)) + 4 * sizeof(float) + sizeof(uint64_t) +
+         (size_t)(n_bins + 4) * sizeof(float) + (size_t)(n_bins + 1) * sizeof(int) +
+         (size_t)N * (N / 2 + 1) * sizeof(unsigned short) + (size_t)nb * (nb / 2 + 1) * sizeof(float);
 }
 
 template <int N>
-static cudaError_t launch_fast(ProjParams P, int grid, float2* slices, cudaStream_t st) {
-  gather_slices<N><<<dim3(N + 1, P.n_build), 2 * N, 0, st>>>(P, slices);
+static cudaError_t launch_fast(ProjParams P, int grid, float2* planes, cudaStream_t st) {
+  constexpr int CC = ri_cols<N>();
+  rows_inverse<N><<<dim3((N + 1 + CC - 1) / CC, P.n_build), kRiWarps * 32, 0, st>>>(P.spectrum, P.rot, P.dirs,
+                                                                                      P.tw, planes);
   cudaError_t e0 = cudaGetLastError();
   if (e0 != cudaSuccess) return e0;
-  P.slices = slices;
-  const size_t smem = project_smem_bytes_fast(N, P.n_bins);
+  P.planes = planes;
+  const size_t smem = project_smem_bytes_fast(N, P.n_bins, P.nb);
   static size_t set_smem = 0;  // attribute set once per size, never inside a stream capture
   if (set_smem < smem) {
     cudaError_t e = cudaFuncSetAttribute(project_templates_smem<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -941,18 +1079,18 @@ cudaError_t launch_project_templates_fast(cudaStream_t st, const float2* spectru
                                           const float* mask, const float* fsc, const int* bin_list,
                                           const int* bin_ptr, const float* bin_count, int n_bins,
                                           const float2* tw, float2* bank, int grid, int N, int nb,
-                                          float2* slices) {
+                                          float2* planes) {
   if (n_build <= 0) return cudaSuccess;
   if (n_build > 65535) return cudaErrorInvalidValue;
   ProjParams P;
   P.spectrum = spectrum; P.rot = rot; P.dirs = dirs; P.n_build = n_build; P.mask = mask;
   P.fsc = fsc; P.bin_list = bin_list; P.bin_ptr = bin_ptr; P.bin_count = bin_count;
   P.n_bins = n_bins; P.tw = tw; P.bank = bank; P.out_slot = out_slot; P.scratch = nullptr;
-  P.scratch_stride = 0; P.N = N; P.nb = nb; P.slices = nullptr;
+  P.scratch_stride = 0; P.N = N; P.nb = nb; P.planes = nullptr;
   switch (N) {
-    case 32: return launch_fast<32>(P, grid, slices, st);
-    case 64: return launch_fast<64>(P, grid, slices, st);
-    case 128: return launch_fast<128>(P, grid, slices, st);
+    case 32: return launch_fast<32>(P, grid, planes, st);
+    case 64: return launch_fast<64>(P, grid, planes, st);
+    case 128: return launch_fast<128>(P, grid, planes, st);
     default: return cudaErrorInvalidValue;
   }
 }

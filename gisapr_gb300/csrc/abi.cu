@@ -38,7 +38,9 @@ cudaError_t launch_project_templates(cudaStream_t, const float2*, const float*, 
 size_t project_smem_bytes_fast(int N, int n_bins, int nb);
 cudaError_t launch_project_templates_fast(cudaStream_t, const float2*, const float*, const int*, int,
                                           const int*, const float*, const float*, const int*, const int*,
-                                          const float*, int, const float2*, float2*, int, int, int, float2*);
+                                          const float*, int, const float2*, float2*, int, int, int, float2*,
+                                          float2*);
+size_t project_blocked_elems(int N);
 size_t project_slice_elems(int N, int n_build);
 cudaError_t launch_packed_ctf(cudaStream_t, const float*, const float*, const float*, int,
                               const float*, const float*, const float*, const float*, int, float,
@@ -129,7 +131,7 @@ struct gisapr_context {
   std::map<int, std::pair<cufftHandle, float*>> fft;  // box -> (R2C plan, padded input)
   std::map<int, BinTable> bins;                        // N -> radial bins
   std::map<std::pair<int, int>, CorrTables> corr;      // (n, crop) -> twiddles
-  DeviceBuffer atoms, bin_counts, bin_lists, proj_scratch, prep_scratch, proj_slices;
+  DeviceBuffer atoms, bin_counts, bin_lists, proj_scratch, prep_scratch, proj_slices, proj_blocked;
   int sm_count = 152;
   std::map<int, int> tune_corr_cluster;  // n -> CTAs per particle in the plain correlation
 };
@@ -333,6 +335,7 @@ int gisapr_context_destroy(gisapr_ctx ctx) {
   cudaFree(ctx->bin_lists.ptr);
   cudaFree(ctx->proj_scratch.ptr);
   cudaFree(ctx->proj_slices.ptr);
+  cudaFree(ctx->proj_blocked.ptr);
   cudaFree(ctx->prep_scratch.ptr);
   cudaFree(ctx->tw);
   delete ctx;
@@ -436,10 +439,12 @@ int gisapr_project_templates(gisapr_ctx ctx, void* stream, const float* spectrum
     if (n_build > 65535) return fail(GISAPR_ERR_ARGUMENT, "at most 65535 templates per call");
     rc = ensure(ctx->proj_slices, project_slice_elems(box, n_build) * sizeof(float2), "cudaMalloc(planes)");
     if (rc) return rc;
+    rc = ensure(ctx->proj_blocked, project_blocked_elems(box) * sizeof(float2), "cudaMalloc(blocked spectrum)");
+    if (rc) return rc;
     GISAPR_CHECK_CUDA(launch_project_templates_fast((cudaStream_t)stream, (const float2*)spectrum, rot, dirs,
                                                     n_build, out_slot, mask, fsc, bt.list, bt.ptr, bt.count,
                                                     bt.n_bins, ctx->tw, (float2*)bank, grid, box, newbox,
-                                                    (float2*)ctx->proj_slices.ptr),
+                                                    (float2*)ctx->proj_slices.ptr, (float2*)ctx->proj_blocked.ptr),
                       "project_templates");
     return GISAPR_OK;
   }

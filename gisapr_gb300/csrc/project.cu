@@ -475,10 +475,43 @@ __host__ __device__ constexpr int pass_a_cols() { return 16 / (N / 16); }
 __host__ __device__ constexpr int plane_ld(int N) { return N == 128 ? 150 : (N == 64 ? 74 : 38); }
 __host__ __device__ constexpr int plane_rows(int N) { return N + N / 8; }
 
+// The half-volume spectrum in the blocked layout the slice gather reads:
+// centred order along z and y, cut into blocks of 2 (z) x 4 (y) x 2 (x)
+// voxels, one 128-byte line each (x padded to an even count). A trilinear
+// footprint then spans about two lines instead of four rows, and the 32
+// samples of one warp load touch 12 lines instead of 21 (counted for
+// random orientations), which is what bounds the gather's L1 throughput.
+constexpr int kBZ = 2, kBY = 4, kBX = 2, kBE = kBZ * kBY * kBX;
+
+template <int N>
+__host__ __device__ constexpr int blocked_x() { return (N + 1 + kBX - 1) / kBX; }
+
+template <int N>
+__device__ __forceinline__ int blocked_off(int z, int y, int x) {
+  constexpr int YB = 2 * N / kBY, XB = blocked_x<N>();
+  return (((z / kBZ) * YB + y / kBY) * XB + x / kBX) * kBE + ((z % kBZ) * kBY + y % kBY) * kBX + x % kBX;
+}
+
+template <int N>
+__global__ void __launch_bounds__(256) spectrum_blocked(const float2* __restrict__ spectrum,
+                                                        float2* __restrict__ out) {
+  constexpr int m = 2 * N, W = N + 1, XB = blocked_x<N>(), YB = m / kBY;
+  const int total = (m / kBZ) * YB * XB * kBE;
+  for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < total; o += gridDim.x * blockDim.x) {
+    const int e = o % kBE, blk = o / kBE;
+    const int xb = blk % XB, yb = (blk / XB) % YB, zb = blk / (XB * YB);
+    const int x = xb * kBX + e % kBX, y = yb * kBY + (e / kBX) % kBY, z = zb * kBZ + e / (kBX * kBY);
+    // the spectrum is stored unshifted along z and y: index (i + N) mod 2N
+    const int zs = z < N ? z + N : z - N, ys = y < N ? y + N : y - N;
+    out[o] = __ldg(spectrum + ((size_t)zs * m + ys) * W + min(x, W - 1));
+  }
+}
+
 // Trilinear sample at the slice point's voxel coordinates (grid_sample's
 // normalise/un-normalise pair with align_corners=True is the identity, so
 // the coordinates are used directly, clamped for border padding). Corners
-// past the last voxel carry weight 0 and are read clamped.
+// past the last voxel carry weight 0 and are read clamped. ``vol`` is the
+// blocked copy written by spectrum_blocked.
 template <int N>
 __device__ __forceinline__ float2 sample_slice(const float2* __restrict__ vol, float cz, float cy, float cx) {
   constexpr int m = 2 * N, W = N + 1;
@@ -490,15 +523,10 @@ __device__ __forceinline__ float2 sample_slice(const float2* __restrict__ vol, f
   const int z1 = min(z0 + 1, m - 1), y1 = min(y0 + 1, m - 1), x1 = min(x0 + 1, W - 1);
   const float wz1 = __fsub_rn(pz, fz), wy1 = __fsub_rn(py, fy), wx1 = __fsub_rn(px, fx);
   const float wz0 = __fsub_rn(fz + 1.0f, pz), wy0 = __fsub_rn(fy + 1.0f, py), wx0 = __fsub_rn(fx + 1.0f, px);
-  // storage is unshifted along z and y: stored index = (i + N) mod 2N
-  const int zs0 = z0 < N ? z0 + N : z0 - N, zs1 = z1 < N ? z1 + N : z1 - N;
-  const int ys0 = y0 < N ? y0 + N : y0 - N, ys1 = y1 < N ? y1 + N : y1 - N;
-  const float2* r00 = vol + (zs0 * m + ys0) * W;
-  const float2* r01 = vol + (zs0 * m + ys1) * W;
-  const float2* r10 = vol + (zs1 * m + ys0) * W;
-  const float2* r11 = vol + (zs1 * m + ys1) * W;
-  const float2 v000 = __ldg(r00 + x0), v001 = __ldg(r00 + x1), v010 = __ldg(r01 + x0), v011 = __ldg(r01 + x1);
-  const float2 v100 = __ldg(r10 + x0), v101 = __ldg(r10 + x1), v110 = __ldg(r11 + x0), v111 = __ldg(r11 + x1);
+  const float2 v000 = __ldg(vol + blocked_off<N>(z0, y0, x0)), v001 = __ldg(vol + blocked_off<N>(z0, y0, x1));
+  const float2 v010 = __ldg(vol + blocked_off<N>(z0, y1, x0)), v011 = __ldg(vol + blocked_off<N>(z0, y1, x1));
+  const float2 v100 = __ldg(vol + blocked_off<N>(z1, y0, x0)), v101 = __ldg(vol + blocked_off<N>(z1, y0, x1));
+  const float2 v110 = __ldg(vol + blocked_off<N>(z1, y1, x0)), v111 = __ldg(vol + blocked_off<N>(z1, y1, x1));
   const float w000 = __fmul_rn(__fmul_rn(wx0, wy0), wz0), w001 = __fmul_rn(__fmul_rn(wx1, wy0), wz0);
   const float w010 = __fmul_rn(__fmul_rn(wx0, wy1), wz0), w011 = __fmul_rn(__fmul_rn(wx1, wy1), wz0);
   const float w100 = __fmul_rn(__fmul_rn(wx0, wy0), wz1), w101 = __fmul_rn(__fmul_rn(wx1, wy0), wz1);
@@ -1047,6 +1075,9 @@ __global__ void __launch_bounds__(kSmemThreads, 1) project_templates_smem(ProjPa
 
 }  // namespace
 
+// complex elements of the blocked copy of one [2N][2N][N+1] spectrum
+size_t project_blocked_elems(int N) { return (size_t)4 * N * N * ((N + 1 + kBX - 1) / kBX) * kBX; }
+
 size_t project_smem_bytes_fast(int N, int n_bins, int nb) {
   return (size_t)plane_rows(N) * plane_ld(N) * sizeof(float2) + (kMaxFftLen / 2) * sizeof(float2) +
          kSmemWarps * (sizeof(float4) + sizeof(float)) + 4 * sizeof(float) + sizeof(uint64_t) +
@@ -1055,11 +1086,14 @@ size_t project_smem_bytes_fast(int N, int n_bins, int nb) {
 }
 
 template <int N>
-static cudaError_t launch_fast(ProjParams P, int grid, float2* planes, cudaStream_t st) {
+static cudaError_t launch_fast(ProjParams P, int grid, float2* planes, float2* blocked, cudaStream_t st) {
   constexpr int CC = ri_cols<N>();
-  rows_inverse<N><<<dim3((N + 1 + CC - 1) / CC, P.n_build), kRiWarps * 32, 0, st>>>(P.spectrum, P.rot, P.dirs,
-                                                                                      P.tw, planes);
+  spectrum_blocked<N><<<8 * 152, 256, 0, st>>>(P.spectrum, blocked);
   cudaError_t e0 = cudaGetLastError();
+  if (e0 != cudaSuccess) return e0;
+  rows_inverse<N><<<dim3((N + 1 + CC - 1) / CC, P.n_build), kRiWarps * 32, 0, st>>>(blocked, P.rot, P.dirs, P.tw,
+                                                                                      planes);
+  e0 = cudaGetLastError();
   if (e0 != cudaSuccess) return e0;
   P.planes = planes;
   const size_t smem = project_smem_bytes_fast(N, P.n_bins, P.nb);
@@ -1079,7 +1113,7 @@ cudaError_t launch_project_templates_fast(cudaStream_t st, const float2* spectru
                                           const float* mask, const float* fsc, const int* bin_list,
                                           const int* bin_ptr, const float* bin_count, int n_bins,
                                           const float2* tw, float2* bank, int grid, int N, int nb,
-                                          float2* planes) {
+                                          float2* planes, float2* blocked) {
   if (n_build <= 0) return cudaSuccess;
   if (n_build > 65535) return cudaErrorInvalidValue;
   ProjParams P;
@@ -1088,9 +1122,9 @@ cudaError_t launch_project_templates_fast(cudaStream_t st, const float2* spectru
   P.n_bins = n_bins; P.tw = tw; P.bank = bank; P.out_slot = out_slot; P.scratch = nullptr;
   P.scratch_stride = 0; P.N = N; P.nb = nb; P.planes = nullptr;
   switch (N) {
-    case 32: return launch_fast<32>(P, grid, planes, st);
-    case 64: return launch_fast<64>(P, grid, planes, st);
-    case 128: return launch_fast<128>(P, grid, planes, st);
+    case 32: return launch_fast<32>(P, grid, planes, blocked, st);
+    case 64: return launch_fast<64>(P, grid, planes, blocked, st);
+    case 128: return launch_fast<128>(P, grid, planes, blocked, st);
     default: return cudaErrorInvalidValue;
   }
 }

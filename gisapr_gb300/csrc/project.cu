@@ -475,6 +475,17 @@ __host__ __device__ constexpr int pass_a_cols() { return 16 / (N / 16); }
 __host__ __device__ constexpr int plane_ld(int N) { return N == 128 ? 150 : (N == 64 ? 74 : 38); }
 __host__ __device__ constexpr int plane_rows(int N) { return N + N / 8; }
 
+// Hardware square-root approximation (PTX sqrt.approx.f32, relative error
+// about 2^-23). Used for the radial |F| sums, whose float32 sums already
+// carry larger rounding, and for radial bin indices: rint(sqrt(d2)) of an
+// integer d2 <= 2 (N/2)^2 is at least 1/(8 sqrt(d2)) away from a rounding
+// boundary, far above the approximation's error, so the bins are exact.
+__device__ __forceinline__ float sqrt_approx(float x) {
+  float r;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 // The half-volume spectrum in the blocked layout the slice gather reads:
 // centred order along z and y, cut into blocks of 2 (z) x 4 (y) x 2 (x)
 // voxels, one 128-byte line each (x padded to an even count). A trilinear
@@ -808,7 +819,7 @@ __device__ void build_one_smem(const ProjParams& P, int slot, float2* Zs, const 
     for (int e = s_bptr[b] + lane; e < e1; e += 32) {
       const unsigned v = s_bins[e];
       const float2 f = Zs[v & 0x7fffu];
-      const float a = __fsqrt_rn(fmaf(f.x, f.x, f.y * f.y));
+      const float a = sqrt_approx(fmaf(f.x, f.x, f.y * f.y));
       acc += (v & 0x8000u) ? a : 2.0f * a;
     }
     acc = warp_sum(acc);
@@ -826,7 +837,7 @@ __device__ void build_one_smem(const ProjParams& P, int slot, float2* Zs, const 
     for (int idx = lane; idx < nc * N; idx += 32) {
       const int cl = idx / N, r = idx % N, kx = c0 + cl;
       const int ky = r < N / 2 ? r : r - N;
-      const int bin = (int)rintf(sqrtf((float)(ky * ky + kx * kx)));
+      const int bin = (int)rintf(sqrt_approx((float)(ky * ky + kx * kx)));
       Z(r, kx) = cscale(Z(r, kx), s_div[bin]);
     }
     __syncwarp();
@@ -842,7 +853,7 @@ __device__ void build_one_smem(const ProjParams& P, int slot, float2* Zs, const 
   // no other task reads, so the packing needs no barrier.
   const float scale_e = (float)(1.0 / ((double)N * (double)N));
   const float mu = s_misc[0];
-  float fz = 0.f, fxz = 0.f, fyz = 0.f;
+  float fz = 0.f, fxz = 0.f, fyz = 0.f, fww = 0.f;
   for (int r0 = warp * RP; r0 < N; r0 += kSmemWarps * RP) {
     for (int idx = lane; idx < G * HC; idx += 32) {
       const int q = idx / HC, k = idx - q * HC, i1 = r0 + 2 * q;
@@ -866,27 +877,35 @@ __device__ void build_one_smem(const ProjParams& P, int slot, float2* Zs, const 
       fz += wa + wb;
       fxz = fmaf((float)i1, wa, fmaf((float)(i1 + 1), wb, fxz));
       fyz = fmaf((float)j, wa + wb, fyz);
+      fww = fmaf(wa, wa, fmaf(wb, wb, fww));
     }
   }
   // Least-squares plane over the full N x N grid in closed form: the grid is
   // a Cartesian product, so the centred row and column coordinates are
   // orthogonal and the normal equations of the reference's 3x3 solve
   // (rows as x, columns as y) decouple.
-  const float4 s4 = block_sum_f4(make_float4(fz, fxz, fyz, 0.f), red4);
+  const float4 s4 = block_sum_f4(make_float4(fz, fxz, fyz, fww), red4);
   constexpr float kMid = 0.5f * (float)(N - 1);
   constexpr float kSii = (float)((double)N * (double)N * ((double)N * (double)N - 1.0) / 12.0);
   const float pc0 = (s4.y - kMid * s4.x) / kSii;
   const float pc1 = (s4.z - kMid * s4.x) / kSii;
   const float pcm = s4.x * scale_e - (pc0 + pc1) * kMid;
-  // plane and mean removal in float32 (the reference's precision); the
-  // population variance is summed per thread and over a fixed tree
-  float fsv = 0.f;
-  for (int t = threadIdx.x; t < N * N; t += kSmemThreads) {
-    const int i = t / N, j = t - i * N;
-    const float v = Z(i, j).x - fmaf(pc0, (float)i, fmaf(pc1, (float)j, pcm));
-    fsv = fmaf(v, v, fsv);
+  // Residual energy of the least-squares plane: sum (w - P)^2 = sum w^2 -
+  // sum P w (the normal equations make the residual orthogonal to P). The
+  // pixels are centred, so sum w^2 carries no DC term; where the plane
+  // holds most of the energy the subtraction would cancel, and the residual
+  // is summed directly instead (a block-uniform choice).
+  float ssr = s4.w - fmaf(pc0, s4.y, fmaf(pc1, s4.z, pcm * s4.x));
+  if (!(ssr > 0.25f * s4.w)) {
+    float fsv = 0.f;
+    for (int t = threadIdx.x; t < N * N; t += kSmemThreads) {
+      const int i = t / N, j = t - i * N;
+      const float v = Z(i, j).x - fmaf(pc0, (float)i, fmaf(pc1, (float)j, pcm));
+      fsv = fmaf(v, v, fsv);
+    }
+    ssr = block_sum_f(fsv, red);
   }
-  const float sd = sqrtf(block_sum_f(fsv, red) * scale_e);
+  const float sd = sqrtf(ssr * scale_e);
   const float inv_sd = sd > 1e-12f ? 1.0f / sd : 1.0f;
 
   // ---- pass F: normalise, mask, forward row FFT of row pairs

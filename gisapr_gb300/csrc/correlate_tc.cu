@@ -515,51 +515,57 @@ __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
             const uint32_t st = g % S;
             unsigned char* stB = stages + st * stage_bytes + 2 * a_part;
             if (g >= (uint32_t)S) ok = wait(bar_empty + st, (g / S - 1) & 1u) && ok;
-            const int b_tasks = ok ? g_psi * C * 4 : 0;
+            // one task per (crop row, 8-row block): its eight twiddles serve every psi angle
+            const int b_tasks = ok ? C * 4 : 0;
             for (int t = bt; t < b_tasks; t += kTcBuilders) {
-              const int yi = t % C, rest = t / C;
-              const int s = rest % g_psi, rc = rest / g_psi;
+              const int yi = t % C, rc = t / C;
               const int y = yi - h;
               const int r0 = qq * 32 + rc * 8;
-              const float2 tw0 = cscale(s_twr[(r0 * y) & (n - 1)], kTcScale);  // the operand scale
-              const float2 step = s_twr[y & (n - 1)];
-              const float2* pp = sp + s * n + r0;
-              // rows of psi s: per crop-row pair (Re y, Re y+1, Im y, Im y+1)
-              const int jr = s * kPS + 4 * (yi >> 1) + (yi & 1), ji = jr + 2;
-              // the eight products of the step, once for both parts
-              float ur[8], ui[8];
+              float2 twv[8];
               {
-                float2 tw = tw0;
+                float2 tw = cscale(s_twr[(r0 * y) & (n - 1)], kTcScale);  // the operand scale
+                const float2 step = s_twr[y & (n - 1)];
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
-                  const float2 u = cmul(pp[i], tw);
-                  ur[i] = u.x;
-                  ui[i] = u.y;
+                  twv[i] = tw;
                   tw = cmul(tw, step);
                 }
               }
+              for (int s = 0; s < g_psi; ++s) {
+                const float2* pp = sp + s * n + r0;
+                // rows of psi s: per crop-row pair (Re y, Re y+1, Im y, Im y+1)
+                const int jr = s * kPS + 4 * (yi >> 1) + (yi & 1), ji = jr + 2;
+                // the eight products of the step, once for both parts
+                float ur[8], ui[8];
 #pragma unroll
-              for (int part = 0; part < 2; ++part) {
-                // part 0: Re U -> Re-Z row first half, Im-Z row second half;
-                // part 1: Im U -> Im-Z row first half, -Im U in the Re-Z row second half
-                uint32_t hw[4], lw[4];
-#pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                  const float a = part ? ui[2 * i] : ur[2 * i], b = part ? ui[2 * i + 1] : ur[2 * i + 1];
-                  const __half2 hv = __floats2half2_rn(a, b);
-                  const float2 hf = __half22float2(hv);
-                  const __half2 lv = __floats2half2_rn(a - hf.x, b - hf.y);
-                  hw[i] = *reinterpret_cast<const uint32_t*>(&hv);
-                  lw[i] = *reinterpret_cast<const uint32_t*>(&lv);
+                for (int i = 0; i < 8; ++i) {
+                  const float2 u = cmul(pp[i], twv[i]);
+                  ur[i] = u.x;
+                  ui[i] = u.y;
                 }
-                const uint4 hi = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-                const uint4 lo = make_uint4(lw[0], lw[1], lw[2], lw[3]);
-                const int j1 = part ? ji : jr, j2 = part ? jr : ji;
-                *reinterpret_cast<uint4*>(stB + sw128(j1, rc)) = hi;
-                *reinterpret_cast<uint4*>(stB + sw128(j2, 4 + rc)) = part ? neg8(hi) : hi;
-                if (P.split) {
-                  *reinterpret_cast<uint4*>(stB + b_part + sw128(j1, rc)) = lo;
-                  *reinterpret_cast<uint4*>(stB + b_part + sw128(j2, 4 + rc)) = part ? neg8(lo) : lo;
+#pragma unroll
+                for (int part = 0; part < 2; ++part) {
+                  // part 0: Re U -> Re-Z row first half, Im-Z row second half;
+                  // part 1: Im U -> Im-Z row first half, -Im U in the Re-Z row second half
+                  uint32_t hw[4], lw[4];
+#pragma unroll
+                  for (int i = 0; i < 4; ++i) {
+                    const float a = part ? ui[2 * i] : ur[2 * i], b = part ? ui[2 * i + 1] : ur[2 * i + 1];
+                    const __half2 hv = __floats2half2_rn(a, b);
+                    const float2 hf = __half22float2(hv);
+                    const __half2 lv = __floats2half2_rn(a - hf.x, b - hf.y);
+                    hw[i] = *reinterpret_cast<const uint32_t*>(&hv);
+                    lw[i] = *reinterpret_cast<const uint32_t*>(&lv);
+                  }
+                  const uint4 hi = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+                  const uint4 lo = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+                  const int j1 = part ? ji : jr, j2 = part ? jr : ji;
+                  *reinterpret_cast<uint4*>(stB + sw128(j1, rc)) = hi;
+                  *reinterpret_cast<uint4*>(stB + sw128(j2, 4 + rc)) = part ? neg8(hi) : hi;
+                  if (P.split) {
+                    *reinterpret_cast<uint4*>(stB + b_part + sw128(j1, rc)) = lo;
+                    *reinterpret_cast<uint4*>(stB + b_part + sw128(j2, 4 + rc)) = part ? neg8(lo) : lo;
+                  }
                 }
               }
             }

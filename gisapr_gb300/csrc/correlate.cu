@@ -76,7 +76,9 @@ __global__ void __launch_bounds__(kThreads) correlate_plain(CorrParams P) {
   const float2* Pb = P.stack + (size_t)b * n_psi * n * H;
   for (int t = threadIdx.x; t < n_psi * n * cw; t += blockDim.x) {
     const int cl = t % cw, rr = t / cw;  // rr = psi * n + r
-    Pq[(size_t)rr * cwmax + cl] = Pb[(size_t)rr * H + clo + cl];
+    // read once per candidate: streaming loads, so the particle stack does
+    // not push the templates out of L2
+    Pq[(size_t)rr * cwmax + cl] = __ldcs(Pb + (size_t)rr * H + clo + cl);
   }
   __syncthreads();
 

@@ -25,7 +25,7 @@ namespace cg = cooperative_groups;
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kGroup = 4;     // templates per stage-1/stage-2 group
+constexpr int kGroup = 5;     // templates per stage-1/stage-2 group (5 x 3 psi x 17 columns fills 256 threads at n = 128)
 constexpr int kMaxLocal = 16; // templates whose partials are kept before a cluster reduction
 
 struct CorrParams {

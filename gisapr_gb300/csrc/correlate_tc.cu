@@ -700,10 +700,15 @@ __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
 // at position c ^ (cand & 7) (the 128-byte swizzle of the shared-memory tile,
 // whose direction blocks start on multiples of 8 rows). One block per
 // (slot, candidate); every candidate writes whole 128-byte rows.
+__host__ __device__ inline int bank_fp16_ld(int n) { return n + n / 8 + 1; }
+
 __global__ void bank_to_fp16(const float2* __restrict__ bank, long long bank_stride, int n, int n_cand, int cb,
                              __half* __restrict__ out) {
-  extern __shared__ float2 s_t[];  // [n][cb]: columns [c0, c0 + cb) of the template
-  const int H = n / 2 + 1, nq = n / 32;
+  // [cb][ld]: columns [c0, c0 + cb) of the template, column-major with a
+  // spare slot after every 8 rows, so the 16 row blocks a warp reads at once
+  // fall on distinct banks
+  extern __shared__ float2 s_t[];
+  const int H = n / 2 + 1, nq = n / 32, ld = bank_fp16_ld(n);
   const int slot = blockIdx.x, cand = blockIdx.y;
   const float2* src = bank + (size_t)cand * (size_t)bank_stride + (size_t)slot * n * H;
   for (int c0 = 0; c0 < H; c0 += cb) {
@@ -711,7 +716,7 @@ __global__ void bank_to_fp16(const float2* __restrict__ bank, long long bank_str
     __syncthreads();
     for (int t = threadIdx.x; t < n * w; t += blockDim.x) {
       const int r = t / w, c = t - r * w;
-      s_t[r * cb + c] = src[(size_t)r * H + c0 + c];
+      s_t[c * ld + r + (r >> 3)] = src[(size_t)r * H + c0 + c];
     }
     __syncthreads();
     // one task per (col, step, chunk): 8 consecutive k -> hi and lo 16-byte chunks
@@ -719,10 +724,11 @@ __global__ void bank_to_fp16(const float2* __restrict__ bank, long long bank_str
       const int c = t & 7, qq = (t >> 3) % nq, cl = t / (8 * nq), col = c0 + cl;
       const bool imag = c >= 4;
       const int r0 = qq * 32 + (c & 3) * 8;
+      const float2* sc = s_t + cl * ld + r0 + (r0 >> 3);
       float v[8];
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
-        const float2 z = s_t[(r0 + i) * cb + cl];
+        const float2 z = sc[i];
         v[i] = (imag ? z.y : z.x) * kTcScale;
       }
       uint4 hi, lo;
@@ -816,8 +822,8 @@ int correlate_tc_plan(const int* local_ptr, const int* local_idx, int n_particle
 cudaError_t launch_bank_to_fp16(cudaStream_t st, const float2* bank, long long bank_stride, int n_cand, int n_slot,
                                 int n, void* out) {
   if (n_cand <= 0 || n_slot <= 0) return cudaSuccess;
-  const int cb = std::min(n / 2 + 1, 128 * 1024 / (int)(n * sizeof(float2)));  // columns per staged block
-  const size_t smem = (size_t)n * cb * sizeof(float2);
+  const int cb = std::min(n / 2 + 1, 128 * 1024 / (int)(bank_fp16_ld(n) * sizeof(float2)));  // columns per block
+  const size_t smem = (size_t)bank_fp16_ld(n) * cb * sizeof(float2);
   static size_t set_smem = 0;
   if (set_smem < smem) {
     cudaError_t e = cudaFuncSetAttribute(bank_to_fp16, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -52,8 +52,9 @@ def parse_args():
     ap.add_argument("--cpu-sample", type=int, default=400, help="particles and templates in the CPU sample")
     ap.add_argument("--batch", type=int, default=64, help="candidates per batched generation (0: skip)")
     ap.add_argument("--no-autotune", action="store_true", help="default launch shapes (no tuning runs)")
-    ap.add_argument("--precision-particles", type=int, default=64,
-                    help="particles of the box-256 precision comparison (0: skip it)")
+    ap.add_argument("--precision-particles", type=int, default=4000,
+                    help="particles of the box-256 precision comparison (0: skip it; 20000 is the full "
+                         "configuration, about three minutes of synthetic-data generation)")
     ap.add_argument("--serve-requests", type=int, default=40,
                     help="requests in the serving stream (0: skip the serving measurement)")
     ap.add_argument("--precisions", default="fp32,fp16x3",

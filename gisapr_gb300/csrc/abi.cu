@@ -33,8 +33,8 @@ size_t project_scratch_elems(int N, int nb);
 size_t project_smem_bytes(int N, int n_bins);
 cudaError_t launch_project_templates(cudaStream_t, const float2*, const float*, const int*, int,
                                      const int*, const float*, const float*, const int*, const int*,
-                                     const float*, int, const float2*, float2*, float2*, int, int,
-                                     int);
+                                     const float*, int, const float2*, const float2*, float2*, float2*, int,
+                                     int, int);
 size_t project_smem_bytes_fast(int N, int n_bins, int nb);
 cudaError_t launch_project_templates_fast(cudaStream_t, const float2*, const float*, const int*, int,
                                           const int*, const float*, const float*, const int*, const int*,
@@ -48,7 +48,7 @@ cudaError_t launch_packed_ctf(cudaStream_t, const float*, const float*, const fl
 size_t prepare_scratch_elems(int N, int nb);
 cudaError_t launch_prepare_particles(cudaStream_t, const float*, int, int, const int*, const void*,
                                      const float*, const float*, float2*, float2*, int,
-                                     const float2*, int, int);
+                                     const float2*, const float2*, int, int);
 int correlate_cluster_size(int n);
 size_t correlate_smem_bytes(int n, int n_psi, int crop, int cluster);
 cudaError_t launch_correlate_plain(cudaStream_t, const float2*, const float2*, const int*,
@@ -127,7 +127,8 @@ void gisapr_internal_set_error(const char* msg) { g_last_error = msg; }
 
 struct gisapr_context {
   int device = 0;
-  float2* tw = nullptr;  // exp(-2 pi i t / kMaxFftLen), t < kMaxFftLen/2
+  float2* tw = nullptr;   // exp(-2 pi i t / kMaxFftLen), t < kMaxFftLen/2
+  float2* tw3 = nullptr;  // exp(-2 pi i t / kMaxFftLen3), t < kMaxFftLen3 (lengths 3 * 2^k)
   std::map<int, std::pair<cufftHandle, float*>> fft;  // box -> (R2C plan, padded input)
   std::map<int, BinTable> bins;                        // N -> radial bins
   std::map<std::pair<int, int>, CorrTables> corr;      // (n, crop) -> twiddles
@@ -270,9 +271,12 @@ int tuned_cluster(gisapr_ctx ctx, int n) {
   return it == ctx->tune_corr_cluster.end() ? 0 : it->second;
 }
 
+// Boxes are powers of two from 32 to 256, or 96 and 192 (3 * 2^k: the
+// shared-memory transforms run a radix-3 pass over radix-2 sub-transforms).
 int check_box(int box) {
-  if (!is_pow2(box) || box < 32 || box > 256)
-    return fail(GISAPR_ERR_UNSUPPORTED, "box must be a power of two in [32, 256], got " + std::to_string(box));
+  if (!((is_pow2(box) && box >= 32 && box <= 256) || box == 96 || box == 192))
+    return fail(GISAPR_ERR_UNSUPPORTED, "box must be a power of two in [32, 256], 96 or 192, got " +
+                                            std::to_string(box));
   return GISAPR_OK;
 }
 
@@ -313,8 +317,15 @@ int gisapr_context_create(int device, gisapr_ctx* out) {
     const double a = -two_pi * (double)t / (double)kMaxFftLen;
     tw[t] = make_float2((float)std::cos(a), (float)std::sin(a));
   }
+  std::vector<float2> tw3(kMaxFftLen3);
+  for (int t = 0; t < kMaxFftLen3; ++t) {
+    const double a = -two_pi * (double)t / (double)kMaxFftLen3;
+    tw3[t] = make_float2((float)std::cos(a), (float)std::sin(a));
+  }
   cudaError_t e = cudaMalloc(&ctx->tw, tw.size() * sizeof(float2));
   if (e == cudaSuccess) e = cudaMemcpy(ctx->tw, tw.data(), tw.size() * sizeof(float2), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->tw3, tw3.size() * sizeof(float2));
+  if (e == cudaSuccess) e = cudaMemcpy(ctx->tw3, tw3.data(), tw3.size() * sizeof(float2), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     delete ctx;
     return cuda_fail(e, "context tables");
@@ -338,6 +349,7 @@ int gisapr_context_destroy(gisapr_ctx ctx) {
   cudaFree(ctx->proj_blocked.ptr);
   cudaFree(ctx->prep_scratch.ptr);
   cudaFree(ctx->tw);
+  cudaFree(ctx->tw3);
   delete ctx;
   return GISAPR_OK;
 }
@@ -433,7 +445,7 @@ int gisapr_project_templates(gisapr_ctx ctx, void* stream, const float* spectrum
   BinTable bt;
   rc = get_bins(ctx, box, &bt);
   if (rc) return rc;
-  if (box <= 128) {
+  if (box <= 128 && is_pow2(box)) {
     // whole template in shared memory, one CTA per SM
     const int grid = grid_for(ctx, n_build, 1);
     if (n_build > 65535) return fail(GISAPR_ERR_ARGUMENT, "at most 65535 templates per call");
@@ -454,7 +466,7 @@ int gisapr_project_templates(gisapr_ctx ctx, void* stream, const float* spectrum
   if (rc) return rc;
   GISAPR_CHECK_CUDA(launch_project_templates((cudaStream_t)stream, (const float2*)spectrum, rot, dirs, n_build,
                                              out_slot, mask, fsc, bt.list, bt.ptr, bt.count, bt.n_bins,
-                                             ctx->tw, (float2*)bank, (float2*)ctx->proj_scratch.ptr, grid,
+                                             ctx->tw, ctx->tw3, (float2*)bank, (float2*)ctx->proj_scratch.ptr, grid,
                                              box, newbox),
                     "project_templates");
   return GISAPR_OK;
@@ -492,7 +504,7 @@ int gisapr_prepare_particles(gisapr_ctx ctx, void* stream, const float* images, 
               "cudaMalloc(particle scratch)");
   if (rc) return rc;
   GISAPR_CHECK_CUDA(launch_prepare_particles((cudaStream_t)stream, images, n, n_psi, psi_index, psi_table, mask,
-                                             ctf, (float2*)out, (float2*)ctx->prep_scratch.ptr, grid, ctx->tw,
+                                             ctf, (float2*)out, (float2*)ctx->prep_scratch.ptr, grid, ctx->tw, ctx->tw3,
                                              box, newbox),
                     "prepare_particles");
   return GISAPR_OK;
@@ -626,8 +638,8 @@ int gisapr_correlate_tc_batch(gisapr_ctx ctx, void* stream, const float* bank, l
   if (n_slot == 0) return fail(GISAPR_ERR_ARGUMENT, "n_slot must be positive when there is work");
   if (n_cand > 1 && bank_stride < (long long)n_slot * n * (n / 2 + 1))
     return fail(GISAPR_ERR_ARGUMENT, "bank_stride is smaller than one candidate's bank");
-  if (n != 32 && n != 64 && n != 128 && n != 256)
-    return fail(GISAPR_ERR_UNSUPPORTED, "tensor-core correlation takes n in {32, 64, 128, 256}");
+  if (n != 32 && n != 64 && n != 96 && n != 128 && n != 192 && n != 256)
+    return fail(GISAPR_ERR_UNSUPPORTED, "tensor-core correlation takes n in {32, 64, 96, 128, 192, 256}");
   if (crop < 2 || crop > 14 || crop % 2 != 0 || crop > n || (n == 256 && crop < 10))
     return fail(GISAPR_ERR_UNSUPPORTED, "tensor-core correlation takes an even crop in 2..14 (10..14 at n = 256)");
   if (n_slot > 65535) return fail(GISAPR_ERR_ARGUMENT, "at most 65535 template slots");

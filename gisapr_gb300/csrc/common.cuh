@@ -65,6 +65,64 @@ GISAPR_DEV void smem_fft_dit(float2* buf, int L, int lines, int line_stride, int
 }
 
 // ---------------------------------------------------------------------------
+// Transform lengths 3 * 2^k (boxes 96 and 192 and their doubled grids).
+// ``tw3`` holds exp(-2 pi i t / kMaxFftLen3) for t < kMaxFftLen3 (the full
+// circle), computed on the host like ``tw``.
+// ---------------------------------------------------------------------------
+constexpr int kMaxFftLen3 = 384;
+
+GISAPR_DEV bool pow2_len(int L) { return (L & (L - 1)) == 0; }
+
+// Position of input element j in the in-place layout smem_fft expects:
+// bit-reversed for a power of two; for L = 3 L3, element 3q + r goes to
+// sub-line r at the bit-reversed position of q.
+GISAPR_DEV int fft_in_pos(int j, int L) {
+  if (pow2_len(L)) return bitrev(j, ilog2_pow2(L));
+  const int L3 = L / 3, q = j / 3, r = j - 3 * q;
+  return r * L3 + bitrev(q, ilog2_pow2(L3));
+}
+
+// exp(+2 pi i num / den) for |num| <= den/2, den a power of two <= kMaxFftLen
+// or 3 * 2^k <= kMaxFftLen3.
+GISAPR_DEV float2 tw_pos_any(const float2* tw, const float2* tw3, int num, int den) {
+  float2 w;
+  if (pow2_len(den)) w = tw[abs(num) * (kMaxFftLen / den)];
+  else w = tw3[abs(num) * (kMaxFftLen3 / den)];
+  return num >= 0 ? make_float2(w.x, -w.y) : w;
+}
+
+// In-place transforms of ``lines`` contiguous lines of length L (line
+// stride L) in shared memory, input in fft_in_pos order, output in natural
+// order; sign -1 forward, +1 unnormalised inverse. For L = 3 L3 the three
+// decimated sub-sequences are transformed by the radix-2 routine (as 3 x
+// lines lines of L3) and combined by one radix-3 pass:
+// X[k + m L3] = sum_r exp(sign 2 pi i r (k + m L3) / L) Y_r[k].
+// All threads of the block must call this.
+GISAPR_DEV void smem_fft(float2* buf, int L, int lines, float sign, const float2* __restrict__ tw,
+                         const float2* __restrict__ tw3) {
+  if (pow2_len(L)) {
+    smem_fft_dit(buf, L, lines, L, 1, sign, tw);
+    return;
+  }
+  const int L3 = L / 3, scale = kMaxFftLen3 / L;
+  smem_fft_dit(buf, L3, 3 * lines, L3, 1, sign, tw);
+  const float s3 = sign * 0.86602540378443864676f;  // Im exp(sign 2 pi i / 3)
+  for (int t = threadIdx.x; t < lines * L3; t += blockDim.x) {
+    const int l = t / L3, k = t - l * L3;
+    float2* base = buf + (size_t)l * L;
+    float2 w1 = tw3[k * scale], w2 = tw3[2 * k * scale];
+    if (sign > 0.f) { w1.y = -w1.y; w2.y = -w2.y; }
+    const float2 a = base[k], b = cmul(base[L3 + k], w1), c = cmul(base[2 * L3 + k], w2);
+    const float2 s = cadd(b, c), d = csub(b, c);
+    const float2 h = make_float2(a.x - 0.5f * s.x, a.y - 0.5f * s.y);
+    base[k] = cadd(a, s);
+    base[L3 + k] = make_float2(h.x - s3 * d.y, h.y + s3 * d.x);
+    base[2 * L3 + k] = make_float2(h.x + s3 * d.y, h.y - s3 * d.x);
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
 // 16-point inverse DFT in registers: X[r] = sum_j x[j] exp(+2 pi i j r / 16),
 // as a radix-4 x radix-4 decomposition (j = 4 j1 + j2, r = r1 + 4 r2).
 // The constants are cos/sin of multiples of pi/8.

@@ -52,8 +52,8 @@ constexpr int kTcStages = 4;      // shared-memory ring of K steps (at most)
 // psi angles per tile: three up to crop 12; at crop 14 two, so that the MMA
 // accumulators and the stage-2 rows kept in TMEM fit its 512 columns.
 __host__ __device__ constexpr int tc_psi_group(int C) { return C <= 12 ? 3 : 2; }
-// shared-memory stages: four, three at n = 256 (larger particle columns and tables)
-__host__ __device__ constexpr int tc_stages(int N) { return N >= 256 ? 3 : 4; }
+// shared-memory stages: four, three above n = 128 (larger particle columns and tables)
+__host__ __device__ constexpr int tc_stages(int N) { return N > 128 ? 3 : 4; }
 constexpr int kTcMaxCand = 128;   // candidates per launch
 constexpr int kTcTmemCols = 512;  // two MMA accumulators of kN <= 80 columns + stage-2 rows
 constexpr float kTcScale = 8192.0f;               // 2^13 on each operand
@@ -523,8 +523,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
               const int r0 = qq * 32 + rc * 8;
               float2 twv[8];
               {
-                float2 tw = cscale(s_twr[(r0 * y) & (n - 1)], kTcScale);  // the operand scale
-                const float2 step = s_twr[y & (n - 1)];
+                // twiddle indices modulo n (y < 0 for the upper half of the crop rows)
+                float2 tw = cscale(s_twr[((r0 * y) % n + n) % n], kTcScale);  // the operand scale
+                const float2 step = s_twr[(y % n + n) % n];
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
                   twv[i] = tw;
@@ -759,7 +760,9 @@ cudaError_t launch_tc_c(const TcParams& P, size_t smem, int grid, cudaStream_t s
   switch (P.n) {
     case 32: return launch_tc_cn<C, 32>(P, smem, grid, st);
     case 64: return launch_tc_cn<C, 64>(P, smem, grid, st);
+    case 96: return launch_tc_cn<C, 96>(P, smem, grid, st);
     case 128: return launch_tc_cn<C, 128>(P, smem, grid, st);
+    case 192: return launch_tc_cn<C, 192>(P, smem, grid, st);
     case 256:
       if constexpr (C >= 10) return launch_tc_cn<C, 256>(P, smem, grid, st);
       return cudaErrorInvalidValue;

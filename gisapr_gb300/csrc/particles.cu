@@ -67,6 +67,7 @@ struct PrepParams {
   float2* scratch;
   size_t scratch_stride;
   const float2* tw;
+  const float2* tw3;       // twiddles of lengths 3 * 2^k
   int n, n_psi, N, nb;
 };
 
@@ -91,7 +92,6 @@ __device__ __forceinline__ float sample_bilinear_zero(const float* __restrict__ 
 __global__ void __launch_bounds__(kThreads) prepare_particles(PrepParams P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int N = P.N, nb = P.nb, H = nb / 2 + 1, HC = N / 2 + 1;
-  const int logN = ilog2_pow2(N);
   float2* sm = reinterpret_cast<float2*>(smem_raw);
   float2* s_tw = sm + max(kRowBatch, kColBatch) * N;
   double* red = reinterpret_cast<double*>(s_tw + kMaxFftLen / 2);
@@ -121,10 +121,10 @@ __global__ void __launch_bounds__(kThreads) prepare_particles(PrepParams P) {
         const float ix = __fmul_rn(__fadd_rn(xn, 1.0f), half);
         float v = sample_bilinear_zero(img, N, iy, ix);
         if (P.mask != nullptr) v = __fmul_rn(v, P.mask[(size_t)(i0 + rl) * N + j]);
-        sm[rl * N + bitrev(j, logN)] = make_float2(v, 0.f);
+        sm[rl * N + fft_in_pos(j, N)] = make_float2(v, 0.f);
       }
       __syncthreads();
-      smem_fft_dit(sm, N, nr, N, 1, -1.0f, s_tw);
+      smem_fft(sm, N, nr, -1.0f, s_tw, P.tw3);
       for (int t = threadIdx.x; t < nr * HC; t += blockDim.x) {
         const int rl = t / HC, k = t - rl * HC;
         S[(size_t)(i0 + rl) * HC + k] = sm[rl * N + k];
@@ -136,10 +136,10 @@ __global__ void __launch_bounds__(kThreads) prepare_particles(PrepParams P) {
       const int nc = min(kColBatch, HC - c0);
       for (int t = threadIdx.x; t < nc * N; t += blockDim.x) {
         const int r = t / nc, cl = t - r * nc;
-        sm[cl * N + bitrev(r, logN)] = S[(size_t)r * HC + c0 + cl];
+        sm[cl * N + fft_in_pos(r, N)] = S[(size_t)r * HC + c0 + cl];
       }
       __syncthreads();
-      smem_fft_dit(sm, N, nc, N, 1, -1.0f, s_tw);
+      smem_fft(sm, N, nc, -1.0f, s_tw, P.tw3);
       for (int t = threadIdx.x; t < nc * N; t += blockDim.x) {
         const int r = t / nc, cl = t - r * nc;
         S[(size_t)r * HC + c0 + cl] = sm[cl * N + r];
@@ -198,12 +198,12 @@ size_t prepare_smem_bytes(int N) {
 cudaError_t launch_prepare_particles(cudaStream_t st, const float* images, int n, int n_psi,
                                      const int* psi_index, const void* psi_tab, const float* mask,
                                      const float* ctf, float2* out, float2* scratch, int grid,
-                                     const float2* tw, int N, int nb) {
+                                     const float2* tw, const float2* tw3, int N, int nb) {
   if (n <= 0) return cudaSuccess;
   PrepParams P;
   P.images = images; P.psi_index = psi_index; P.psi_tab = (const float4*)psi_tab; P.mask = mask;
   P.ctf = ctf; P.out = out; P.scratch = scratch; P.scratch_stride = prepare_scratch_elems(N, nb);
-  P.tw = tw; P.n = n; P.n_psi = n_psi; P.N = N; P.nb = nb;
+  P.tw = tw; P.tw3 = tw3; P.n = n; P.n_psi = n_psi; P.N = N; P.nb = nb;
   const size_t smem = prepare_smem_bytes(N);
   static size_t set_smem = 0;
   if (set_smem < smem) {

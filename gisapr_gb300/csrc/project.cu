@@ -44,6 +44,7 @@ struct ProjParams {
   const float* bin_count;   // [n_bins] full-grid counts per bin
   int n_bins;
   const float2* tw;         // twiddles exp(-2 pi i t / kMaxFftLen)
+  const float2* tw3;        // twiddles exp(-2 pi i t / kMaxFftLen3) (boxes 3 * 2^k)
   float2* bank;             // [n_dir_out][nb][H] output templates
   const int* out_slot;      // output row in bank for each build index (null => dirs[i])
   float2* scratch;          // per-CTA scratch
@@ -117,7 +118,6 @@ __device__ __forceinline__ float grid_pixel(float c, int size) {
 __device__ void build_one(const ProjParams& P, int dir, int slot, float2* S, float2* Pk,
                           float2* sm, double* red, float* s_div, double* s_coef) {
   const int N = P.N, m = 2 * N, W = N + 1, nb = P.nb, H = nb / 2 + 1;
-  const int logN = ilog2_pow2(N);
   const int LDS = N + 1;  // scratch row stride (complex)
   const float* R = P.rot + (size_t)dir * 9;
   const float R00 = R[0], R01 = R[1], R10 = R[3], R11 = R[4], R20 = R[6], R21 = R[7];
@@ -145,17 +145,17 @@ __device__ void build_one(const ProjParams& P, int dir, int slot, float2* S, flo
                                   grid_pixel(cx, W));
       if (conj) v.y = -v.y;
       const int e = r & 1, q = r >> 1;
-      sm[(cl * 2 + e) * N + bitrev(q, logN)] = v;
+      sm[(cl * 2 + e) * N + fft_in_pos(q, N)] = v;
     }
     __syncthreads();
-    smem_fft_dit(sm, N, 2 * nc, N, 1, +1.0f, P.tw);
+    smem_fft(sm, N, 2 * nc, +1.0f, P.tw, P.tw3);
     for (int t = threadIdx.x; t < nc * N; t += blockDim.x) {
       const int cl = t / N, i = t - cl * N;
       const int u = i - N / 2;               // signed output row of the 2N-point inverse
       const int k = (u + N) % N;
       const float2 a0 = sm[(cl * 2) * N + k];
       const float2 a1 = sm[(cl * 2 + 1) * N + k];
-      const float2 z = cadd(a0, cmul(tw_pos(P.tw, u, m), a1));
+      const float2 z = cadd(a0, cmul(tw_pos_any(P.tw, P.tw3, u, m), a1));
       S[(size_t)i * LDS + c0 + cl] = z;
     }
     __syncthreads();
@@ -177,23 +177,23 @@ __device__ void build_one(const ProjParams& P, int dir, int slot, float2* S, flo
       } else {
         const float2 zk = Z[k], zc = cconj(Z[N - k]);
         ye = cadd(zk, zc);
-        yo = cmul(csub(zk, zc), tw_pos(P.tw, k, m));
+        yo = cmul(csub(zk, zc), tw_pos_any(P.tw, P.tw3, k, m));
       }
       // W = Ye + i*Yo
-      sm[rl * N + bitrev(k, logN)] = make_float2(ye.x - yo.y, ye.y + yo.x);
+      sm[rl * N + fft_in_pos(k, N)] = make_float2(ye.x - yo.y, ye.y + yo.x);
     }
     __syncthreads();
-    smem_fft_dit(sm, N, nr, N, 1, +1.0f, P.tw);
+    smem_fft(sm, N, nr, +1.0f, P.tw, P.tw3);
     // p(2n) = Re z(n), p(2n+1) = Im z(n); keep v = (j - N/2) mod 2N.
     for (int t = threadIdx.x; t < nr * N; t += blockDim.x) {
       const int rl = t / N, j = t - rl * N;
       const int v = (j - N / 2 + m) % m;
       const float2 zz = sm[rl * N + (v >> 1)];
       const float p = ((v & 1) ? zz.y : zz.x) * scale_b;
-      sm2[rl * N + bitrev(j, logN)] = make_float2(p, 0.f);
+      sm2[rl * N + fft_in_pos(j, N)] = make_float2(p, 0.f);
     }
     __syncthreads();
-    smem_fft_dit(sm2, N, nr, N, 1, -1.0f, P.tw);
+    smem_fft(sm2, N, nr, -1.0f, P.tw, P.tw3);
     for (int t = threadIdx.x; t < nr * (N / 2 + 1); t += blockDim.x) {
       const int rl = t / (N / 2 + 1), k = t - rl * (N / 2 + 1);
       S[(size_t)(i0 + rl) * LDS + k] = sm2[rl * N + k];
@@ -207,10 +207,10 @@ __device__ void build_one(const ProjParams& P, int dir, int slot, float2* S, flo
     const int nc = min(kColBatch, HC - c0);
     for (int t = threadIdx.x; t < nc * N; t += blockDim.x) {
       const int r = t / nc, cl = t - r * nc;
-      sm[cl * N + bitrev(r, logN)] = S[(size_t)r * LDS + c0 + cl];
+      sm[cl * N + fft_in_pos(r, N)] = S[(size_t)r * LDS + c0 + cl];
     }
     __syncthreads();
-    smem_fft_dit(sm, N, nc, N, 1, -1.0f, P.tw);
+    smem_fft(sm, N, nc, -1.0f, P.tw, P.tw3);
     for (int t = threadIdx.x; t < nc * N; t += blockDim.x) {
       const int r = t / nc, cl = t - r * nc;
       S[(size_t)r * LDS + c0 + cl] = sm[cl * N + r];
@@ -243,10 +243,10 @@ __device__ void build_one(const ProjParams& P, int dir, int slot, float2* S, flo
       const int kx = c0 + cl;
       const int ky = r < N / 2 ? r : r - N;
       const int bin = (int)rintf(sqrtf((float)(ky * ky + kx * kx)));
-      sm[cl * N + bitrev(r, logN)] = cscale(S[(size_t)r * LDS + kx], s_div[bin]);
+      sm[cl * N + fft_in_pos(r, N)] = cscale(S[(size_t)r * LDS + kx], s_div[bin]);
     }
     __syncthreads();
-    smem_fft_dit(sm, N, nc, N, 1, +1.0f, P.tw);
+    smem_fft(sm, N, nc, +1.0f, P.tw, P.tw3);
     for (int t = threadIdx.x; t < nc * N; t += blockDim.x) {
       const int r = t / nc, cl = t - r * nc;
       S[(size_t)r * LDS + c0 + cl] = sm[cl * N + r];
@@ -266,10 +266,10 @@ __device__ void build_one(const ProjParams& P, int dir, int slot, float2* S, flo
       if (k == 0 || k == N / 2) y = make_float2(G[k].x, 0.f);
       else if (k < N / 2) y = G[k];
       else y = cconj(G[N - k]);
-      sm[rl * N + bitrev(k, logN)] = y;
+      sm[rl * N + fft_in_pos(k, N)] = y;
     }
     __syncthreads();
-    smem_fft_dit(sm, N, nr, N, 1, +1.0f, P.tw);
+    smem_fft(sm, N, nr, +1.0f, P.tw, P.tw3);
     for (int t = threadIdx.x; t < nr * N; t += blockDim.x) {
       const int rl = t / N, j = t - rl * N;
       const int i = i0 + rl;
@@ -327,10 +327,10 @@ __device__ void build_one(const ProjParams& P, int dir, int slot, float2* S, flo
       double v = ((double)S[(size_t)i * LDS + j].x - (pc0 * i + pc1 * j + pc2) - mean) * inv_sd;
       float f = (float)v;
       if (P.mask != nullptr) f *= P.mask[(size_t)i * N + j];
-      sm[rl * N + bitrev(j, logN)] = make_float2(f, 0.f);
+      sm[rl * N + fft_in_pos(j, N)] = make_float2(f, 0.f);
     }
     __syncthreads();
-    smem_fft_dit(sm, N, nr, N, 1, -1.0f, P.tw);
+    smem_fft(sm, N, nr, -1.0f, P.tw, P.tw3);
     for (int t = threadIdx.x; t < nr * HC; t += blockDim.x) {
       const int rl = t / HC, k = t - rl * HC;
       S[(size_t)(i0 + rl) * LDS + k] = sm[rl * N + k];
@@ -342,10 +342,10 @@ __device__ void build_one(const ProjParams& P, int dir, int slot, float2* S, flo
     const int nc = min(kColBatch, HC - c0);
     for (int t = threadIdx.x; t < nc * N; t += blockDim.x) {
       const int r = t / nc, cl = t - r * nc;
-      sm[cl * N + bitrev(r, logN)] = S[(size_t)r * LDS + c0 + cl];
+      sm[cl * N + fft_in_pos(r, N)] = S[(size_t)r * LDS + c0 + cl];
     }
     __syncthreads();
-    smem_fft_dit(sm, N, nc, N, 1, -1.0f, P.tw);
+    smem_fft(sm, N, nc, -1.0f, P.tw, P.tw3);
     for (int t = threadIdx.x; t < nc * N; t += blockDim.x) {
       const int r = t / nc, cl = t - r * nc;
       S[(size_t)r * LDS + c0 + cl] = sm[cl * N + r];
@@ -426,13 +426,13 @@ cudaError_t launch_project_templates(cudaStream_t st, const float2* spectrum, co
                                      const int* dirs, int n_build, const int* out_slot,
                                      const float* mask, const float* fsc, const int* bin_list,
                                      const int* bin_ptr, const float* bin_count, int n_bins,
-                                     const float2* tw, float2* bank, float2* scratch, int grid,
-                                     int N, int nb) {
+                                     const float2* tw, const float2* tw3, float2* bank, float2* scratch,
+                                     int grid, int N, int nb) {
   if (n_build <= 0) return cudaSuccess;
   ProjParams P;
   P.spectrum = spectrum; P.rot = rot; P.dirs = dirs; P.n_build = n_build; P.mask = mask;
   P.fsc = fsc; P.bin_list = bin_list; P.bin_ptr = bin_ptr; P.bin_count = bin_count;
-  P.n_bins = n_bins; P.tw = tw; P.bank = bank; P.out_slot = out_slot; P.scratch = scratch; P.planes = nullptr;
+  P.n_bins = n_bins; P.tw = tw; P.tw3 = tw3; P.bank = bank; P.out_slot = out_slot; P.scratch = scratch; P.planes = nullptr;
   P.scratch_stride = project_scratch_elems(N, nb); P.N = N; P.nb = nb;
   const size_t smem = project_smem_bytes(N, n_bins);
   static size_t set_smem = 0;
@@ -1138,7 +1138,7 @@ cudaError_t launch_project_templates_fast(cudaStream_t st, const float2* spectru
   ProjParams P;
   P.spectrum = spectrum; P.rot = rot; P.dirs = dirs; P.n_build = n_build; P.mask = mask;
   P.fsc = fsc; P.bin_list = bin_list; P.bin_ptr = bin_ptr; P.bin_count = bin_count;
-  P.n_bins = n_bins; P.tw = tw; P.bank = bank; P.out_slot = out_slot; P.scratch = nullptr;
+  P.n_bins = n_bins; P.tw = tw; P.tw3 = nullptr; P.bank = bank; P.out_slot = out_slot; P.scratch = nullptr;
   P.scratch_stride = 0; P.N = N; P.nb = nb; P.planes = nullptr;
   switch (N) {
     case 32: return launch_fast<32>(P, grid, planes, blocked, st);

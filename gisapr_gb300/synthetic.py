@@ -305,6 +305,11 @@ WORKLOADS = {
                                fsc_half_res=None, mask_edge=3),
     "box64_small": WorkloadSpec("box64_small", 64, 1.5, 760, 3030, 48, 2, 15.0, 15.0, 4,
                                 fsc_half_res=8.0),
+    "box96_tiny": WorkloadSpec("box96_tiny", 96, 2.0, 300, 900, 16, 1, 30.0, 15.0, 3,
+                               fsc_half_res=8.0, mask_edge=3),
+    # the serving stream's other box sizes (3 * 2^k)
+    "box96_serve": WorkloadSpec("box96_serve", 96, 1.1, 1000, 8000, 1000, 3, 10.0, 7.5, 5),
+    "box192_serve": WorkloadSpec("box192_serve", 192, 1.1, 6000, 20000, 2000, 3, 10.0, 7.5, 5),
 }
 
 

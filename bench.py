@@ -313,7 +313,7 @@ def run_precision(args, device):
     return out
 
 
-SERVE_JOBS = (("box64_small", 2000), ("box128_5kp", 1000), ("box128_5kp", 2500))  # (workload, particles)
+SERVE_JOBS = (("box96_serve", 2000), ("box128_5kp", 2500), ("box192_serve", 1000))  # (workload, particles)
 
 
 def run_serving(args, device):
@@ -347,11 +347,11 @@ def run_serving(args, device):
     n_req = args.serve_requests
     jids = sorted(jobs)
     req_job = [jids[int(i)] for i in rng.integers(0, len(jids), size=n_req)]
-    req_n = [int(x) for x in rng.integers(1, 17, size=n_req)]
+    req_n = [int(x) for x in rng.integers(1, 65, size=n_req)]
     req_poses = [syn.candidate_poses(k, args.seed + 9000 + i, 5.0, 3.0) for i, k in enumerate(req_n)]
-    gaps = rng.exponential(0.010, size=n_req)  # mean 10 ms between arrivals
+    gaps = rng.exponential(0.100, size=n_req)  # mean 100 ms between arrivals (about 0.3k candidates/s offered)
     arrive = np.cumsum(gaps)
-    max_batch = 32
+    max_batch = 64
     with ScoringServer(device, hbm_cap_bytes=150e9, max_batch=max_batch, n_workers=3, precision="fp16x3") as srv:
         for jid in jids:
             cfg, data, spec = jobs[jid]
@@ -405,7 +405,7 @@ def run_serving(args, device):
     return {
         "requests": n_req, "candidates": total, "jobs": [f"{n}: {p} particles" for n, p in SERVE_JOBS],
         "drivers": 4, "workers": 3, "max_batch": max_batch, "precision": "fp16x3",
-        "arrivals": "Poisson, mean gap 10 ms, 1-16 candidates per request",
+        "arrivals": "Poisson, mean gap 100 ms, 1-64 candidates per request",
         "value": total / wall, "unit": UNIT, "wall_s": wall,
         "latency_ms": {"p50": st.latency_ms_p50, "p99": st.latency_ms_p99},
         "batches": st.batches, "mean_batch": st.mean_batch,

@@ -561,7 +561,7 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
         "roofline": roofline,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 12 * 8,
                 "d2h_bytes_per_step": 8 + 4 * len(job.records)},
-        "gpu_launches": ScoringJob.KERNELS_PER_CANDIDATE * K,
+        "gpu_launches": job.launches_per_candidate() * K,
         "clocks": clk,
         "setup_s": {"synthetic_data": t_data, "job": job.setup_s},
         "score_sample": scores[0],

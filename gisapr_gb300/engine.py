@@ -176,8 +176,19 @@ class ScoringJob:
         self._alloc_search_buffers()
 
     # ------------------------------------------------------------------
-    # launches of this engine per scored candidate (cuFFT's own kernels not counted)
-    KERNELS_PER_CANDIDATE = 6
+    # launches of this engine per scored candidate at box <= 128 (cuFFT's own
+    # kernels not counted): atoms + splat, blocked spectrum copy + slice rows +
+    # template tail, correlation, records, score sum
+    KERNELS_PER_CANDIDATE = 8
+
+    @staticmethod
+    def projector_launches(box: int) -> int:
+        """Kernels of one projector call: three in the shared-memory path
+        (powers of two up to 128), one in the general path."""
+        return 3 if box <= 128 and box & (box - 1) == 0 else 1
+
+    def launches_per_candidate(self) -> int:
+        return 5 + self.projector_launches(self.cfg.box)
     STAGES = ("density", "volume_fft", "templates", "correlate", "records")
 
     def enqueue(self, pose_device: torch.Tensor, write_volume: Optional[torch.Tensor] = None,
@@ -414,13 +425,14 @@ class BatchScoringJob:
         if self.precision != "fp32" and int(self.tc_status.item()) != 0:
             raise RuntimeError("tensor-core correlation: an on-chip barrier wait ran out; results are incomplete")
 
-    KERNELS_PER_CANDIDATE = 3  # splat (2 launches) and projector, per slot
     KERNELS_PER_BATCH = 3      # correlation, records, score sums
 
     def launches_per_batch(self) -> int:
-        # fp16 hi/lo bank copy and tensor-core kernel per chunk instead of one plain kernel
+        # per slot: splat (2 launches) and the projector; fp16 hi/lo bank copy
+        # and tensor-core kernel per chunk instead of one plain kernel
+        per_slot = 2 + ScoringJob.projector_launches(self.job.cfg.box)
         extra = 2 * len(self.tc_chunks) - 1 if self.precision != "fp32" else 0
-        return self.n_cand * self.KERNELS_PER_CANDIDATE + self.KERNELS_PER_BATCH + extra
+        return self.n_cand * per_slot + self.KERNELS_PER_BATCH + extra
 
     def enqueue(self, marks: Optional[list] = None, n_active: Optional[int] = None) -> None:
         """Enqueue the whole batch on the current stream (poses already on the device).

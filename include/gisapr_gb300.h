@@ -115,8 +115,8 @@ int gisapr_volume_spectrum(gisapr_ctx ctx, void* stream, const float* volume, in
  * direction indices, out_slot [n_build] int32 rows of ``bank`` to write (NULL:
  * row = dirs[i]), mask [box][box] float32 or NULL, fsc [newbox][newbox/2+1]
  * float32 packed FSC, bank [..][newbox][newbox/2+1] complex pre-shifted
- * packed templates. box: power of two, 32..256; newbox: even, <= box,
- * multiple of 16.
+ * packed templates. box: power of two, 32..256, or 96 or 192; newbox:
+ * even, <= box, multiple of 16.
  */
 int gisapr_project_templates(gisapr_ctx ctx, void* stream, const float* spectrum, int box,
                              const float* rot, const int* dirs, int n_build, const int* out_slot,
@@ -202,7 +202,7 @@ int gisapr_get_tuning(gisapr_ctx ctx, int key, int size, int* value);
  *     match the correlation call);
  *   status: device int, set to 1 if an on-chip barrier wait ran out (the
  *     outputs are then incomplete); the caller zeroes it.
- * Sizes: n in {32, 64, 128, 256}, crop even in 2..14 (10..14 at n = 256),
+ * Sizes: n in {32, 64, 96, 128, 192, 256}, crop even in 2..14 (10..14 at n = 256),
  * n_cand <= 128 per call (the
  * work list is planned for that n_cand: a tile holds 128 / ceil8(n_cand)
  * whole directions).

@@ -13,9 +13,10 @@
 //   stage 2 (cols):  raw(y, x) = sum_c Re[Z(y, c) w_c w_n^{c x}].
 // One thread-block cluster per particle splits the H columns over its CTAs;
 // each CTA keeps its columns of all psi spectra of the particle in shared
-// memory, reads templates from L2, and the column partials of every map are
-// summed over distributed shared memory by the cluster's rank-0 CTA, which
-// takes the row-major first maximum. Per-map translation maps never reach HBM.
+// memory (loaded with asynchronous copies), reads templates from L2, and the
+// column partials of every map are summed over distributed shared memory by
+// one CTA of the cluster (maps dealt out by rank), which takes the row-major
+// first maximum. Per-map translation maps never reach HBM.
 #include <cooperative_groups.h>
 
 #include "common.cuh"
@@ -43,6 +44,16 @@ struct CorrParams {
   long long bank_stride;   // complex elements between candidates' banks
   int nnz;                 // entries of the CSR (output stride per candidate)
 };
+
+// 8-byte asynchronous global-to-shared copy with an L2 evict-first hint:
+// the particle spectra are read once per launch and should not push the
+// templates out of L2.
+__device__ __forceinline__ void cp_async8_stream(void* dst, const void* src, uint64_t policy) {
+  asm volatile("cp.async.ca.shared.global.L2::cache_hint [%0], [%1], 8, %2;" ::"r"(
+                   (uint32_t)__cvta_generic_to_shared(dst)),
+               "l"(src), "l"(policy)
+               : "memory");
+}
 
 __host__ __device__ inline int col_lo(int H, int K, int r) {
   const int base = H / K, extra = H % K;
@@ -73,12 +84,16 @@ __global__ void __launch_bounds__(kThreads) correlate_plain(CorrParams P) {
 
   for (int t = threadIdx.x; t < M * C; t += blockDim.x) s_two[t] = P.tw_outer[t];
   for (int t = threadIdx.x; t < cw * C; t += blockDim.x) s_twc[t] = P.tw_col[(size_t)clo * C + t];
+  // the particle's columns, all copies in flight at once (one wait)
   const float2* Pb = P.stack + (size_t)b * n_psi * n * H;
-  for (int t = threadIdx.x; t < n_psi * n * cw; t += blockDim.x) {
-    const int cl = t % cw, rr = t / cw;  // rr = psi * n + r
-    // read once per candidate: streaming loads, so the particle stack does
-    // not push the templates out of L2
-    Pq[(size_t)rr * cwmax + cl] = __ldcs(Pb + (size_t)rr * H + clo + cl);
+  {
+    uint64_t policy;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(policy));
+    for (int t = threadIdx.x; t < n_psi * n * cw; t += blockDim.x) {
+      const int cl = t % cw, rr = t / cw;  // rr = psi * n + r
+      cp_async8_stream(Pq + (size_t)rr * cwmax + cl, Pb + (size_t)rr * H + clo + cl, policy);
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
   }
   __syncthreads();
 
@@ -139,11 +154,13 @@ __global__ void __launch_bounds__(kThreads) correlate_plain(CorrParams P) {
       }
       __syncthreads();
     }
-    // ---- cluster reduction and first-maximum search (rank 0)
+    // ---- cluster reduction and first-maximum search: the maps are dealt
+    // out to the cluster's CTAs (map mp to rank mp mod K), each sums the K
+    // partials of its maps over distributed shared memory in rank order
     cluster.sync();
-    if (rank == 0) {
+    {
       const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-      for (int mp = warp; mp < dsg * n_psi; mp += nw) {
+      for (int mp = rank + K * warp; mp < dsg * n_psi; mp += K * nw) {
         float best = -INFINITY;
         int bi = CC;
         for (int e = lane; e < CC; e += 32) {

@@ -178,7 +178,7 @@ def test_tensor_path_rejects_unsupported_sizes(golden32):
     st = nat.stream_of(DEV)
     buf = torch.zeros(1 << 20, dtype=torch.uint8, device=DEV)
     p = nat.ptr(buf)
-    for n, crop, n_psi in [(512, 12, 3), (128, 16, 3), (96, 12, 3), (256, 8, 3)]:
+    for n, crop, n_psi in [(512, 12, 3), (128, 16, 3), (80, 12, 3), (256, 8, 3)]:
         with pytest.raises(ValueError):
             nat.call("gisapr_correlate_tc_batch", ctx, st, p, 0, 1, 1, p, p, p, p, p, 1, 1, n_psi, n, crop, 1,
                      p, p, p, p)

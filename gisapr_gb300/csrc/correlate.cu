@@ -248,17 +248,33 @@ __global__ void particle_results(const int* __restrict__ local_ptr, const float*
 }
 
 // sum over particles with at least one direction of exp(peak / 1024), FP64,
-// fixed summation order (one CTA).
-__global__ void score_sum(const int* __restrict__ local_ptr, const float* __restrict__ peak,
-                          int n_particles, double* __restrict__ out) {
+// fixed summation order. One cluster of kScoreCtas CTAs per candidate (on
+// different SMs: GB300's FP64 rate is low, so one SM would spend tens of
+// microseconds on the exponentials); CTA r sums a contiguous range of
+// particles and rank 0 adds the partials in rank order.
+constexpr int kScoreCtas = 8;
+
+__global__ void __launch_bounds__(256) score_sum(const int* __restrict__ local_ptr, const float* __restrict__ peak,
+                                                 int n_particles, double* __restrict__ out) {
   __shared__ double red[32];
-  peak += (size_t)blockIdx.x * n_particles;  // candidate blockIdx.x
-  out += blockIdx.x;
+  __shared__ double part;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank(), cand = blockIdx.x / kScoreCtas;
+  peak += (size_t)cand * n_particles;
+  const int per = (n_particles + kScoreCtas - 1) / kScoreCtas;
+  const int p0 = rank * per, p1 = min(n_particles, p0 + per);
   double acc = 0.0;
-  for (int p = threadIdx.x; p < n_particles; p += blockDim.x)
+  for (int p = p0 + threadIdx.x; p < p1; p += blockDim.x)
     if (local_ptr[p + 1] > local_ptr[p]) acc += exp((double)peak[p] / 1024.0);
   acc = block_sum_d(acc, red);
-  if (threadIdx.x == 0) *out = acc;
+  if (threadIdx.x == 0) part = acc;
+  cluster.sync();
+  if (rank == 0 && threadIdx.x == 0) {
+    double t = 0.0;
+    for (int r = 0; r < kScoreCtas; ++r) t += *cluster.map_shared_rank(&part, r);
+    out[cand] = t;
+  }
+  cluster.sync();
 }
 
 }  // namespace
@@ -344,6 +360,16 @@ cudaError_t launch_particle_results(cudaStream_t st, const int* local_ptr, const
 cudaError_t launch_score_sum(cudaStream_t st, const int* local_ptr, const float* peak, int n_particles,
                              double* out, int n_cand) {
   if (n_cand <= 0) return cudaSuccess;
-  score_sum<<<n_cand, 1024, 0, st>>>(local_ptr, peak, n_particles, out);
-  return cudaGetLastError();
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(n_cand * kScoreCtas));
+  cfg.blockDim = dim3(256);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = kScoreCtas;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, score_sum, local_ptr, peak, n_particles, out);
 }

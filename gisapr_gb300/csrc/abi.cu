@@ -133,6 +133,10 @@ struct gisapr_context {
   std::map<int, BinTable> bins;                        // N -> radial bins
   std::map<std::pair<int, int>, CorrTables> corr;      // (n, crop) -> twiddles
   DeviceBuffer atoms, bin_counts, bin_lists, proj_scratch, prep_scratch, proj_slices, proj_blocked;
+  // Buffers replaced by larger ones. They are freed only with the context:
+  // a CUDA graph captured before a buffer grew still names the old one, and
+  // that buffer stays valid (and large enough for the graph's own sizes).
+  std::vector<void*> retired;
   int sm_count = 152;
   std::map<int, int> tune_corr_cluster;  // n -> CTAs per particle in the plain correlation
 };
@@ -144,9 +148,9 @@ int set_device(gisapr_ctx ctx) {
   return GISAPR_OK;
 }
 
-int ensure(DeviceBuffer& b, size_t bytes, const char* what) {
+int ensure(gisapr_ctx ctx, DeviceBuffer& b, size_t bytes, const char* what) {
   if (b.bytes >= bytes) return GISAPR_OK;
-  if (b.ptr) cudaFree(b.ptr);
+  if (b.ptr) ctx->retired.push_back(b.ptr);
   b.ptr = nullptr;
   b.bytes = 0;
   cudaError_t e = cudaMalloc(&b.ptr, bytes);
@@ -349,6 +353,7 @@ int gisapr_context_destroy(gisapr_ctx ctx) {
   cudaFree(ctx->proj_blocked.ptr);
   cudaFree(ctx->prep_scratch.ptr);
   cudaFree(ctx->tw);
+  for (void* p : ctx->retired) cudaFree(p);
   cudaFree(ctx->tw3);
   delete ctx;
   return GISAPR_OK;
@@ -369,12 +374,12 @@ static int deposit_common(gisapr_ctx ctx, void* stream, const float* xyz, const 
   int rc = set_device(ctx);
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
-  rc = ensure(ctx->atoms, (size_t)(n > 0 ? n : 1) * atom_record_bytes(), "cudaMalloc(atoms)");
+  rc = ensure(ctx, ctx->atoms, (size_t)(n > 0 ? n : 1) * atom_record_bytes(), "cudaMalloc(atoms)");
   if (rc) return rc;
   const size_t nbricks = (size_t)splat_bin_count(box);
-  rc = ensure(ctx->bin_counts, nbricks * sizeof(int), "cudaMalloc(brick counts)");
+  rc = ensure(ctx, ctx->bin_counts, nbricks * sizeof(int), "cudaMalloc(brick counts)");
   if (rc) return rc;
-  rc = ensure(ctx->bin_lists, nbricks * splat_bin_cap() * sizeof(int), "cudaMalloc(brick lists)");
+  rc = ensure(ctx, ctx->bin_lists, nbricks * splat_bin_cap() * sizeof(int), "cudaMalloc(brick lists)");
   if (rc) return rc;
   GISAPR_CHECK_CUDA(launch_splat_binned(st, xyz, numbers, n, transform, pivot, rot, shift, initial, out, padded,
                                         box, width, apix, rp, kn, ctx->atoms.ptr, (int*)ctx->bin_counts.ptr,
@@ -449,9 +454,9 @@ int gisapr_project_templates(gisapr_ctx ctx, void* stream, const float* spectrum
     // whole template in shared memory, one CTA per SM
     const int grid = grid_for(ctx, n_build, 1);
     if (n_build > 65535) return fail(GISAPR_ERR_ARGUMENT, "at most 65535 templates per call");
-    rc = ensure(ctx->proj_slices, project_slice_elems(box, n_build) * sizeof(float2), "cudaMalloc(planes)");
+    rc = ensure(ctx, ctx->proj_slices, project_slice_elems(box, n_build) * sizeof(float2), "cudaMalloc(planes)");
     if (rc) return rc;
-    rc = ensure(ctx->proj_blocked, project_blocked_elems(box) * sizeof(float2), "cudaMalloc(blocked spectrum)");
+    rc = ensure(ctx, ctx->proj_blocked, project_blocked_elems(box) * sizeof(float2), "cudaMalloc(blocked spectrum)");
     if (rc) return rc;
     GISAPR_CHECK_CUDA(launch_project_templates_fast((cudaStream_t)stream, (const float2*)spectrum, rot, dirs,
                                                     n_build, out_slot, mask, fsc, bt.list, bt.ptr, bt.count,
@@ -461,7 +466,7 @@ int gisapr_project_templates(gisapr_ctx ctx, void* stream, const float* spectrum
     return GISAPR_OK;
   }
   const int grid = grid_for(ctx, n_build, 2);
-  rc = ensure(ctx->proj_scratch, (size_t)grid * project_scratch_elems(box, newbox) * sizeof(float2),
+  rc = ensure(ctx, ctx->proj_scratch, (size_t)grid * project_scratch_elems(box, newbox) * sizeof(float2),
               "cudaMalloc(projector scratch)");
   if (rc) return rc;
   GISAPR_CHECK_CUDA(launch_project_templates((cudaStream_t)stream, (const float2*)spectrum, rot, dirs, n_build,
@@ -500,7 +505,7 @@ int gisapr_prepare_particles(gisapr_ctx ctx, void* stream, const float* images, 
   rc = set_device(ctx);
   if (rc) return rc;
   const int grid = grid_for(ctx, n * n_psi, 4);
-  rc = ensure(ctx->prep_scratch, (size_t)grid * prepare_scratch_elems(box, newbox) * sizeof(float2),
+  rc = ensure(ctx, ctx->prep_scratch, (size_t)grid * prepare_scratch_elems(box, newbox) * sizeof(float2),
               "cudaMalloc(particle scratch)");
   if (rc) return rc;
   GISAPR_CHECK_CUDA(launch_prepare_particles((cudaStream_t)stream, images, n, n_psi, psi_index, psi_table, mask,

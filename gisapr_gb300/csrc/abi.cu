@@ -465,7 +465,9 @@ int gisapr_project_templates(gisapr_ctx ctx, void* stream, const float* spectrum
                       "project_templates");
     return GISAPR_OK;
   }
-  const int grid = grid_for(ctx, n_build, 2);
+  // CTAs per SM of the general path (measured on GB300): smaller boxes fill
+  // the SM with more CTAs while their scratch planes still fit L2
+  const int grid = grid_for(ctx, n_build, box == 96 ? 6 : (box == 192 ? 3 : 2));
   rc = ensure(ctx, ctx->proj_scratch, (size_t)grid * project_scratch_elems(box, newbox) * sizeof(float2),
               "cudaMalloc(projector scratch)");
   if (rc) return rc;

@@ -42,20 +42,23 @@ GISAPR_DEV int bitrev(int i, int logn) { return (int)(__brev((unsigned)i) >> (32
 // ---------------------------------------------------------------------------
 GISAPR_DEV void smem_fft_dit(float2* buf, int L, int lines, int line_stride, int elem_stride,
                              float sign, const float2* __restrict__ tw) {
-  const int half_total = L >> 1;
+  // L, the butterfly span and the twiddle step are powers of two: the index
+  // arithmetic is shifts and masks
+  const int log_ht = ilog2_pow2(L) - 1, half_total = L >> 1;
   const int work = lines * half_total;
-  for (int half = 1; half < L; half <<= 1) {
-    const int twstep = kMaxFftLen / (half << 1);
+  constexpr int kLogMax = 9;  // log2(kMaxFftLen)
+  static_assert((1 << kLogMax) == kMaxFftLen, "twiddle table length");
+  for (int lh = 0, half = 1; half < L; ++lh, half <<= 1) {
+    const int tw_shift = kLogMax - 1 - lh;  // twiddle step kMaxFftLen / (2 half)
     for (int t = threadIdx.x; t < work; t += blockDim.x) {
-      const int line = t / half_total;
-      const int b = t - line * half_total;
-      const int group = b / half;
-      const int k = b - group * half;
-      const int i = group * (half << 1) + k;
+      const int line = t >> log_ht;
+      const int b = t & (half_total - 1);
+      const int k = b & (half - 1);
+      const int i = ((b >> lh) << (lh + 1)) + k;
       float2* base = buf + line * line_stride;
       float2 u = base[i * elem_stride];
       float2 v = base[(i + half) * elem_stride];
-      float2 w = tw[k * twstep];
+      float2 w = tw[k << tw_shift];
       float2 vt = cmul_sign(v, w, -sign);  // tw is exp(-..): sign=-1 keeps it, +1 conjugates
       base[i * elem_stride] = cadd(u, vt);
       base[(i + half) * elem_stride] = csub(u, vt);

@@ -115,9 +115,11 @@ __device__ __forceinline__ float grid_pixel(float c, int size) {
   return pix;
 }
 
+template <int N>
 __device__ void build_one(const ProjParams& P, int dir, int slot, float2* S, float2* Pk,
                           float2* sm, double* red, float* s_div, double* s_coef) {
-  const int N = P.N, m = 2 * N, W = N + 1, nb = P.nb, H = nb / 2 + 1;
+  constexpr int m = 2 * N, W = N + 1;
+  const int nb = P.nb, H = nb / 2 + 1;
   const int LDS = N + 1;  // scratch row stride (complex)
   const float* R = P.rot + (size_t)dir * 9;
   const float R00 = R[0], R01 = R[1], R10 = R[3], R11 = R[4], R20 = R[6], R21 = R[7];
@@ -380,10 +382,10 @@ __device__ void build_one(const ProjParams& P, int dir, int slot, float2* S, flo
   __syncthreads();
 }
 
+template <int N>
 __global__ void __launch_bounds__(kThreads) project_templates(ProjParams P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* sm = reinterpret_cast<float2*>(smem_raw);
-  const int N = P.N;
   const int line_elems = max(2 * kLineCols * N, 2 * kRowBatch * N);
   const int lines = max(line_elems, kColBatch * N);
   float2* s_tw = sm + lines;
@@ -399,7 +401,7 @@ __global__ void __launch_bounds__(kThreads) project_templates(ProjParams P) {
   for (int b = blockIdx.x; b < P.n_build; b += gridDim.x) {
     const int dir = P.dirs[b];
     const int slot = P.out_slot ? P.out_slot[b] : dir;
-    build_one(Q, dir, slot, S, Pk, sm, red, s_div, s_coef);
+    build_one<N>(Q, dir, slot, S, Pk, sm, red, s_div, s_coef);
   }
 }
 
@@ -422,6 +424,19 @@ size_t project_smem_bytes(int N, int n_bins) {
          (size_t)(n_bins + 4) * sizeof(float);
 }
 
+template <int N>
+static cudaError_t launch_general(const ProjParams& P, int grid, size_t smem, cudaStream_t st) {
+  static size_t set_smem = 0;  // attribute set once per size, never inside a stream capture
+  if (set_smem < smem) {
+    cudaError_t e = cudaFuncSetAttribute(project_templates<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    set_smem = smem;
+  }
+  project_templates<N><<<grid, kThreads, smem, st>>>(P);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_project_templates(cudaStream_t st, const float2* spectrum, const float* rot,
                                      const int* dirs, int n_build, const int* out_slot,
                                      const float* mask, const float* fsc, const int* bin_list,
@@ -435,15 +450,12 @@ cudaError_t launch_project_templates(cudaStream_t st, const float2* spectrum, co
   P.n_bins = n_bins; P.tw = tw; P.tw3 = tw3; P.bank = bank; P.out_slot = out_slot; P.scratch = scratch; P.planes = nullptr;
   P.scratch_stride = project_scratch_elems(N, nb); P.N = N; P.nb = nb;
   const size_t smem = project_smem_bytes(N, n_bins);
-  static size_t set_smem = 0;
-  if (set_smem < smem) {
-    cudaError_t e = cudaFuncSetAttribute(project_templates, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e != cudaSuccess) return e;
-    set_smem = smem;
+  switch (N) {
+    case 96: return launch_general<96>(P, grid, smem, st);
+    case 192: return launch_general<192>(P, grid, smem, st);
+    case 256: return launch_general<256>(P, grid, smem, st);
+    default: return cudaErrorInvalidValue;  // powers of two up to 128 take the shared-memory path
   }
-  project_templates<<<grid, kThreads, smem, st>>>(P);
-  return cudaGetLastError();
 }
 
 // ===========================================================================

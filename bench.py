@@ -472,8 +472,11 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
     lat = sorted(step_ev[i].elapsed_time(step_ev[i + 1]) for i in range(K))
     stage_ms = {s: statistics.mean(a.elapsed_time(b) for a, b in v) for s, v in stage_events.items()}
 
-    # ---- end to end through the public API, host buffers each step
+    # ---- end to end through the public API, host buffers each step (two
+    # untimed calls first: the second captures the call's launch sequence)
     peaks_host = torch.empty(len(job.records), dtype=torch.float32).pin_memory()
+    for _ in range(2):
+        job.score(poses[0])
     barrier()
     torch.cuda.synchronize(device)
     e0 = torch.cuda.Event(enable_timing=True)

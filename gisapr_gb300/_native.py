@@ -109,8 +109,18 @@ TUNE_CORR_CLUSTER = 1  # gisapr_set_tuning keys (include/gisapr_gb300.h)
 DEFAULT_TUNING: dict = {}
 
 
+_TUNING_VERSION = [0]
+
+
+def tuning_version() -> int:
+    """Changes whenever set_default_tuning does (captured launch sequences
+    taken before then use the old launch shapes and must be re-captured)."""
+    return _TUNING_VERSION[0]
+
+
 def set_default_tuning(key: int, size: int, value: int) -> None:
     DEFAULT_TUNING[(int(key), int(size))] = int(value)
+    _TUNING_VERSION[0] += 1
     cache = getattr(Context._per_thread, "ctx", None) or {}
     for ctx in cache.values():
         call("gisapr_set_tuning", ctx.handle, int(key), int(size), int(value))

@@ -14,6 +14,7 @@ run_search (v606:1749-1810) replaced by batched kernels.
 from __future__ import annotations
 
 import ctypes as C
+import threading
 import time
 from dataclasses import dataclass
 from typing import Dict, List, Optional, Sequence
@@ -134,6 +135,11 @@ class ScoringJob:
         self.total = torch.zeros(1, dtype=torch.float64, device=dev)
         self.pose_dev = torch.zeros(12, dtype=torch.float64, device=dev)
         self.pose_host = torch.zeros(12, dtype=torch.float64).pin_memory()
+        # score(): per host thread, the candidate's launch sequence is captured
+        # as a CUDA graph on the second call and replayed after that
+        self.use_graph = True
+        self._graphs: Dict[int, tuple] = {}
+        self._warm: Dict[int, int] = {}
         self.total_host = torch.zeros(1, dtype=torch.float64).pin_memory()
         torch.cuda.synchronize(dev)
         self.setup_s = time.perf_counter() - t0
@@ -174,6 +180,8 @@ class ScoringJob:
         must be rebuilt."""
         self._set_lists(local)
         self._alloc_search_buffers()
+        self._graphs.clear()
+        self._warm.clear()
 
     # ------------------------------------------------------------------
     # launches of this engine per scored candidate at box <= 128 (cuFFT's own
@@ -256,10 +264,40 @@ class ScoringJob:
         """sum_i exp(rawCC_i / 1024) of one pose (degrees, Angstrom)."""
         self.pose_host.copy_(self.density.pose_tensor(pose))
         self.pose_dev.copy_(self.pose_host, non_blocking=True)
-        self.enqueue(self.pose_dev)
+        g = self._score_graph()
+        if g is not None:
+            g.replay()
+        else:
+            self.enqueue(self.pose_dev)
         self.total_host.copy_(self.total, non_blocking=True)
         torch.cuda.current_stream(self.device).synchronize()
         return float(self.total_host[0])
+
+    def _score_graph(self):
+        """The captured launch sequence of score() for this host thread, or
+        None while it runs eagerly: the first call on a thread (and the first
+        after set_local or a tuning change) creates plans, tables and scratch;
+        the second is captured. Replays launch the same kernels on the same
+        buffers, so scores are bitwise those of eager calls."""
+        if not self.use_graph or self.density is None:
+            return None
+        key = threading.get_ident()
+        ver = nat.tuning_version()
+        ent = self._graphs.get(key)
+        if ent is not None and ent[1] == ver:
+            return ent[0]
+        if self._warm.get(key) != ver:
+            self._warm[key] = ver
+            return None
+        cur = torch.cuda.current_stream(self.device)
+        side = torch.cuda.Stream(self.device)
+        side.wait_stream(cur)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=side):
+            self.enqueue(self.pose_dev)
+        cur.wait_stream(side)
+        self._graphs[key] = (g, ver)
+        return g
 
     def score_many(self, poses) -> np.ndarray:
         return np.asarray([self.score(p) for p in poses], dtype=np.float64)

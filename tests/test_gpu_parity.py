@@ -247,6 +247,26 @@ def test_scoring_job_matches_reference(golden32):
     assert job.score(g["pose"]) == score
 
 
+def test_score_graph_replay_equals_eager(golden32):
+    """score() runs eagerly once per thread, then replays a captured launch
+    sequence: the scores equal the eager ones bit for bit, and new direction
+    lists drop the captured sequence."""
+    g = golden32
+    job = _job_from_golden(g)
+    poses = [g["pose"]] + list(syn.candidate_poses(3, 41, 3.0, 1.5, exact=True))
+    job.use_graph = False
+    eager = [job.score(p) for p in poses]
+    job.use_graph = True
+    graphed = [job.score(p) for p in poses] + [job.score(p) for p in poses]
+    assert graphed == eager + eager
+    job.set_local([lst[:1] for lst in job.local])
+    job.use_graph = False
+    eager2 = [job.score(p) for p in poses]
+    job.use_graph = True
+    assert [job.score(p) for p in poses] == eager2
+    assert eager2 != eager
+
+
 def test_scoring_job_box64_published_config(golden64):
     g = golden64
     spec = syn.WORKLOADS["box64_200p"]

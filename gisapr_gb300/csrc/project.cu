@@ -459,15 +459,21 @@ cudaError_t launch_project_templates(cudaStream_t st, const float2* spectrum, co
 }
 
 // ===========================================================================
-// Shared-memory projector for box <= 128.
+// Shared-memory projector for boxes 32, 64 and 128, in three launches:
+// spectrum_blocked (a blocked copy of the half-volume spectrum),
+// rows_inverse (slice gather and pass A at high occupancy, each template's
+// plane written to global memory) and project_templates_smem (passes B-G,
+// one template at a time per CTA, its plane arriving by bulk async copies).
 //
-// The whole per-template working set (the N x (N+1) plane left by the pruned
+// The template's working set (the N x (N+1) plane left by the pruned
 // inverse along rows, then the N x (N/2+1) spectra of the whitening) stays in
 // shared memory. Every 1-D transform is a four-step 16 x (N/16) FFT done by
 // one warp on whole lines: a 16-point register codelet over n1, twiddles,
 // then N/16-point codelets, with only warp barriers inside a pass and block
-// barriers between passes. The arithmetic of every pass is that of the
-// general kernel above (same float32 slice coordinates, same passes A-G).
+// barriers between passes. The passes compute what the general kernel above
+// computes (same float32 slice coordinates); the forward transforms of real
+// rows run two rows per complex line, and the block sums are float32 over a
+// fixed tree.
 // ===========================================================================
 namespace {
 

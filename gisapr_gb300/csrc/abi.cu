@@ -42,6 +42,11 @@ cudaError_t launch_project_templates_fast(cudaStream_t, const float2*, const flo
                                           float2*);
 size_t project_blocked_elems(int N);
 size_t project_slice_elems(int N, int n_build);
+cudaError_t launch_project_templates_planes(cudaStream_t, const float2*, const float*, const int*, int,
+                                            const int*, const float*, const float*, const int*, const int*,
+                                            const float*, int, const float2*, const float2*, float2*, float2*,
+                                            int, int, int, float2*, float2*, int);
+size_t project_flat_plane_elems(int N, int n);
 cudaError_t launch_packed_ctf(cudaStream_t, const float*, const float*, const float*, int,
                               const float*, const float*, const float*, const float*, int, float,
                               float, float, float, float, float*);
@@ -471,6 +476,23 @@ int gisapr_project_templates(gisapr_ctx ctx, void* stream, const float* spectrum
   rc = ensure(ctx, ctx->proj_scratch, (size_t)grid * project_scratch_elems(box, newbox) * sizeof(float2),
               "cudaMalloc(projector scratch)");
   if (rc) return rc;
+  if (box == 256) {
+    // the gather and pass A in their own high-occupancy kernel, from the
+    // blocked spectrum, at most 4,096 planes (2.2 GB) at a time
+    const int chunk = std::min(n_build, 4096);
+    rc = ensure(ctx, ctx->proj_slices, project_flat_plane_elems(box, chunk) * sizeof(float2), "cudaMalloc(planes)");
+    if (rc) return rc;
+    rc = ensure(ctx, ctx->proj_blocked, project_blocked_elems(box) * sizeof(float2), "cudaMalloc(blocked spectrum)");
+    if (rc) return rc;
+    GISAPR_CHECK_CUDA(launch_project_templates_planes((cudaStream_t)stream, (const float2*)spectrum, rot, dirs,
+                                                      n_build, out_slot, mask, fsc, bt.list, bt.ptr, bt.count,
+                                                      bt.n_bins, ctx->tw, ctx->tw3, (float2*)bank,
+                                                      (float2*)ctx->proj_scratch.ptr, grid, box, newbox,
+                                                      (float2*)ctx->proj_slices.ptr, (float2*)ctx->proj_blocked.ptr,
+                                                      chunk),
+                      "project_templates");
+    return GISAPR_OK;
+  }
   GISAPR_CHECK_CUDA(launch_project_templates((cudaStream_t)stream, (const float2*)spectrum, rot, dirs, n_build,
                                              out_slot, mask, fsc, bt.list, bt.ptr, bt.count, bt.n_bins,
                                              ctx->tw, ctx->tw3, (float2*)bank, (float2*)ctx->proj_scratch.ptr, grid,

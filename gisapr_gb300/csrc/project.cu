@@ -49,7 +49,8 @@ struct ProjParams {
   const int* out_slot;      // output row in bank for each build index (null => dirs[i])
   float2* scratch;          // per-CTA scratch
   size_t scratch_stride;    // complex elements per CTA
-  const float2* planes;     // [n_build][N][plane_ld(N)] pass-A planes of the shared-memory path (or null)
+  const float2* planes;     // pass-A planes written by rows_inverse (or null): [n_build][N][plane_ld(N)]
+                            // for the shared-memory path, [n_build][N][N+1] for the general kernel
   int N;
   int nb;
 };
@@ -116,7 +117,7 @@ __device__ __forceinline__ float grid_pixel(float c, int size) {
 }
 
 template <int N>
-__device__ void build_one(const ProjParams& P, int dir, int slot, float2* S, float2* Pk,
+__device__ void build_one(const ProjParams& P, int b, int dir, int slot, float2* S, float2* Pk,
                           float2* sm, double* red, float* s_div, double* s_coef) {
   constexpr int m = 2 * N, W = N + 1;
   const int nb = P.nb, H = nb / 2 + 1;
@@ -125,8 +126,10 @@ __device__ void build_one(const ProjParams& P, int dir, int slot, float2* S, flo
   const float R00 = R[0], R01 = R[1], R10 = R[3], R11 = R[4], R20 = R[6], R21 = R[7];
   const float inv_m = (float)(1.0 / (double)m);
 
-  // ---- pass A: gather + row inverse (pruned to the N centred rows)
-  for (int c0 = 0; c0 < W; c0 += kLineCols) {
+  // ---- pass A: gather + row inverse (pruned to the N centred rows), unless
+  // rows_inverse already wrote this template's plane (P.planes, [N][N+1])
+  const float2* A = P.planes != nullptr ? P.planes + (size_t)b * N * LDS : S;
+  for (int c0 = 0; P.planes == nullptr && c0 < W; c0 += kLineCols) {
     const int nc = min(kLineCols, W - c0);
     const int total = nc * m;
     for (int t = threadIdx.x; t < total; t += blockDim.x) {
@@ -170,7 +173,7 @@ __device__ void build_one(const ProjParams& P, int dir, int slot, float2* S, flo
     const int nr = min(kRowBatch, N - i0);
     for (int t = threadIdx.x; t < nr * N; t += blockDim.x) {
       const int rl = t / N, k = t - rl * N;
-      const float2* Z = S + (size_t)(i0 + rl) * LDS;
+      const float2* Z = A + (size_t)(i0 + rl) * LDS;
       float2 ye, yo;
       if (k == 0) {
         const float a = Z[0].x, b = Z[N].x;
@@ -401,7 +404,7 @@ __global__ void __launch_bounds__(kThreads) project_templates(ProjParams P) {
   for (int b = blockIdx.x; b < P.n_build; b += gridDim.x) {
     const int dir = P.dirs[b];
     const int slot = P.out_slot ? P.out_slot[b] : dir;
-    build_one<N>(Q, dir, slot, S, Pk, sm, red, s_div, s_coef);
+    build_one<N>(Q, b, dir, slot, S, Pk, sm, red, s_div, s_coef);
   }
 }
 
@@ -490,7 +493,11 @@ __host__ __device__ constexpr int pass_a_cols() { return 16 / (N / 16); }
 
 // Row stride (complex elements) of the padded shared-memory plane: holds the
 // N + 1 columns plus one spare slot per 8, chosen by a bank-conflict search.
-__host__ __device__ constexpr int plane_ld(int N) { return N == 128 ? 150 : (N == 64 ? 74 : 38); }
+// Box 256 has no shared-memory plane; its value there is the stride of
+// rows_inverse's staging lines (256 elements plus one spare slot per 8).
+__host__ __device__ constexpr int plane_ld(int N) {
+  return N == 256 ? 290 : (N == 128 ? 150 : (N == 64 ? 74 : 38));
+}
 __host__ __device__ constexpr int plane_rows(int N) { return N + N / 8; }
 
 // Hardware square-root approximation (PTX sqrt.approx.f32, relative error
@@ -1007,8 +1014,15 @@ __device__ void build_one_smem(const ProjParams& P, int slot, float2* Zs, const 
 // inverse (output row (k + N/2) mod N takes frequency k). The CTA then
 // writes its columns row by row into the template's plane in global memory,
 // laid out as the shared-memory plane's rows (row stride plane_ld(N),
-// column c at c + c/8), so the projector loads it with bulk copies.
+// column c at c + c/8), so the projector loads it with bulk copies. For box
+// 256 the plane is the general kernel's unpadded [N][N+1] scratch layout,
+// which that kernel's pass B reads directly.
 constexpr int kRiWarps = 4;
+
+template <int N>
+__host__ __device__ constexpr bool flat_plane() { return N > 128; }
+template <int N>
+__host__ __device__ constexpr int plane_out_ld() { return flat_plane<N>() ? N + 1 : plane_ld(N); }
 
 template <int N>
 __host__ __device__ constexpr int ri_cols() { return kRiWarps * pass_a_cols<N>(); }
@@ -1049,11 +1063,12 @@ __global__ void __launch_bounds__(kRiWarps * 32) rows_inverse(const float2* __re
     }
   }
   __syncthreads();
-  float2* dst = planes + (size_t)b * N * plane_ld(N);
+  constexpr int OUT = plane_out_ld<N>();
+  float2* dst = planes + (size_t)b * N * OUT;
   const int ncta = min(CC, W - c_cta);
   for (int e = threadIdx.x; e < N * CC; e += blockDim.x) {
     const int y = e / CC, cl = e - y * CC, c = c_cta + cl;
-    if (cl < ncta) dst[(size_t)y * plane_ld(N) + c + (c >> 3)] = s_out[y][cl];
+    if (cl < ncta) dst[(size_t)y * OUT + (flat_plane<N>() ? c : c + (c >> 3))] = s_out[y][cl];
   }
 }
 
@@ -1165,3 +1180,39 @@ cudaError_t launch_project_templates_fast(cudaStream_t st, const float2* spectru
     default: return cudaErrorInvalidValue;
   }
 }
+
+// Box 256: the slice gather and pass A run in rows_inverse from the blocked
+// spectrum (its plane [N][N+1] written to global memory, ``chunk`` templates
+// at a time), passes B-G in the general kernel, which reads those planes.
+cudaError_t launch_project_templates_planes(cudaStream_t st, const float2* spectrum, const float* rot,
+                                            const int* dirs, int n_build, const int* out_slot,
+                                            const float* mask, const float* fsc, const int* bin_list,
+                                            const int* bin_ptr, const float* bin_count, int n_bins,
+                                            const float2* tw, const float2* tw3, float2* bank, float2* scratch,
+                                            int grid, int N, int nb, float2* planes, float2* blocked, int chunk) {
+  constexpr int kN = 256, CC = ri_cols<kN>();
+  if (n_build <= 0) return cudaSuccess;
+  if (N != kN || chunk <= 0 || chunk > 65535 || grid <= 0) return cudaErrorInvalidValue;
+  spectrum_blocked<kN><<<8 * 152, 256, 0, st>>>(spectrum, blocked);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  ProjParams P;
+  P.spectrum = spectrum; P.rot = rot; P.mask = mask; P.fsc = fsc; P.bin_list = bin_list; P.bin_ptr = bin_ptr;
+  P.bin_count = bin_count; P.n_bins = n_bins; P.tw = tw; P.tw3 = tw3; P.bank = bank; P.scratch = scratch;
+  P.scratch_stride = project_scratch_elems(N, nb); P.N = N; P.nb = nb; P.planes = planes;
+  const size_t smem = project_smem_bytes(N, n_bins);
+  for (int b0 = 0; b0 < n_build; b0 += chunk) {
+    const int n = min(chunk, n_build - b0);
+    rows_inverse<kN><<<dim3((kN + 1 + CC - 1) / CC, n), kRiWarps * 32, 0, st>>>(blocked, rot, dirs + b0, tw,
+                                                                                 planes);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    P.dirs = dirs + b0; P.out_slot = out_slot ? out_slot + b0 : nullptr; P.n_build = n;
+    e = launch_general<kN>(P, min(grid, n), smem, st);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// complex elements of the box-256 pass-A planes of ``n`` templates
+size_t project_flat_plane_elems(int N, int n) { return (size_t)n * N * (N + 1); }

@@ -190,13 +190,19 @@ class ScoringJob:
     KERNELS_PER_CANDIDATE = 8
 
     @staticmethod
-    def projector_launches(box: int) -> int:
-        """Kernels of one projector call: three in the shared-memory path
-        (powers of two up to 128), one in the general path."""
-        return 3 if box <= 128 and box & (box - 1) == 0 else 1
+    def projector_launches(box: int, n_build: int = 1) -> int:
+        """Kernels of one projector call of ``n_build`` templates: three in the
+        shared-memory path (powers of two up to 128), one in the general path
+        (boxes 96 and 192); for box 256 the blocked spectrum copy, then the
+        gather kernel and the general kernel per 4,096 templates."""
+        if box <= 128 and box & (box - 1) == 0:
+            return 3
+        if box == 256:
+            return 1 + 2 * max(1, -(-n_build // 4096))
+        return 1
 
     def launches_per_candidate(self) -> int:
-        return 5 + self.projector_launches(self.cfg.box)
+        return 5 + self.projector_launches(self.cfg.box, len(self.needed))
     STAGES = ("density", "volume_fft", "templates", "correlate", "records")
 
     def enqueue(self, pose_device: torch.Tensor, write_volume: Optional[torch.Tensor] = None,
@@ -468,7 +474,7 @@ class BatchScoringJob:
     def launches_per_batch(self) -> int:
         # per slot: splat (2 launches) and the projector; fp16 hi/lo bank copy
         # and tensor-core kernel per chunk instead of one plain kernel
-        per_slot = 2 + ScoringJob.projector_launches(self.job.cfg.box)
+        per_slot = 2 + ScoringJob.projector_launches(self.job.cfg.box, len(self.job.needed))
         extra = 2 * len(self.tc_chunks) - 1 if self.precision != "fp32" else 0
         return self.n_cand * per_slot + self.KERNELS_PER_BATCH + extra
 

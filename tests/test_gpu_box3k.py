@@ -1,6 +1,8 @@
 """Boxes 96 and 192 (3 * 2^k: a radix-3 pass over radix-2 shared-memory
 transforms) on the GPU, through the C ABI, against the CPU oracle: templates,
-particle spectra, the end-to-end score and the tensor-core forms."""
+particle spectra, the end-to-end score and the tensor-core forms. Box 256
+templates (slice gather and row inverse in their own kernel, the remaining
+passes in the general projector) against the oracle as well."""
 import numpy as np
 import pytest
 
@@ -45,7 +47,7 @@ def _blob_density(n, seed):
     return v.astype(np.float32)
 
 
-@pytest.mark.parametrize("n,n_dir", [(96, 8), (192, 3)])
+@pytest.mark.parametrize("n,n_dir", [(96, 8), (192, 3), (256, 2)])
 def test_templates_vs_oracle(n, n_dir):
     rng = np.random.default_rng(n)
     vol = _blob_density(n, n)

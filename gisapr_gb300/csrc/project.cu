@@ -116,10 +116,171 @@ __device__ __forceinline__ float grid_pixel(float c, int size) {
   return pix;
 }
 
+// Hardware square-root approximation (PTX sqrt.approx.f32, relative error
+// about 2^-23). Used for the radial |F| sums, whose float32 sums already
+// carry larger rounding, and for radial bin indices: rint(sqrt(d2)) of an
+// integer d2 <= 2 (N/2)^2 is at least 1/(8 sqrt(d2)) away from a rounding
+// boundary, far above the approximation's error, so the bins are exact.
+__device__ __forceinline__ float sqrt_approx(float x) {
+  float r;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// Deterministic float32 block sums over NW warps (xor tree inside each
+// warp, warps added in index order). ``scratch`` holds NW entries; two uses
+// of the same scratch must be separated by a block barrier.
+template <int NW>
+__device__ __forceinline__ float4 block_sum_f4(float4 v, float4* scratch) {
+  v.x = warp_sum(v.x); v.y = warp_sum(v.y); v.z = warp_sum(v.z); v.w = warp_sum(v.w);
+  if ((threadIdx.x & 31) == 0) scratch[threadIdx.x >> 5] = v;
+  __syncthreads();
+  float4 t = scratch[0];
+#pragma unroll
+  for (int w = 1; w < NW; ++w) {
+    const float4 u = scratch[w];
+    t.x += u.x; t.y += u.y; t.z += u.z; t.w += u.w;
+  }
+  return t;
+}
+template <int NW>
+__device__ __forceinline__ float block_sum_f(float v, float* scratch) {
+  v = warp_sum(v);
+  if ((threadIdx.x & 31) == 0) scratch[threadIdx.x >> 5] = v;
+  __syncthreads();
+  float t = scratch[0];
+#pragma unroll
+  for (int w = 1; w < NW; ++w) t += scratch[w];
+  return t;
+}
+
+// Row stride (complex elements) of the padded shared-memory plane: holds the
+// N + 1 columns plus one spare slot per 8, chosen by a bank-conflict search.
+// Box 256 has no shared-memory plane; its value there is the stride of
+// rows_inverse's staging lines (256 elements plus one spare slot per 8).
+__host__ __device__ constexpr int plane_ld(int N) {
+  return N == 256 ? 290 : (N == 128 ? 150 : (N == 64 ? 74 : 38));
+}
+__host__ __device__ constexpr int plane_rows(int N) { return N + N / 8; }
+
+// Lines of length N with one spare slot per 8 elements, line stride
+// plane_ld(N): element k of line g.
+template <int N>
+struct StageLines {
+  float2* p;
+  __device__ __forceinline__ float2& at(int g, int k) const { return p[g * plane_ld(N) + k + (k >> 3)]; }
+};
+
+// In-place four-step FFT of ``nlines`` (<= 32 / (N/16)) lines, natural order
+// in and out: a 16-point register codelet over n1, twiddles, then N/16-point
+// codelets over n2 (N = 16 * (N/16)). One warp, warp barriers only. With
+// ``cj`` the input is conjugated on load and the output on store, which
+// turns the transform into the one of the opposite direction.
+template <int N, int DIR, class Lines>
+__device__ __forceinline__ void warp_fft(const Lines& L, int nlines, const float2* tw, bool cj = false) {
+  constexpr int L2 = N / 16, G = 32 / L2, T = (G * 16) / 32;
+  const int lane = threadIdx.x & 31;
+  {
+    const int g = lane / L2, n2 = lane % L2;
+    if (g < nlines) {
+      float2 x[16];
+#pragma unroll
+      for (int n1 = 0; n1 < 16; ++n1) {
+        x[n1] = L.at(g, L2 * n1 + n2);
+        if (cj) x[n1].y = -x[n1].y;
+      }
+      dft<16, DIR>(x);
+#pragma unroll
+      for (int k1 = 1; k1 < 16; ++k1)
+        if (n2) x[k1] = cmul(x[k1], tw_full<DIR>(tw, n2 * k1, N));
+#pragma unroll
+      for (int k1 = 0; k1 < 16; ++k1) L.at(g, L2 * k1 + n2) = x[k1];
+    }
+  }
+  __syncwarp();
+  float2 y[T][L2];
+#pragma unroll
+  for (int t = 0; t < T; ++t) {
+    const int task = lane + 32 * t, g = task / 16, k1 = task % 16;
+    if (g < nlines) {
+#pragma unroll
+      for (int n2 = 0; n2 < L2; ++n2) y[t][n2] = L.at(g, L2 * k1 + n2);
+      dft<L2, DIR>(y[t]);
+    }
+  }
+  __syncwarp();
+#pragma unroll
+  for (int t = 0; t < T; ++t) {
+    const int task = lane + 32 * t, g = task / 16, k1 = task % 16;
+    if (g < nlines) {
+#pragma unroll
+      for (int k2 = 0; k2 < L2; ++k2) L.at(g, k1 + 16 * k2) = cj ? cconj(y[t][k2]) : y[t][k2];
+    }
+  }
+  __syncwarp();
+}
+
+// Line batches of the general kernel in shared memory. Box 256 runs its
+// 1-D transforms as four-step warp FFTs on padded lines (natural order in
+// and out, line stride plane_ld(N), element k at k + k/8), 16 rows per row
+// batch; the other boxes use the block-wide radix-2/3 transform on unpadded
+// lines, input in fft_in_pos order.
+template <int N>
+__host__ __device__ constexpr bool warp_lines() { return N == 256; }
+template <int N>
+__host__ __device__ constexpr int line_len() { return warp_lines<N>() ? plane_ld(N) : N; }
+template <int N>
+__host__ __device__ constexpr int row_batch() { return warp_lines<N>() ? 16 : kRowBatch; }
+
+// complex elements of the line batches (the largest of passes A-G)
+__host__ __device__ constexpr int general_line_elems(int N) {
+  const int len = N == 256 ? plane_ld(256) : N;
+  const int rb = N == 256 ? 16 : kRowBatch;
+  int lines = 2 * kLineCols;
+  if (2 * rb > lines) lines = 2 * rb;
+  if (kColBatch > lines) lines = kColBatch;
+  return lines * len;
+}
+
+// position of input element k of a line, and of output element k
+template <int N>
+__device__ __forceinline__ int lin(int line, int k) {
+  return warp_lines<N>() ? line * plane_ld(N) + k + (k >> 3) : line * N + fft_in_pos(k, N);
+}
+template <int N>
+__device__ __forceinline__ int lout(int line, int k) {
+  return warp_lines<N>() ? line * plane_ld(N) + k + (k >> 3) : line * N + k;
+}
+
+// One warp's transform of one or two lines (``inv``: the unnormalised
+// inverse), one out-of-line copy for both directions: inlined at every call
+// site of the general kernel, the lane's twiddle factors were hoisted out of
+// the pass loops and held in registers throughout (255 registers, spills).
+template <int N>
+__device__ __noinline__ void warp_fft_lines(float2* p, int nlines, const float2* tw, bool inv) {
+  warp_fft<N, -1>(StageLines<N>{p}, nlines, tw, inv);
+}
+
+// In-place transforms of ``lines`` lines of the batch (sign -1 forward, +1
+// unnormalised inverse), followed by a block barrier.
+template <int N>
+__device__ __forceinline__ void line_fft(float2* buf, int lines, float sign, const float2* tw,
+                                         const float2* tw3) {
+  if constexpr (warp_lines<N>()) {
+    const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int g0 = 2 * warp; g0 < lines; g0 += 2 * nw) {
+      warp_fft_lines<N>(buf + g0 * plane_ld(N), min(2, lines - g0), tw, sign > 0.f);
+    }
+    __syncthreads();
+  } else {
+    smem_fft(buf, N, lines, sign, tw, tw3);
+  }
+}
+
 template <int N>
 __device__ void build_one(const ProjParams& P, int b, int dir, int slot, float2* S, float2* Pk,
-                          float2* sm, double* red, float* s_div, double* s_coef) {
-  constexpr int m = 2 * N, W = N + 1;
+                          float2* sm, float4* red4, float* redf, float* s_mu, float* s_div) {
+  constexpr int m = 2 * N, W = N + 1, RB = row_batch<N>();
   const int nb = P.nb, H = nb / 2 + 1;
   const int LDS = N + 1;  // scratch row stride (complex)
   const float* R = P.rot + (size_t)dir * 9;
@@ -150,16 +311,16 @@ __device__ void build_one(const ProjParams& P, int b, int dir, int slot, float2*
                                   grid_pixel(cx, W));
       if (conj) v.y = -v.y;
       const int e = r & 1, q = r >> 1;
-      sm[(cl * 2 + e) * N + fft_in_pos(q, N)] = v;
+      sm[lin<N>(cl * 2 + e, q)] = v;
     }
     __syncthreads();
-    smem_fft(sm, N, 2 * nc, +1.0f, P.tw, P.tw3);
+    line_fft<N>(sm, 2 * nc, +1.0f, P.tw, P.tw3);
     for (int t = threadIdx.x; t < nc * N; t += blockDim.x) {
       const int cl = t / N, i = t - cl * N;
       const int u = i - N / 2;               // signed output row of the 2N-point inverse
       const int k = (u + N) % N;
-      const float2 a0 = sm[(cl * 2) * N + k];
-      const float2 a1 = sm[(cl * 2 + 1) * N + k];
+      const float2 a0 = sm[lout<N>(cl * 2, k)];
+      const float2 a1 = sm[lout<N>(cl * 2 + 1, k)];
       const float2 z = cadd(a0, cmul(tw_pos_any(P.tw, P.tw3, u, m), a1));
       S[(size_t)i * LDS + c0 + cl] = z;
     }
@@ -168,9 +329,9 @@ __device__ void build_one(const ProjParams& P, int b, int dir, int slot, float2*
 
   // ---- pass B: C2R along columns, keep centred N, then forward row FFT
   const float scale_b = (float)(1.0 / ((double)m * (double)m));
-  float2* sm2 = sm + kRowBatch * N;
-  for (int i0 = 0; i0 < N; i0 += kRowBatch) {
-    const int nr = min(kRowBatch, N - i0);
+  float2* sm2 = sm + RB * line_len<N>();
+  for (int i0 = 0; i0 < N; i0 += RB) {
+    const int nr = min(RB, N - i0);
     for (int t = threadIdx.x; t < nr * N; t += blockDim.x) {
       const int rl = t / N, k = t - rl * N;
       const float2* Z = A + (size_t)(i0 + rl) * LDS;
@@ -185,23 +346,23 @@ __device__ void build_one(const ProjParams& P, int b, int dir, int slot, float2*
         yo = cmul(csub(zk, zc), tw_pos_any(P.tw, P.tw3, k, m));
       }
       // W = Ye + i*Yo
-      sm[rl * N + fft_in_pos(k, N)] = make_float2(ye.x - yo.y, ye.y + yo.x);
+      sm[lin<N>(rl, k)] = make_float2(ye.x - yo.y, ye.y + yo.x);
     }
     __syncthreads();
-    smem_fft(sm, N, nr, +1.0f, P.tw, P.tw3);
+    line_fft<N>(sm, nr, +1.0f, P.tw, P.tw3);
     // p(2n) = Re z(n), p(2n+1) = Im z(n); keep v = (j - N/2) mod 2N.
     for (int t = threadIdx.x; t < nr * N; t += blockDim.x) {
       const int rl = t / N, j = t - rl * N;
       const int v = (j - N / 2 + m) % m;
-      const float2 zz = sm[rl * N + (v >> 1)];
+      const float2 zz = sm[lout<N>(rl, v >> 1)];
       const float p = ((v & 1) ? zz.y : zz.x) * scale_b;
-      sm2[rl * N + fft_in_pos(j, N)] = make_float2(p, 0.f);
+      sm2[lin<N>(rl, j)] = make_float2(p, 0.f);
     }
     __syncthreads();
-    smem_fft(sm2, N, nr, -1.0f, P.tw, P.tw3);
+    line_fft<N>(sm2, nr, -1.0f, P.tw, P.tw3);
     for (int t = threadIdx.x; t < nr * (N / 2 + 1); t += blockDim.x) {
       const int rl = t / (N / 2 + 1), k = t - rl * (N / 2 + 1);
-      S[(size_t)(i0 + rl) * LDS + k] = sm2[rl * N + k];
+      S[(size_t)(i0 + rl) * LDS + k] = sm2[lout<N>(rl, k)];
     }
     __syncthreads();
   }
@@ -212,32 +373,38 @@ __device__ void build_one(const ProjParams& P, int b, int dir, int slot, float2*
     const int nc = min(kColBatch, HC - c0);
     for (int t = threadIdx.x; t < nc * N; t += blockDim.x) {
       const int r = t / nc, cl = t - r * nc;
-      sm[cl * N + fft_in_pos(r, N)] = S[(size_t)r * LDS + c0 + cl];
+      sm[lin<N>(cl, r)] = S[(size_t)r * LDS + c0 + cl];
     }
     __syncthreads();
-    smem_fft(sm, N, nc, -1.0f, P.tw, P.tw3);
+    line_fft<N>(sm, nc, -1.0f, P.tw, P.tw3);
     for (int t = threadIdx.x; t < nc * N; t += blockDim.x) {
       const int r = t / nc, cl = t - r * nc;
-      S[(size_t)r * LDS + c0 + cl] = sm[cl * N + r];
+      S[(size_t)r * LDS + c0 + cl] = sm[lout<N>(cl, r)];
     }
     __syncthreads();
   }
-  // radial sums of |F| over the full grid: columns 1..N/2-1 stand for two bins
+  // radial sums of |F| over the full grid in float32 (columns 1..N/2-1
+  // stand for two bins): per lane, then a fixed xor tree across the warp
   {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int b = warp; b < P.n_bins; b += nw) {
-      double acc = 0.0;
+      float acc = 0.f;
       for (int e = P.bin_ptr[b] + lane; e < P.bin_ptr[b + 1]; e += 32) {
         const int idx = P.bin_list[e];
         const int r = idx / HC, kx = idx - r * HC;
         const float2 f = S[(size_t)r * LDS + kx];
-        const double a = (double)hypotf(f.x, f.y);
-        acc += (kx == 0 || kx == N / 2) ? a : 2.0 * a;
+        const float a = sqrt_approx(fmaf(f.x, f.x, f.y * f.y));
+        acc += (kx == 0 || kx == N / 2) ? a : 2.0f * a;
       }
-      acc = warp_sum_d(acc);
-      if (lane == 0) s_div[b] = (b == 0) ? 1.0f : (float)((double)P.bin_count[b] / acc);
+      acc = warp_sum(acc);
+      if (lane == 0) s_div[b] = (b == 0) ? 1.0f : __fdiv_rn(P.bin_count[b], acc);
     }
   }
+  // The DC term (bin 0, left as it is) over N^2 is the image mean; it is read
+  // before column 0 is transformed and taken out of every pixel in pass E,
+  // so the float32 plane-fit and variance sums run on centred values.
+  const float scale_e = (float)(1.0 / ((double)N * (double)N));
+  if (threadIdx.x == 0) s_mu[0] = S[0].x * scale_e;
   __syncthreads();
 
   // ---- pass D: scale by the radial divisor, inverse column FFT
@@ -248,22 +415,23 @@ __device__ void build_one(const ProjParams& P, int b, int dir, int slot, float2*
       const int kx = c0 + cl;
       const int ky = r < N / 2 ? r : r - N;
       const int bin = (int)rintf(sqrtf((float)(ky * ky + kx * kx)));
-      sm[cl * N + fft_in_pos(r, N)] = cscale(S[(size_t)r * LDS + kx], s_div[bin]);
+      sm[lin<N>(cl, r)] = cscale(S[(size_t)r * LDS + kx], s_div[bin]);
     }
     __syncthreads();
-    smem_fft(sm, N, nc, +1.0f, P.tw, P.tw3);
+    line_fft<N>(sm, nc, +1.0f, P.tw, P.tw3);
     for (int t = threadIdx.x; t < nc * N; t += blockDim.x) {
       const int r = t / nc, cl = t - r * nc;
-      S[(size_t)r * LDS + c0 + cl] = sm[cl * N + r];
+      S[(size_t)r * LDS + c0 + cl] = sm[lout<N>(cl, r)];
     }
     __syncthreads();
   }
 
-  // ---- pass E: inverse row transform (real part), plane-fit sums
-  const float scale_e = (float)(1.0 / ((double)N * (double)N));
-  double sz = 0.0, sxz = 0.0, syz = 0.0;
-  for (int i0 = 0; i0 < N; i0 += kRowBatch) {
-    const int nr = min(kRowBatch, N - i0);
+  // ---- pass E: inverse row transform (real part), centred pixels, float32
+  // plane-fit sums (per thread, then a fixed tree across the block)
+  const float mu = s_mu[0];
+  float fz = 0.f, fxz = 0.f, fyz = 0.f, fww = 0.f;
+  for (int i0 = 0; i0 < N; i0 += RB) {
+    const int nr = min(RB, N - i0);
     for (int t = threadIdx.x; t < nr * N; t += blockDim.x) {
       const int rl = t / N, k = t - rl * N;
       const float2* G = S + (size_t)(i0 + rl) * LDS;
@@ -271,74 +439,63 @@ __device__ void build_one(const ProjParams& P, int b, int dir, int slot, float2*
       if (k == 0 || k == N / 2) y = make_float2(G[k].x, 0.f);
       else if (k < N / 2) y = G[k];
       else y = cconj(G[N - k]);
-      sm[rl * N + fft_in_pos(k, N)] = y;
+      sm[lin<N>(rl, k)] = y;
     }
     __syncthreads();
-    smem_fft(sm, N, nr, +1.0f, P.tw, P.tw3);
+    line_fft<N>(sm, nr, +1.0f, P.tw, P.tw3);
     for (int t = threadIdx.x; t < nr * N; t += blockDim.x) {
       const int rl = t / N, j = t - rl * N;
       const int i = i0 + rl;
-      const float w = sm[rl * N + j].x * scale_e;
+      const float w = fmaf(sm[lout<N>(rl, j)].x, scale_e, -mu);
       S[(size_t)i * LDS + j] = make_float2(w, 0.f);
-      sz += (double)w;
-      sxz += (double)i * (double)w;
-      syz += (double)j * (double)w;
+      fz += w;
+      fxz = fmaf((float)i, w, fxz);
+      fyz = fmaf((float)j, w, fyz);
+      fww = fmaf(w, w, fww);
     }
     __syncthreads();
   }
-  sz = block_sum_d(sz, red);
-  sxz = block_sum_d(sxz, red);
-  syz = block_sum_d(syz, red);
-  if (threadIdx.x == 0) {
-    // Normal equations of z = c0*row + c1*col + c2 over the N x N grid.
-    const double n = (double)N, n2 = n * n;
-    const double s1 = n * (n - 1.0) / 2.0 * n;           // sum of row (or col) indices
-    const double s2 = (n - 1.0) * n * (2.0 * n - 1.0) / 6.0 * n;  // sum of squares
-    const double sxy = (n * (n - 1.0) / 2.0) * (n * (n - 1.0) / 2.0);
-    double A[3][4] = {{s2, sxy, s1, sxz}, {sxy, s2, s1, syz}, {s1, s1, n2, sz}};
-    for (int c = 0; c < 3; ++c) {  // Gauss-Jordan with partial pivoting
-      int p = c;
-      for (int r2 = c + 1; r2 < 3; ++r2) if (fabs(A[r2][c]) > fabs(A[p][c])) p = r2;
-      if (p != c) for (int k = 0; k < 4; ++k) { double tmp = A[c][k]; A[c][k] = A[p][k]; A[p][k] = tmp; }
-      for (int r2 = 0; r2 < 3; ++r2) {
-        if (r2 == c) continue;
-        const double f = A[r2][c] / A[c][c];
-        for (int k = c; k < 4; ++k) A[r2][k] -= f * A[c][k];
-      }
+  // Least-squares plane z = c0*row + c1*col + c2 over the full N x N grid in
+  // closed form: the grid is a Cartesian product, so the centred row and
+  // column coordinates are orthogonal and the 3x3 normal equations decouple.
+  const float4 s4 = block_sum_f4<kThreads / 32>(make_float4(fz, fxz, fyz, fww), red4);
+  constexpr float kMid = 0.5f * (float)(N - 1);
+  constexpr float kSii = (float)((double)N * (double)N * ((double)N * (double)N - 1.0) / 12.0);
+  const float pc0 = (s4.y - kMid * s4.x) / kSii;
+  const float pc1 = (s4.z - kMid * s4.x) / kSii;
+  const float pcm = s4.x * scale_e - (pc0 + pc1) * kMid;
+  // Residual energy sum (w - P)^2 = sum w^2 - sum P w (the residual of a
+  // least-squares fit is orthogonal to the fit); where the plane holds most
+  // of the energy the subtraction would cancel, and the residual is summed
+  // directly instead (a block-uniform choice).
+  float ssr = s4.w - fmaf(pc0, s4.y, fmaf(pc1, s4.z, pcm * s4.x));
+  if (!(ssr > 0.25f * s4.w)) {
+    float fsv = 0.f;
+    for (int t = threadIdx.x; t < N * N; t += blockDim.x) {
+      const int i = t / N, j = t - i * N;
+      const float v = S[(size_t)i * LDS + j].x - fmaf(pc0, (float)i, fmaf(pc1, (float)j, pcm));
+      fsv = fmaf(v, v, fsv);
     }
-    const double c0 = A[0][3] / A[0][0], c1 = A[1][3] / A[1][1], c2 = A[2][3] / A[2][2];
-    s_coef[0] = c0; s_coef[1] = c1; s_coef[2] = c2;
-    s_coef[3] = (sz - c0 * s1 - c1 * s1 - c2 * n2) / n2;  // mean after plane removal
+    ssr = block_sum_f<kThreads / 32>(fsv, redf);
   }
-  __syncthreads();
-  const double pc0 = s_coef[0], pc1 = s_coef[1], pc2 = s_coef[2], mean = s_coef[3];
-  // ---- pass F1: population variance after plane removal
-  double sv = 0.0;
-  for (int t = threadIdx.x; t < N * N; t += blockDim.x) {
-    const int i = t / N, j = t - i * N;
-    const double v = (double)S[(size_t)i * LDS + j].x - (pc0 * i + pc1 * j + pc2) - mean;
-    sv += v * v;
-  }
-  sv = block_sum_d(sv, red);
-  const double sd = sqrt(sv / ((double)N * (double)N));
-  const double inv_sd = sd > 1e-12 ? 1.0 / sd : 1.0;
+  const float sd = sqrtf(ssr * scale_e);
+  const float inv_sd = sd > 1e-12f ? 1.0f / sd : 1.0f;
 
-  // ---- pass F2: normalise, mask, forward row FFT
-  for (int i0 = 0; i0 < N; i0 += kRowBatch) {
-    const int nr = min(kRowBatch, N - i0);
+  // ---- pass F: normalise, mask, forward row FFT
+  for (int i0 = 0; i0 < N; i0 += RB) {
+    const int nr = min(RB, N - i0);
     for (int t = threadIdx.x; t < nr * N; t += blockDim.x) {
       const int rl = t / N, j = t - rl * N;
       const int i = i0 + rl;
-      double v = ((double)S[(size_t)i * LDS + j].x - (pc0 * i + pc1 * j + pc2) - mean) * inv_sd;
-      float f = (float)v;
+      float f = (S[(size_t)i * LDS + j].x - fmaf(pc0, (float)i, fmaf(pc1, (float)j, pcm))) * inv_sd;
       if (P.mask != nullptr) f *= P.mask[(size_t)i * N + j];
-      sm[rl * N + fft_in_pos(j, N)] = make_float2(f, 0.f);
+      sm[lin<N>(rl, j)] = make_float2(f, 0.f);
     }
     __syncthreads();
-    smem_fft(sm, N, nr, -1.0f, P.tw, P.tw3);
+    line_fft<N>(sm, nr, -1.0f, P.tw, P.tw3);
     for (int t = threadIdx.x; t < nr * HC; t += blockDim.x) {
       const int rl = t / HC, k = t - rl * HC;
-      S[(size_t)(i0 + rl) * LDS + k] = sm[rl * N + k];
+      S[(size_t)(i0 + rl) * LDS + k] = sm[lout<N>(rl, k)];
     }
     __syncthreads();
   }
@@ -347,18 +504,18 @@ __device__ void build_one(const ProjParams& P, int b, int dir, int slot, float2*
     const int nc = min(kColBatch, HC - c0);
     for (int t = threadIdx.x; t < nc * N; t += blockDim.x) {
       const int r = t / nc, cl = t - r * nc;
-      sm[cl * N + fft_in_pos(r, N)] = S[(size_t)r * LDS + c0 + cl];
+      sm[lin<N>(cl, r)] = S[(size_t)r * LDS + c0 + cl];
     }
     __syncthreads();
-    smem_fft(sm, N, nc, -1.0f, P.tw, P.tw3);
+    line_fft<N>(sm, nc, -1.0f, P.tw, P.tw3);
     for (int t = threadIdx.x; t < nc * N; t += blockDim.x) {
       const int r = t / nc, cl = t - r * nc;
-      S[(size_t)r * LDS + c0 + cl] = sm[cl * N + r];
+      S[(size_t)r * LDS + c0 + cl] = sm[lout<N>(cl, r)];
     }
     __syncthreads();
   }
-  // crop + pack + FSC, L2 norm
-  double ss = 0.0;
+  // crop + pack + FSC, L2 norm (float32 per thread, fixed tree across the block)
+  float fss = 0.f;
   for (int t = threadIdx.x; t < nb * H; t += blockDim.x) {
     const int r = t / H, c = t - r * H;
     const int ky = r < nb / 2 ? r : r - nb;
@@ -372,10 +529,9 @@ __device__ void build_one(const ProjParams& P, int b, int dir, int slot, float2*
     }
     f = cscale(f, P.fsc[t]);
     Pk[t] = f;
-    ss += (double)f.x * f.x + (double)f.y * f.y;
+    fss = fmaf(f.x, f.x, fmaf(f.y, f.y, fss));
   }
-  ss = block_sum_d(ss, red);
-  const float inv_norm = (float)(1.0 / sqrt(ss));
+  const float inv_norm = 1.0f / sqrtf(block_sum_f<kThreads / 32>(fss, redf));
   float2* out = P.bank + (size_t)slot * nb * H;
   for (int t = threadIdx.x; t < nb * H; t += blockDim.x) {
     const int r = t / H, c = t - r * H;
@@ -385,16 +541,17 @@ __device__ void build_one(const ProjParams& P, int b, int dir, int slot, float2*
   __syncthreads();
 }
 
+// Box 256 asks for two CTAs per SM (128 registers); a minimum of 0 leaves the
+// other boxes to the compiler's default (40 registers; 72 with a minimum of 1).
 template <int N>
-__global__ void __launch_bounds__(kThreads) project_templates(ProjParams P) {
+__global__ void __launch_bounds__(kThreads, warp_lines<N>() ? 2 : 0) project_templates(ProjParams P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* sm = reinterpret_cast<float2*>(smem_raw);
-  const int line_elems = max(2 * kLineCols * N, 2 * kRowBatch * N);
-  const int lines = max(line_elems, kColBatch * N);
-  float2* s_tw = sm + lines;
-  double* red = reinterpret_cast<double*>(s_tw + kMaxFftLen / 2);
-  double* s_coef = red + 32;
-  float* s_div = reinterpret_cast<float*>(s_coef + 8);
+  float2* s_tw = sm + general_line_elems(N);
+  float4* red4 = reinterpret_cast<float4*>(s_tw + kMaxFftLen / 2);  // [kThreads / 32]
+  float* redf = reinterpret_cast<float*>(red4 + kThreads / 32);      // [kThreads / 32]
+  float* s_mu = redf + kThreads / 32;                                 // [4]
+  float* s_div = s_mu + 4;                                            // [n_bins + 4]
   for (int t = threadIdx.x; t < kMaxFftLen / 2; t += blockDim.x) s_tw[t] = P.tw[t];
   __syncthreads();
   ProjParams Q = P;
@@ -404,7 +561,7 @@ __global__ void __launch_bounds__(kThreads) project_templates(ProjParams P) {
   for (int b = blockIdx.x; b < P.n_build; b += gridDim.x) {
     const int dir = P.dirs[b];
     const int slot = P.out_slot ? P.out_slot[b] : dir;
-    build_one<N>(Q, b, dir, slot, S, Pk, sm, red, s_div, s_coef);
+    build_one<N>(Q, b, dir, slot, S, Pk, sm, red4, redf, s_mu, s_div);
   }
 }
 
@@ -421,10 +578,8 @@ size_t project_scratch_elems(int N, int nb) {
 }
 
 size_t project_smem_bytes(int N, int n_bins) {
-  const int line_elems = max(2 * kLineCols * N, 2 * kRowBatch * N);
-  const int lines = max(line_elems, kColBatch * N);
-  return (size_t)lines * sizeof(float2) + (kMaxFftLen / 2) * sizeof(float2) + 40 * sizeof(double) +
-         (size_t)(n_bins + 4) * sizeof(float);
+  return (size_t)general_line_elems(N) * sizeof(float2) + (kMaxFftLen / 2) * sizeof(float2) +
+         (kThreads / 32) * (sizeof(float4) + sizeof(float)) + (size_t)(4 + n_bins + 4) * sizeof(float);
 }
 
 template <int N>
@@ -491,25 +646,7 @@ template <int N>
 __host__ __device__ constexpr int pass_a_cols() { return 16 / (N / 16); }
 
 
-// Row stride (complex elements) of the padded shared-memory plane: holds the
-// N + 1 columns plus one spare slot per 8, chosen by a bank-conflict search.
-// Box 256 has no shared-memory plane; its value there is the stride of
-// rows_inverse's staging lines (256 elements plus one spare slot per 8).
-__host__ __device__ constexpr int plane_ld(int N) {
-  return N == 256 ? 290 : (N == 128 ? 150 : (N == 64 ? 74 : 38));
-}
-__host__ __device__ constexpr int plane_rows(int N) { return N + N / 8; }
 
-// Hardware square-root approximation (PTX sqrt.approx.f32, relative error
-// about 2^-23). Used for the radial |F| sums, whose float32 sums already
-// carry larger rounding, and for radial bin indices: rint(sqrt(d2)) of an
-// integer d2 <= 2 (N/2)^2 is at least 1/(8 sqrt(d2)) away from a rounding
-// boundary, far above the approximation's error, so the bins are exact.
-__device__ __forceinline__ float sqrt_approx(float x) {
-  float r;
-  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
-  return r;
-}
 
 // The half-volume spectrum in the blocked layout the slice gather reads:
 // centred order along z and y, cut into blocks of 2 (z) x 4 (y) x 2 (x)
@@ -601,11 +738,6 @@ struct ColLines {  // lines are plane columns c0 + g
   Plane<N> pl; int c0;
   __device__ __forceinline__ float2& at(int g, int k) const { return pl(k, c0 + g); }
 };
-template <int N>
-struct StageLines {  // staging lines of one warp, same padding along the line
-  float2* p;
-  __device__ __forceinline__ float2& at(int g, int k) const { return p[g * plane_ld(N) + k + (k >> 3)]; }
-};
 
 // The value of the central slice at row r (standard order of the 2N grid)
 // and column c: the reference's float32 coordinates, border-clamped
@@ -631,49 +763,6 @@ __device__ __forceinline__ float2 slice_value(const float2* __restrict__ spectru
   return v;
 }
 
-// In-place four-step FFT of ``nlines`` (<= 32 / (N/16)) lines, natural order
-// in and out: a 16-point register codelet over n1, twiddles, then N/16-point
-// codelets over n2 (N = 16 * (N/16)). One warp, warp barriers only.
-template <int N, int DIR, class Lines>
-__device__ __forceinline__ void warp_fft(const Lines& L, int nlines, const float2* tw) {
-  constexpr int L2 = N / 16, G = 32 / L2, T = (G * 16) / 32;
-  const int lane = threadIdx.x & 31;
-  {
-    const int g = lane / L2, n2 = lane % L2;
-    if (g < nlines) {
-      float2 x[16];
-#pragma unroll
-      for (int n1 = 0; n1 < 16; ++n1) x[n1] = L.at(g, L2 * n1 + n2);
-      dft<16, DIR>(x);
-#pragma unroll
-      for (int k1 = 1; k1 < 16; ++k1)
-        if (n2) x[k1] = cmul(x[k1], tw_full<DIR>(tw, n2 * k1, N));
-#pragma unroll
-      for (int k1 = 0; k1 < 16; ++k1) L.at(g, L2 * k1 + n2) = x[k1];
-    }
-  }
-  __syncwarp();
-  float2 y[T][L2];
-#pragma unroll
-  for (int t = 0; t < T; ++t) {
-    const int task = lane + 32 * t, g = task / 16, k1 = task % 16;
-    if (g < nlines) {
-#pragma unroll
-      for (int n2 = 0; n2 < L2; ++n2) y[t][n2] = L.at(g, L2 * k1 + n2);
-      dft<L2, DIR>(y[t]);
-    }
-  }
-  __syncwarp();
-#pragma unroll
-  for (int t = 0; t < T; ++t) {
-    const int task = lane + 32 * t, g = task / 16, k1 = task % 16;
-    if (g < nlines) {
-#pragma unroll
-      for (int k2 = 0; k2 < L2; ++k2) L.at(g, k1 + 16 * k2) = y[t][k2];
-    }
-  }
-  __syncwarp();
-}
 
 // Lines of the paired row passes: line q is plane row r0 + 2q, which holds
 // z = a + i b for the real rows a = r0 + 2q and b = r0 + 2q + 1.
@@ -701,30 +790,6 @@ __device__ __forceinline__ void pair_split(const Plane<N>& Z, int r0, int lane) 
   }
 }
 
-// Deterministic float32 block sums (xor tree inside each warp, warps added
-// in index order). ``scratch`` holds kSmemWarps entries; two uses of the
-// same scratch must be separated by a block barrier.
-__device__ __forceinline__ float4 block_sum_f4(float4 v, float4* scratch) {
-  v.x = warp_sum(v.x); v.y = warp_sum(v.y); v.z = warp_sum(v.z); v.w = warp_sum(v.w);
-  if ((threadIdx.x & 31) == 0) scratch[threadIdx.x >> 5] = v;
-  __syncthreads();
-  float4 t = scratch[0];
-#pragma unroll
-  for (int w = 1; w < kSmemWarps; ++w) {
-    const float4 u = scratch[w];
-    t.x += u.x; t.y += u.y; t.z += u.z; t.w += u.w;
-  }
-  return t;
-}
-__device__ __forceinline__ float block_sum_f(float v, float* scratch) {
-  v = warp_sum(v);
-  if ((threadIdx.x & 31) == 0) scratch[threadIdx.x >> 5] = v;
-  __syncthreads();
-  float t = scratch[0];
-#pragma unroll
-  for (int w = 1; w < kSmemWarps; ++w) t += scratch[w];
-  return t;
-}
 
 // The pass-A plane of one template arrives by bulk async copies: 8 plane
 // rows per copy (the rows of one padding group are contiguous in shared
@@ -909,7 +974,7 @@ __device__ void build_one_smem(const ProjParams& P, int slot, float2* Zs, const 
   // a Cartesian product, so the centred row and column coordinates are
   // orthogonal and the normal equations of the reference's 3x3 solve
   // (rows as x, columns as y) decouple.
-  const float4 s4 = block_sum_f4(make_float4(fz, fxz, fyz, fww), red4);
+  const float4 s4 = block_sum_f4<kSmemWarps>(make_float4(fz, fxz, fyz, fww), red4);
   constexpr float kMid = 0.5f * (float)(N - 1);
   constexpr float kSii = (float)((double)N * (double)N * ((double)N * (double)N - 1.0) / 12.0);
   const float pc0 = (s4.y - kMid * s4.x) / kSii;
@@ -928,7 +993,7 @@ __device__ void build_one_smem(const ProjParams& P, int slot, float2* Zs, const 
       const float v = Z(i, j).x - fmaf(pc0, (float)i, fmaf(pc1, (float)j, pcm));
       fsv = fmaf(v, v, fsv);
     }
-    ssr = block_sum_f(fsv, red);
+    ssr = block_sum_f<kSmemWarps>(fsv, red);
   }
   const float sd = sqrtf(ssr * scale_e);
   const float inv_sd = sd > 1e-12f ? 1.0f / sd : 1.0f;
@@ -986,7 +1051,7 @@ __device__ void build_one_smem(const ProjParams& P, int slot, float2* Zs, const 
       if (c >= H) { c -= H; ++r; }
     }
   }
-  const float ss = block_sum_f(fss, red);
+  const float ss = block_sum_f<kSmemWarps>(fss, red);
   if (threadIdx.x == 0 && next_plane != nullptr) plane_load<N>(Zs, next_plane, bar);
   const float inv_norm = 1.0f / sqrtf(ss);
   float2* out = P.bank + (size_t)slot * nb * H;

@@ -36,6 +36,7 @@ SIGNATURES = {
     "gisapr_particle_results_batch": [_p, _p, _p, _p, _p, _i, _i, _i, _p, _p, _p, _p, _p, _p],
     "gisapr_score_sum_batch": [_p, _p, _p, _i, _i, _p],
     "gisapr_tc_bank_bytes": [_i, _i],
+    "gisapr_project_launches": [_i, _i],
     "gisapr_set_tuning": [_p, _i, _i, _i],
     "gisapr_get_tuning": [_p, _i, _i, _p],
     "gisapr_tc_plan_work": [_p, _p, _i, _i, _i, _i, _p, _i, _p],
@@ -47,7 +48,8 @@ SIGNATURES = {
     "gisapr_restraint_eval": [_p, _p, _p, _p, _p, _i, _p, _f, _p],
 }
 
-# functions that return something other than an int status
+# functions that return something other than an int status (gisapr_project_launches
+# returns a count)
 RESTYPES = {"gisapr_tc_bank_bytes": C.c_longlong}
 
 _lib = None

@@ -439,6 +439,17 @@ int gisapr_volume_spectrum(gisapr_ctx ctx, void* stream, const float* volume, in
   return GISAPR_OK;
 }
 
+// box-256 templates per rows_inverse + general-kernel pair (planes of 526 KB)
+constexpr int kPlaneChunk = 4096;
+
+int gisapr_project_launches(int box, int n_build) {
+  if (!((is_pow2(box) && box >= 32 && box <= 256) || box == 96 || box == 192)) return -1;
+  if (n_build <= 0) return 0;
+  if (box <= 128 && is_pow2(box)) return 3;  // blocked copy, gather + row inverse, template tail
+  if (box == 256) return 1 + 2 * ((n_build + kPlaneChunk - 1) / kPlaneChunk);
+  return 1;
+}
+
 int gisapr_project_templates(gisapr_ctx ctx, void* stream, const float* spectrum, int box,
                              const float* rot, const int* dirs, int n_build, const int* out_slot,
                              const float* mask, const float* fsc, int newbox, float* bank) {
@@ -479,7 +490,7 @@ int gisapr_project_templates(gisapr_ctx ctx, void* stream, const float* spectrum
   if (box == 256) {
     // the gather and pass A in their own high-occupancy kernel, from the
     // blocked spectrum, at most 4,096 planes (2.2 GB) at a time
-    const int chunk = std::min(n_build, 4096);
+    const int chunk = std::min(n_build, kPlaneChunk);
     rc = ensure(ctx, ctx->proj_slices, project_flat_plane_elems(box, chunk) * sizeof(float2), "cudaMalloc(planes)");
     if (rc) return rc;
     rc = ensure(ctx, ctx->proj_blocked, project_blocked_elems(box) * sizeof(float2), "cudaMalloc(blocked spectrum)");

@@ -191,15 +191,15 @@ class ScoringJob:
 
     @staticmethod
     def projector_launches(box: int, n_build: int = 1) -> int:
-        """Kernels of one projector call of ``n_build`` templates: three in the
-        shared-memory path (powers of two up to 128), one in the general path
-        (boxes 96 and 192); for box 256 the blocked spectrum copy, then the
-        gather kernel and the general kernel per 4,096 templates."""
-        if box <= 128 and box & (box - 1) == 0:
-            return 3
-        if box == 256:
-            return 1 + 2 * max(1, -(-n_build // 4096))
-        return 1
+        """Kernels of one projector call of ``n_build`` templates, as the
+        library reports them: three in the shared-memory path (powers of two
+        up to 128), one in the general path (boxes 96 and 192); for box 256
+        the blocked spectrum copy, then the gather kernel and the general
+        kernel per 4,096 templates."""
+        n = int(nat.load().gisapr_project_launches(int(box), max(1, int(n_build))))
+        if n < 0:
+            raise ValueError(f"unsupported box {box}")
+        return n
 
     def launches_per_candidate(self) -> int:
         return 5 + self.projector_launches(self.cfg.box, len(self.needed))

@@ -123,6 +123,14 @@ int gisapr_project_templates(gisapr_ctx ctx, void* stream, const float* spectrum
                              const float* mask, const float* fsc, int newbox, float* bank);
 
 /*
+ * Kernel launches one gisapr_project_templates call of ``n_build``
+ * templates enqueues at ``box`` (0 for n_build <= 0; -1 for an unsupported
+ * box). Host only, no context; lets a caller count its launches or size a
+ * captured graph. This query has no counterpart in the reference.
+ */
+int gisapr_project_launches(int box, int n_build);
+
+/*
  * CTF * ISSPA weight per particle in the packed layout. Replaces
  * PackedCTFTorch.batch (v606:781-829). dfu/dfv/dfa [n] float32 (Angstrom,
  * degrees); tx, ty, tu4, tnc [K] float32 static tables (packed frequency x,

@@ -86,3 +86,27 @@ def test_tensor_core_work_plan_on_host(native_lib):
     assert lib.gisapr_tc_plan_work(vp(ptr), vp(idx), 40, 129, 3, 12, None, 0, C.byref(n)) == 1
     assert lib.gisapr_tc_plan_work(vp(ptr), vp(idx), 40, 8, 3, 16, None, 0, C.byref(n)) == 4
     assert lib.gisapr_tc_bank_bytes(760, 128) == 760 * 65 * 2 * 256 * 2
+
+
+def test_projector_launch_counts_on_host(native_lib):
+    """The launch count one projector call enqueues: three kernels on the
+    shared-memory path, one on the general path at 96 and 192, and at 256 the
+    blocked spectrum copy plus a gather and a general kernel per 4,096
+    templates. The engine's gpu_launches figure is built from it."""
+    lib = native_lib
+    lib.gisapr_project_launches.argtypes = [C.c_int, C.c_int]
+    for box in (32, 64, 128):
+        assert lib.gisapr_project_launches(box, 3072) == 3
+    for box in (96, 192):
+        assert lib.gisapr_project_launches(box, 3072) == 1
+    assert lib.gisapr_project_launches(256, 1) == 3
+    assert lib.gisapr_project_launches(256, 4096) == 3
+    assert lib.gisapr_project_launches(256, 4097) == 5
+    assert lib.gisapr_project_launches(256, 3 * 4096 + 5) == 9
+    assert lib.gisapr_project_launches(128, 0) == 0
+    for bad in (16, 80, 512):
+        assert lib.gisapr_project_launches(bad, 10) == -1
+    from gisapr_gb300.engine import ScoringJob
+    assert ScoringJob.projector_launches(256, 8192) == 5
+    with pytest.raises(ValueError):
+        ScoringJob.projector_launches(80, 1)

@@ -281,6 +281,10 @@ template <int N>
 __device__ void build_one(const ProjParams& P, int b, int dir, int slot, float2* S, float2* Pk,
                           float2* sm, float4* red4, float* redf, float* s_mu, float* s_div) {
   constexpr int m = 2 * N, W = N + 1, RB = row_batch<N>();
+  // unroll of the loops that read the scratch plane: box 256 keeps four
+  // loads in flight per thread (the smaller boxes run more CTAs per SM and
+  // keep their register count)
+  constexpr int UNR = warp_lines<N>() ? 4 : 1;
   const int nb = P.nb, H = nb / 2 + 1;
   const int LDS = N + 1;  // scratch row stride (complex)
   const float* R = P.rot + (size_t)dir * 9;
@@ -332,6 +336,7 @@ __device__ void build_one(const ProjParams& P, int b, int dir, int slot, float2*
   float2* sm2 = sm + RB * line_len<N>();
   for (int i0 = 0; i0 < N; i0 += RB) {
     const int nr = min(RB, N - i0);
+#pragma unroll (UNR)
     for (int t = threadIdx.x; t < nr * N; t += blockDim.x) {
       const int rl = t / N, k = t - rl * N;
       const float2* Z = A + (size_t)(i0 + rl) * LDS;
@@ -371,6 +376,7 @@ __device__ void build_one(const ProjParams& P, int b, int dir, int slot, float2*
   const int HC = N / 2 + 1;
   for (int c0 = 0; c0 < HC; c0 += kColBatch) {
     const int nc = min(kColBatch, HC - c0);
+#pragma unroll (UNR)
     for (int t = threadIdx.x; t < nc * N; t += blockDim.x) {
       const int r = t / nc, cl = t - r * nc;
       sm[lin<N>(cl, r)] = S[(size_t)r * LDS + c0 + cl];
@@ -389,6 +395,7 @@ __device__ void build_one(const ProjParams& P, int b, int dir, int slot, float2*
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int b = warp; b < P.n_bins; b += nw) {
       float acc = 0.f;
+#pragma unroll (UNR / 2 > 0 ? UNR / 2 : 1)
       for (int e = P.bin_ptr[b] + lane; e < P.bin_ptr[b + 1]; e += 32) {
         const int idx = P.bin_list[e];
         const int r = idx / HC, kx = idx - r * HC;
@@ -410,6 +417,7 @@ __device__ void build_one(const ProjParams& P, int b, int dir, int slot, float2*
   // ---- pass D: scale by the radial divisor, inverse column FFT
   for (int c0 = 0; c0 < HC; c0 += kColBatch) {
     const int nc = min(kColBatch, HC - c0);
+#pragma unroll (UNR)
     for (int t = threadIdx.x; t < nc * N; t += blockDim.x) {
       const int r = t / nc, cl = t - r * nc;
       const int kx = c0 + cl;
@@ -432,6 +440,7 @@ __device__ void build_one(const ProjParams& P, int b, int dir, int slot, float2*
   float fz = 0.f, fxz = 0.f, fyz = 0.f, fww = 0.f;
   for (int i0 = 0; i0 < N; i0 += RB) {
     const int nr = min(RB, N - i0);
+#pragma unroll (UNR)
     for (int t = threadIdx.x; t < nr * N; t += blockDim.x) {
       const int rl = t / N, k = t - rl * N;
       const float2* G = S + (size_t)(i0 + rl) * LDS;
@@ -484,6 +493,7 @@ __device__ void build_one(const ProjParams& P, int b, int dir, int slot, float2*
   // ---- pass F: normalise, mask, forward row FFT
   for (int i0 = 0; i0 < N; i0 += RB) {
     const int nr = min(RB, N - i0);
+#pragma unroll (UNR)
     for (int t = threadIdx.x; t < nr * N; t += blockDim.x) {
       const int rl = t / N, j = t - rl * N;
       const int i = i0 + rl;
@@ -502,6 +512,7 @@ __device__ void build_one(const ProjParams& P, int b, int dir, int slot, float2*
   // ---- pass G: forward column FFT
   for (int c0 = 0; c0 < HC; c0 += kColBatch) {
     const int nc = min(kColBatch, HC - c0);
+#pragma unroll (UNR)
     for (int t = threadIdx.x; t < nc * N; t += blockDim.x) {
       const int r = t / nc, cl = t - r * nc;
       sm[lin<N>(cl, r)] = S[(size_t)r * LDS + c0 + cl];
@@ -516,6 +527,7 @@ __device__ void build_one(const ProjParams& P, int b, int dir, int slot, float2*
   }
   // crop + pack + FSC, L2 norm (float32 per thread, fixed tree across the block)
   float fss = 0.f;
+#pragma unroll (UNR)
   for (int t = threadIdx.x; t < nb * H; t += blockDim.x) {
     const int r = t / H, c = t - r * H;
     const int ky = r < nb / 2 ? r : r - nb;

@@ -32,7 +32,7 @@ enum {
   GISAPR_ERR_ARGUMENT = 1,    /* bad size, shape or null pointer (Python: ValueError) */
   GISAPR_ERR_CUDA = 2,        /* CUDA runtime / launch failure (Python: RuntimeError) */
   GISAPR_ERR_CUFFT = 3,       /* cuFFT failure */
-  GISAPR_ERR_UNSUPPORTED = 4  /* a size this build does not implement */
+  GISAPR_ERR_UNSUPPORTED = 4  /* a size the library does not implement */
 };
 
 typedef struct gisapr_context* gisapr_ctx;

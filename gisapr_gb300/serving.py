@@ -35,15 +35,40 @@ from typing import Callable, Deque, Dict, List, Optional
 
 import numpy as np
 
-__all__ = ["ScoringServer", "ServerStats", "job_footprint_bytes"]
+__all__ = ["ScoringServer", "ServerStats", "job_footprint_bytes", "projector_scratch_bytes"]
+
+
+def projector_scratch_bytes(box: int, new_box: int, n_dirs: int, sm_count: int = 152) -> int:
+    """Device memory the library context holds for one projector call of
+    ``n_dirs`` templates at ``box``: the blocked spectrum copy and the pass-A
+    planes (powers of two; at box 256 at most 4,096 planes of 256 x 257), and
+    the general projector's per-CTA scratch planes (boxes 96, 192, 256; 6, 3
+    and 2 CTAs per SM). The context keeps the largest size it has seen and
+    shares it between the jobs that use it."""
+    n, h = int(box), new_box // 2 + 1
+    pow2 = n & (n - 1) == 0
+    out = 0
+    if pow2:
+        out += 4 * n * n * ((n + 2) // 2 * 2) * 8            # blocked spectrum
+    if pow2 and n <= 128:
+        ld = {32: 38, 64: 74, 128: 150}[n]
+        out += n_dirs * n * ld * 8                            # pass-A planes
+    else:
+        if n == 256:
+            out += min(n_dirs, 4096) * n * (n + 1) * 8        # pass-A planes
+        per_sm = {96: 6, 192: 3}.get(n, 2)
+        out += min(n_dirs, sm_count * per_sm) * (n * (n + 1) + new_box * h) * 8
+    return int(out)
 
 
 def job_footprint_bytes(box: int, new_box: int, n_particles: int, n_psi: int, n_dirs: int, max_batch: int,
                         precision: str = "fp32", local_dirs: int = 64) -> int:
     """Upper bound of a job's device memory: resident particle spectra and
     tables, the per-candidate volume and spectrum buffers, the batch's
-    template banks (every model direction counted as needed) and its per-map
-    outputs (``local_dirs`` directions per particle at most)."""
+    template banks (every model direction counted as needed), its per-map
+    outputs (``local_dirs`` directions per particle at most) and the
+    projector scratch of the library context (counted for every job, although
+    jobs on one context share it)."""
     h = new_box // 2 + 1
     spectra = n_particles * n_psi * new_box * h * 8
     tables = n_particles * (new_box * h * 4 + 64) + n_dirs * 64 + 8 * new_box * h * 4
@@ -53,7 +78,7 @@ def job_footprint_bytes(box: int, new_box: int, n_particles: int, n_psi: int, n_
         banks += min(max_batch, 128) * n_dirs * new_box * h * 8
     maps = max_batch * n_particles * min(local_dirs, n_dirs) * n_psi * 12
     records = max_batch * n_particles * 24 + max_batch * 16
-    return int(spectra + tables + volume + banks + maps + records)
+    return int(spectra + tables + volume + banks + maps + records + projector_scratch_bytes(box, new_box, n_dirs))
 
 
 @dataclass

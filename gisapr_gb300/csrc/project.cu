@@ -623,8 +623,9 @@ cudaError_t launch_project_templates(cudaStream_t st, const float2* spectrum, co
   switch (N) {
     case 96: return launch_general<96>(P, grid, smem, st);
     case 192: return launch_general<192>(P, grid, smem, st);
-    case 256: return launch_general<256>(P, grid, smem, st);
-    default: return cudaErrorInvalidValue;  // powers of two up to 128 take the shared-memory path
+    // powers of two up to 128 take the shared-memory path, box 256
+    // launch_project_templates_planes
+    default: return cudaErrorInvalidValue;
   }
 }
 

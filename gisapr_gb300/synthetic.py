@@ -324,6 +324,22 @@ def logistic_fsc(box: int, apix: float, half_res: Optional[float]) -> np.ndarray
     return (1.0 / (1.0 + np.exp((freq - f0) / (0.08 * f0)))).astype(np.float32)
 
 
+def blob_density(n: int, seed: int) -> np.ndarray:
+    """Six Gaussian blobs around the box centre plus 0.2 white noise, float32
+    [z, y, x], from ``seed``. The noise keeps every radial shell of the
+    spectrum well above float32 rounding (the whitening rescales each shell
+    to unit mean amplitude), so template comparisons at any box measure the
+    arithmetic, not rounding noise in empty shells."""
+    rng = np.random.default_rng(seed)
+    z, y, x = np.meshgrid(*(np.arange(n, dtype=np.float64),) * 3, indexing="ij")
+    v = 0.2 * rng.standard_normal((n, n, n))
+    for _ in range(6):
+        c = n / 2 + rng.normal(scale=n / 10, size=3)
+        s = rng.uniform(1.5, n / 16)
+        v += rng.uniform(0.5, 2.0) * np.exp(-((z - c[0]) ** 2 + (y - c[1]) ** 2 + (x - c[2]) ** 2) / (2 * s * s))
+    return v.astype(np.float32)
+
+
 def random_rotations(n: int, rng: np.random.Generator):
     """Uniform SO(3) as RELION (rot, tilt, psi) degrees."""
     rot = rng.uniform(-180.0, 180.0, n)

@@ -43,8 +43,8 @@ def projector_scratch_bytes(box: int, new_box: int, n_dirs: int, sm_count: int =
     ``n_dirs`` templates at ``box``: the blocked spectrum copy and the pass-A
     planes (powers of two; at box 256 at most 4,096 planes of 256 x 257), and
     the general projector's per-CTA scratch planes (boxes 96, 192, 256; 6, 3
-    and 2 CTAs per SM). The context keeps the largest size it has seen and
-    shares it between the jobs that use it."""
+    and 2 CTAs per SM). Each host thread's context keeps the largest size it
+    has seen and shares it between the jobs that thread runs."""
     n, h = int(box), new_box // 2 + 1
     pow2 = n & (n - 1) == 0
     out = 0
@@ -67,8 +67,8 @@ def job_footprint_bytes(box: int, new_box: int, n_particles: int, n_psi: int, n_
     tables, the per-candidate volume and spectrum buffers, the batch's
     template banks (every model direction counted as needed), its per-map
     outputs (``local_dirs`` directions per particle at most) and the
-    projector scratch of the library context (counted for every job, although
-    jobs on one context share it)."""
+    projector scratch of a library context (counted once for every job,
+    although a context is per host thread and shared by that thread's jobs)."""
     h = new_box // 2 + 1
     spectra = n_particles * n_psi * new_box * h * 8
     tables = n_particles * (new_box * h * 4 + 64) + n_dirs * 64 + 8 * new_box * h * 4

@@ -32,25 +32,10 @@ def _t(a):
     return torch.as_tensor(np.ascontiguousarray(a)).to(DEV)
 
 
-def _blob_density(n, seed):
-    """Gaussian blobs around the box centre plus white noise, float32 [z, y,
-    x]. The noise keeps every radial shell well above float32 rounding: the
-    whitening rescales each shell to unit mean amplitude, so a density whose
-    outer shells sit near rounding level would compare float32 noise."""
-    rng = np.random.default_rng(seed)
-    z, y, x = np.meshgrid(*(np.arange(n, dtype=np.float64),) * 3, indexing="ij")
-    v = 0.2 * rng.standard_normal((n, n, n))
-    for _ in range(6):
-        c = n / 2 + rng.normal(scale=n / 10, size=3)
-        s = rng.uniform(1.5, n / 16)
-        v += rng.uniform(0.5, 2.0) * np.exp(-((z - c[0]) ** 2 + (y - c[1]) ** 2 + (x - c[2]) ** 2) / (2 * s * s))
-    return v.astype(np.float32)
-
-
 @pytest.mark.parametrize("n,n_dir", [(96, 8), (192, 3), (256, 2)])
 def test_templates_vs_oracle(n, n_dir):
     rng = np.random.default_rng(n)
-    vol = _blob_density(n, n)
+    vol = syn.blob_density(n, n)  # blobs plus white noise: no shell near float32 rounding
     rot = rng.uniform(-180.0, 180.0, n_dir)
     tilt = np.rad2deg(np.arccos(rng.uniform(-1.0, 1.0, n_dir)))
     angles = model_angles_from_lists(rot, tilt)

@@ -1,15 +1,19 @@
 // Central-slice projector and template tail (v606:856-1147) for sm_103a.
 //
-// One CTA builds one template at a time (grid-stride over directions). Every
-// 2-D array of a template lives in an L2-resident scratch area owned by the
-// CTA; each pass stages a batch of rows or columns in shared memory, runs
-// radix-2 FFTs there and writes the batch back. The passes are:
+// General kernel (boxes 96, 192, 256): one CTA builds one template at a
+// time (grid-stride over directions). Every 2-D array of a template lives in
+// a global scratch plane owned by the CTA; each pass stages a batch of rows
+// or columns in shared memory, transforms it there (block-wide radix-2/3
+// FFTs at 96 and 192, four-step warp FFTs at 256) and writes the batch back.
+// Boxes 32, 64 and 128 use the shared-memory path further below, which runs
+// the same passes on a plane held in shared memory. The passes are:
 //
 //   A  slice gather + inverse along rows: trilinear samples of the half
 //      volume (border clamp, conjugate where the rotated x < 0) feed two
 //      N-point inverse FFTs per column (even/odd rows of the 2N grid); the
 //      pair combines into exactly the N centred output rows of the 2N-point
-//      inverse that the crop keeps (v606:1099-1130).
+//      inverse that the crop keeps (v606:1099-1130). At box 256 (and on the
+//      shared-memory path) this pass is its own kernel, rows_inverse.
 //   B  C2R along columns (2N-point real output from N+1 coefficients, via an
 //      N-point complex inverse), keep the N centred columns, scale 1/(2N)^2;
 //      then the forward row FFT that starts the whitening.
@@ -17,9 +21,10 @@
 //      reductions over a host-built bin list).
 //   D  divide by the radial mean amplitude (DC bin untouched), inverse
 //      column FFT.
-//   E  inverse row transform (real part), plane-fit sums in FP64.
-//   F  plane removal, mean/population-sigma normalisation, soft mask,
-//      forward row FFT.
+//   E  inverse row transform (real part) of pixels centred on the image
+//      mean, float32 plane-fit sums (per thread, then a fixed tree).
+//   F  plane removal (the least-squares plane in closed form), population
+//      sigma normalisation, soft mask, forward row FFT.
 //   G  forward column FFT, Fourier crop and packing, FSC weight, L2 norm
 //      over the packed half plane, pre-shift (fftshift both dims) into the
 //      template bank (v606:1132-1147, 531-537).

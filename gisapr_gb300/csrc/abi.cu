@@ -141,6 +141,8 @@ struct gisapr_context {
   // Buffers replaced by larger ones. They are freed only with the context:
   // a CUDA graph captured before a buffer grew still names the old one, and
   // that buffer stays valid (and large enough for the graph's own sizes).
+  // A buffer that grows at least doubles (see ensure), so the retired
+  // buffers of one kind hold less memory than the live one.
   std::vector<void*> retired;
   int sm_count = 152;
   std::map<int, int> tune_corr_cluster;  // n -> CTAs per particle in the plain correlation
@@ -153,9 +155,17 @@ int set_device(gisapr_ctx ctx) {
   return GISAPR_OK;
 }
 
+// Make ``b`` hold at least ``bytes``. The first allocation is exact; a
+// buffer that has to grow is replaced by one of at least twice its size, so
+// a context that sees growing requests keeps less than twice the live
+// buffer in total (live plus retired) and the live buffer stays below twice
+// the largest request.
 int ensure(gisapr_ctx ctx, DeviceBuffer& b, size_t bytes, const char* what) {
   if (b.bytes >= bytes) return GISAPR_OK;
-  if (b.ptr) ctx->retired.push_back(b.ptr);
+  if (b.ptr) {
+    ctx->retired.push_back(b.ptr);
+    bytes = std::max(bytes, 2 * b.bytes);
+  }
   b.ptr = nullptr;
   b.bytes = 0;
   cudaError_t e = cudaMalloc(&b.ptr, bytes);

@@ -140,8 +140,8 @@ __device__ __forceinline__ float fftfreq_shifted_f32(int i, int m) {
 }
 
 __global__ void __launch_bounds__(256)
-splat_bricks(const AtomRec* __restrict__ atoms, int n_atoms, const float* __restrict__ initial,
-             float* __restrict__ out, float* __restrict__ padded, int box, float rp_hi,
+splat_bricks(const AtomRec* __restrict__ atoms, int n_atoms, const float* initial,
+             float* out, float* __restrict__ padded, int box, float rp_hi,
              float rp_lo) {
   __shared__ AtomRec s_atoms[256];
   __shared__ int s_count;
@@ -346,7 +346,7 @@ extern "C" int gisapr_deposit_noalloc(void* stream, const float* xyz, const floa
                             " (split the atoms over several calls or use gisapr_deposit)");
   if (box < 1 || box > 1024) return noalloc_fail(GISAPR_ERR_ARGUMENT, "box out of range");
   if (width < 3) return noalloc_fail(GISAPR_ERR_ARGUMENT, "width must be >= 3 (insufficient sampling)");
-  if (!(apix > 0.0) || !isfinite(apix) || !isfinite(rp) || !isfinite(kn))
+  if (!(apix > 0.0) || !(rp > 0.0) || !(kn > 0.0) || !isfinite(apix) || !isfinite(rp) || !isfinite(kn))
     return noalloc_fail(GISAPR_ERR_ARGUMENT, "apix, rp and kn must be positive and finite");
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -362,6 +362,14 @@ extern "C" int gisapr_deposit_noalloc(void* stream, const float* xyz, const floa
       e = cudaGetSymbolAddress(&p, g_noalloc_atoms);
       if (e != cudaSuccess || !p)
         return noalloc_fail(GISAPR_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+      // Under lazy module loading a kernel is loaded on its first launch,
+      // which could fall inside a later stream capture; querying both
+      // kernels' attributes here loads them now, even for an empty call.
+      cudaFuncAttributes fa;
+      e = cudaFuncGetAttributes(&fa, atoms_prepare);
+      if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, splat_bricks);
+      if (e != cudaSuccess)
+        return noalloc_fail(GISAPR_ERR_CUDA, std::string("cudaFuncGetAttributes: ") + cudaGetErrorString(e));
       g_noalloc_ptr[dev] = p;
     }
     recs = g_noalloc_ptr[dev];
@@ -455,7 +463,7 @@ __global__ void atoms_prepare_binned(const float* __restrict__ xyz, const float*
 
 __global__ void __launch_bounds__(512)
 splat_binned(const AtomRec* __restrict__ atoms, int n_atoms, const int* __restrict__ counts,
-             const int* __restrict__ lists, int cap, const float* __restrict__ initial, float* __restrict__ out,
+             const int* __restrict__ lists, int cap, const float* initial, float* out,
              float* __restrict__ padded, int box, float rp_hi, float rp_lo) {
   extern __shared__ int s_ids[];  // cap entries (power of two >= count for the sort)
   __shared__ AtomRec s_rec[64];

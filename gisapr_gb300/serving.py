@@ -38,13 +38,23 @@ import numpy as np
 __all__ = ["ScoringServer", "ServerStats", "job_footprint_bytes", "projector_scratch_bytes"]
 
 
+# A library context grows a scratch buffer to at least twice its size when
+# a call needs more, and keeps the buffers it replaced (CUDA graphs captured
+# earlier may still name them): for the largest request R a context has
+# seen, the live buffer is below 2 R and the replaced ones together below the
+# live one, so the context holds less than 4 R of that kind of buffer.
+CONTEXT_GROWTH_BOUND = 4
+
+
 def projector_scratch_bytes(box: int, new_box: int, n_dirs: int, sm_count: int = 152) -> int:
-    """Device memory the library context holds for one projector call of
-    ``n_dirs`` templates at ``box``: the blocked spectrum copy and the pass-A
-    planes (powers of two; at box 256 at most 4,096 planes of 256 x 257), and
-    the general projector's per-CTA scratch planes (boxes 96, 192, 256; 6, 3
-    and 2 CTAs per SM). Each host thread's context keeps the largest size it
-    has seen and shares it between the jobs that thread runs."""
+    """Upper bound of the device memory a library context holds for
+    projector calls of up to ``n_dirs`` templates at ``box``: the blocked
+    spectrum copy and the pass-A planes (powers of two; at box 256 at most
+    4,096 planes of 256 x 257), and the general projector's per-CTA scratch
+    planes (boxes 96, 192, 256; 6, 3 and 2 CTAs per SM), each times
+    CONTEXT_GROWTH_BOUND (buffers grown by later, larger calls keep their
+    predecessors). Each host thread's context is shared by the jobs that
+    thread runs."""
     n, h = int(box), new_box // 2 + 1
     pow2 = n & (n - 1) == 0
     out = 0
@@ -58,7 +68,7 @@ def projector_scratch_bytes(box: int, new_box: int, n_dirs: int, sm_count: int =
             out += min(n_dirs, 4096) * n * (n + 1) * 8        # pass-A planes
         per_sm = {96: 6, 192: 3}.get(n, 2)
         out += min(n_dirs, sm_count * per_sm) * (n * (n + 1) + new_box * h) * 8
-    return int(out)
+    return int(CONTEXT_GROWTH_BOUND * out)
 
 
 def job_footprint_bytes(box: int, new_box: int, n_particles: int, n_psi: int, n_dirs: int, max_batch: int,

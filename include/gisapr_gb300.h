@@ -69,8 +69,10 @@ int gisapr_deposit(gisapr_ctx ctx, void* stream, const float* xyz, const float* 
  * (3 MiB) in the library's static device memory, held by every GPU that
  * loads the library until the process exits; more atoms per call are
  * rejected with GISAPR_ERR_ARGUMENT. No context is needed. The first call
- * on a device resolves the array's device address with that device current,
- * so make that first call before capturing a stream. All calls share the
+ * on a device resolves the array's device address and loads the two kernels
+ * with that device current (a call with n_atoms == 0 does this too and
+ * launches nothing), so make that first call before capturing a stream.
+ * apix, rp and kn must be positive and finite. All calls share the
  * array: calls whose work overlaps on the GPU (other streams, other host
  * threads) race on it, so serialise them.
  */

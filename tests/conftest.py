@@ -25,6 +25,21 @@ def golden64():
 
 
 @pytest.fixture(scope="session")
+def golden128():
+    import numpy as np
+    return dict(np.load(ROOT / "tests" / "golden" / "golden_box128.npz"))
+
+
+@pytest.fixture(scope="session")
+def box128_case(golden128):
+    """The box-128 fixture's job regenerated from its seed (images checked
+    against the stored checksums) and the FP64 oracle's evaluation of its
+    candidate (about 25 s on the CPU; shared by the tests of a session)."""
+    from tests.helpers import box128_case as make
+    return make(golden128)
+
+
+@pytest.fixture(scope="session")
 def native_lib():
     """The built library (built here if needed; nvcc cross-compiles)."""
     import __graft_entry__ as g

@@ -192,7 +192,7 @@ def _flat(lists, dtype):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", required=True, help="root of the GisAPR sources (flat script directory with the two zips)")
     ap.add_argument("--out", default=str(HERE))
     args = ap.parse_args()
     import torch

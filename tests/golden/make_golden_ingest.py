@@ -28,7 +28,7 @@ CROP, PIXEL, HIGHPASS = 48, 1.5, 20.0
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", required=True, help="root of the GisAPR sources (flat script directory with the two zips)")
     ap.add_argument("--out", default=str(HERE / "golden_ingest.npz"))
     args = ap.parse_args()
     for name in ("starfile", "mrcfile"):

@@ -47,7 +47,7 @@ PIVOT_POSES = np.asarray([[0.0, 25.0, 10.0, 30.0, 20.0, 0.0], [15.0, 0.0, -35.0,
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", required=True, help="root of the GisAPR sources (flat script directory with the two zips)")
     ap.add_argument("--out", default=str(HERE / "golden_restraint.npz"))
     args = ap.parse_args()
     model = syn.make_model(syn.residues_for_atoms(760), syn.residues_for_atoms(3030), seed=41)

@@ -52,7 +52,7 @@ def make_texts(seed=7):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", required=True, help="root of the GisAPR sources (flat script directory with the two zips)")
     ap.add_argument("--out", default=str(HERE / "golden_scorer.npz"))
     args = ap.parse_args()
     texts = make_texts()

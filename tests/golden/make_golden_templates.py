@@ -64,7 +64,7 @@ def reference_templates(v606, n: int, n_dir: int, half_res: float, tmp: Path) ->
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", required=True, help="root of the GisAPR sources (flat script directory with the two zips)")
     ap.add_argument("--out", default=str(HERE / "golden_templates.npz"))
     a = ap.parse_args()
     out = {"apix": np.float64(APIX), "mask_edge": np.int64(MASK_EDGE)}

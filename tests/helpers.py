@@ -7,12 +7,23 @@ from gisapr_gb300 import synthetic as syn
 from gisapr_gb300.tables import ParticleRecord
 
 # Tolerances. Density, particle spectra and scores follow the stated parity
-# bar; templates carry the reference's own float32 whitening error (its
-# templates differ from the FP64 oracle by up to 6e-5 relative RMS, checked in
-# test_oracle_golden), so the template bar sits above that floor.
+# bar. Templates are held to TEMPLATE_RRMS against the FP64 oracle (the exact
+# answer). Against the reference's own float32 templates the bar is that
+# reference's distance from the oracle plus TEMPLATE_RRMS: its whitening
+# rescales weak radial shells to unit amplitude and so amplifies its float32
+# FFT rounding, to 6e-5 relative RMS at box 32, 1.3e-4 at box 256 and 6.7e-4
+# at box 128 with the logistic FSC (test_oracle_golden*.py measure these).
 DENSITY_RRMS = 1e-5
 SPECTRUM_RRMS = 1e-5
-TEMPLATE_RRMS = 3e-4
+TEMPLATE_RRMS = 1e-4
+# the reference's own distance from the oracle (measured maxima, rounded up)
+TEMPLATE_REF_FLOOR = {32: 1e-4, 64: 1e-4, 96: 1e-4, 128: 7e-4, 192: 1e-4, 256: 1.5e-4}
+
+
+def template_ref_rrms(n: int) -> float:
+    """Bar of a template against the reference's own template at box n."""
+    return TEMPLATE_REF_FLOOR[int(n)] + TEMPLATE_RRMS
+
 CTF_ABS = 2e-5
 SCORE_REL = 1e-4
 PEAK_REL = 1e-4
@@ -117,3 +128,83 @@ def parse_search_text(path_or_text):
     if len(rows) % 3:
         raise ValueError("a search text holds three records per particle")
     return [tuple(rows[i:i + 3]) for i in range(0, len(rows), 3)]
+
+
+# ---------------------------------------------------------------------------
+# Per-particle argmax: identical, or a tie within TIE_REL
+# ---------------------------------------------------------------------------
+
+
+def argmax_mismatches(ptr, n_psi, ref_scores, ref_ys, ref_xs, got_entry, got_psi, got_y, got_x, window=None,
+                      tie_rel=TIE_REL):
+    """Particles whose chosen (direction, psi, y, x) differs from the
+    reference's first maximum without being a tie.
+
+    ``ref_scores/ys/xs`` are the reference's per-map maxima ([entry][psi]
+    flattened, entries in CSR order). A different map is a tie when the
+    reference's own maximum of the chosen map is within ``tie_rel`` of its
+    best; a different position inside the same map is a tie when
+    ``window(particle, entry_offset, psi)`` (an exact crop window, e.g. the
+    oracle's) holds values within ``tie_rel`` at both positions. Returns the
+    list of (particle, reason)."""
+    bad = []
+    for i in range(len(ptr) - 1):
+        e0, e1 = int(ptr[i]), int(ptr[i + 1])
+        if e1 <= e0:
+            if int(got_entry[i]) != -1:
+                bad.append((i, "record for a particle without directions"))
+            continue
+        rs = np.asarray(ref_scores[e0 * n_psi:e1 * n_psi], dtype=np.float64)
+        b = int(np.argmax(rs))
+        best = rs[b]
+        a = (int(got_entry[i]) - e0) * n_psi + int(got_psi[i])
+        if not 0 <= a < len(rs):
+            bad.append((i, "chosen map outside the particle's list"))
+            continue
+        ry, rx = int(ref_ys[e0 * n_psi + b]), int(ref_xs[e0 * n_psi + b])
+        gy, gx = int(got_y[i]), int(got_x[i])
+        if a == b:
+            if (gy, gx) == (ry, rx):
+                continue
+            if window is None:
+                bad.append((i, f"same map, position {(gy, gx)} vs {(ry, rx)}"))
+                continue
+            w = window(i, a // n_psi, a % n_psi)
+            if abs(w[gy, gx] - w[ry, rx]) > tie_rel * abs(w[ry, rx]):
+                bad.append((i, f"same map, position {(gy, gx)} vs {(ry, rx)}: {w[gy, gx]} vs {w[ry, rx]}"))
+            continue
+        if abs(rs[a] - best) > tie_rel * abs(best):
+            bad.append((i, f"map {a} ({rs[a]}) vs {b} ({best})"))
+    return bad
+
+
+def box128_case(g):
+    """Regenerate the box-128 fixture's job (checked against its input
+    checksums) and evaluate its candidate with the FP64 oracle."""
+    from oracle import gisapr_oracle as O
+    spec = syn.WORKLOADS[str(g["spec_name"])]
+    data = syn.make_job(spec, seed=int(g["seed"]), n_particles=int(g["n_particles"]))
+    im = data.images.astype(np.float64)
+    # numpy's transforms may round differently on another CPU architecture,
+    # so the regenerated images are compared to float32 precision
+    np.testing.assert_allclose([im.sum(), (im ** 2).sum()], g["image_checksum"], rtol=1e-6, atol=1e-6)
+    np.testing.assert_allclose(data.images[:, 64, 64], g["image_probe"], rtol=1e-5, atol=1e-6)
+    rd = data.records
+    ora = O.evaluate_candidate(data.model.pdb_text, g["pose"], spec.box, spec.apix, spec.res, data.model_rot,
+                               data.model_tilt, data.images, rd.line_index, rd.rot, rd.tilt, rd.psi,
+                               rd.defocus_u, rd.defocus_v, rd.defocus_angle, data.fsc, spec.mask_radius,
+                               spec.mask_edge, spec.psi_step, spec.local_range, spec.crop, kk=spec.kk,
+                               keep_templates=True)
+    return spec, data, ora
+
+
+def oracle_window(ora, crop):
+    """window(particle, entry_offset, psi) over the oracle's templates and
+    particle spectra (for argmax_mismatches)."""
+    from oracle import gisapr_oracle as O
+
+    def window(i, k, s):
+        p = ora["particles"][i]
+        t = ora["templates"][int(p["local"][k])]
+        return O.correlation_window(t[None], p["spectra"][s:s + 1], crop)[0, 0]
+    return window

@@ -47,6 +47,18 @@ def test_version_and_argument_errors_without_gpu(native_lib):
     assert rc == 1
 
 
+def test_noalloc_deposit_rejects_non_positive_parameters_without_gpu(native_lib):
+    """The no-allocation deposit checks apix, rp and kn (positive, finite)
+    before it touches the device."""
+    fake = C.c_void_p(16)
+    for apix, rp, kn in ((0.0, 1.0, 1.0), (1.5, 0.0, 1.0), (1.5, 1.0, -2.0), (1.5, float("nan"), 1.0),
+                         (1.5, 1.0, float("inf"))):
+        rc = native_lib.gisapr_deposit_noalloc(None, fake, fake, 4, fake, 32, 6, C.c_double(apix), C.c_double(rp),
+                                               C.c_double(kn))
+        assert rc == 1
+        assert b"positive and finite" in native_lib.gisapr_last_error()
+
+
 def test_cpu_device_is_rejected():
     from gisapr_gb300.pdb2mrc import density_from_coords
     with pytest.raises(ValueError):

@@ -16,7 +16,7 @@ from gisapr_gb300.search import (CorrelationWorkspace, IntegratedProjector, Pack
 from gisapr_gb300.tables import model_angles_from_lists  # noqa: E402
 from oracle import gisapr_oracle as O  # noqa: E402
 from tests.helpers import (CTF_ABS, DENSITY_RRMS, PEAK_REL, SCORE_REL, SPECTRUM_RRMS, TEMPLATE_RRMS,  # noqa: E402
-                           argmax_agrees, records_from_golden, records_from_job, rrms)
+                           argmax_agrees, argmax_mismatches, oracle_window, template_ref_rrms, records_from_golden, records_from_job, rrms)
 
 DEV = "cuda:0"
 
@@ -120,7 +120,8 @@ def test_templates_match_reference_and_oracle(golden32):
         errs_ref.append(rrms(tm[k], g["templates"][k]))
         ref = O.template_from_slice(O.central_slice(dft, g["rot_t"][k], 32), 32, 32, g["mask"], g["packed_fsc"])
         errs_or.append(rrms(tm[k], ref))
-    assert max(errs_ref) < TEMPLATE_RRMS, max(errs_ref)
+    print(f"box 32 templates: max rRMS {max(errs_or):.2e} from the oracle, {max(errs_ref):.2e} from the reference")
+    assert max(errs_ref) < template_ref_rrms(32), max(errs_ref)
     assert max(errs_or) < TEMPLATE_RRMS, max(errs_or)
     norms = np.sqrt((np.abs(tm) ** 2).sum(axis=(1, 2)))
     np.testing.assert_allclose(norms, 1.0, rtol=1e-5)
@@ -286,13 +287,19 @@ def test_scoring_job_box64_published_config(golden64):
     ora = O.evaluate_candidate(data.model.pdb_text, g["pose"], 64, 1.5, 3.0, data.model_rot, data.model_tilt,
                                data.images, rd.line_index, rd.rot, rd.tilt, rd.psi, rd.defocus_u, rd.defocus_v,
                                rd.defocus_angle, data.fsc, spec.mask_radius, spec.mask_edge, spec.psi_step,
-                               spec.local_range, spec.crop, kk=spec.kk, keep_templates=False)
+                               spec.local_range, spec.crop, kk=spec.kk, keep_templates=True)
+    ora_full = ora
     np.testing.assert_allclose(r["peak"][valid], ora["raw"], rtol=PEAK_REL)
     np.testing.assert_allclose(r["peak"][valid], g["peak"], rtol=2 * PEAK_REL)
     assert abs(score / ora["score"] - 1.0) < SCORE_REL
-    best_dir = np.asarray([job.needed[int(job.local_idx[e])] for e in r["best_entry"][valid]])
-    agree = np.mean(best_dir == g["best_dir"])
-    assert agree >= 0.99, agree
+    # per particle: (direction, psi, y, x) identical to the reference's first
+    # maximum, or a tie within 1e-5 (judged on the reference's map maxima, and
+    # inside one map on the oracle's exact crop window)
+    ptr = job.local_ptr.cpu().numpy()
+    np.testing.assert_array_equal(ptr, g["local_ptr"])
+    bad = argmax_mismatches(ptr, job.n_psi, g["scores"], g["ys"], g["xs"], r["best_entry"], r["best_psi"],
+                            r["peak_y"], r["peak_x"], window=oracle_window(ora_full, spec.crop))
+    assert not bad, bad
 
 
 def test_particles_without_directions_are_skipped(golden32):

@@ -9,7 +9,7 @@ import pytest
 
 from gisapr_gb300 import synthetic as syn
 from oracle import gisapr_oracle as O
-from tests.helpers import TEMPLATE_RRMS, rrms
+from tests.helpers import TEMPLATE_REF_FLOOR, rrms
 
 GOLDEN = Path(__file__).resolve().parent / "golden" / "golden_templates.npz"
 
@@ -37,4 +37,4 @@ def test_oracle_templates_match_reference(golden, n):
         # 8.0e-5 and 1.3e-4 relative RMS at 96, 192 and 256, spread over all
         # frequencies (float32-sized noise added to the oracle's volume
         # spectrum alone moves its box-256 template by 4.5e-5)
-        assert rrms(got, want[k]) < TEMPLATE_RRMS, (n, k, rrms(got, want[k]))
+        assert rrms(got, want[k]) < TEMPLATE_REF_FLOOR[n], (n, k, rrms(got, want[k]))

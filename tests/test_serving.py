@@ -116,14 +116,17 @@ def test_footprint_estimate_counts_spectra_and_banks():
 
 
 def test_footprint_counts_projector_scratch():
-    from gisapr_gb300.serving import projector_scratch_bytes
+    from gisapr_gb300.serving import CONTEXT_GROWTH_BOUND as G, projector_scratch_bytes
+    # a context's buffers grow by doubling and keep their predecessors: the
+    # bound is four times the request
+    assert G == 4
     # box 128: blocked spectrum (256 x 256 x 130 complex) + 768 planes of 128 x 150
-    assert projector_scratch_bytes(128, 128, 768) == 4 * 128 * 128 * 130 * 8 + 768 * 128 * 150 * 8
+    assert projector_scratch_bytes(128, 128, 768) == G * (4 * 128 * 128 * 130 * 8 + 768 * 128 * 150 * 8)
     # box 256: blocked spectrum, at most 4,096 flat planes, 304 CTA scratch planes
     small = projector_scratch_bytes(256, 256, 3072)
-    assert small == 4 * 256 * 256 * 258 * 8 + 3072 * 256 * 257 * 8 + 304 * (256 * 257 + 256 * 129) * 8
+    assert small == G * (4 * 256 * 256 * 258 * 8 + 3072 * 256 * 257 * 8 + 304 * (256 * 257 + 256 * 129) * 8)
     assert projector_scratch_bytes(256, 256, 20000) == projector_scratch_bytes(256, 256, 4096)
     # boxes 96 and 192: general-kernel scratch only
-    assert projector_scratch_bytes(96, 96, 10) == 10 * (96 * 97 + 96 * 49) * 8
-    assert projector_scratch_bytes(192, 192, 10000) == 456 * (192 * 193 + 192 * 97) * 8
+    assert projector_scratch_bytes(96, 96, 10) == G * 10 * (96 * 97 + 96 * 49) * 8
+    assert projector_scratch_bytes(192, 192, 10000) == G * 456 * (192 * 193 + 192 * 97) * 8
     assert job_footprint_bytes(256, 256, 4000, 3, 3072, 8) - small > 0

@@ -16,8 +16,9 @@ then one batched correlation over every slot (tensor-core form with
 ``options['precision']`` "fp16x3" or "fp16"), replayed as a CUDA graph when
 the batch is full. Other models (a whole PDB, centred or y-flipped
 densities) get their density from generate_volume and are scored one at a
-time. Given ``orientation_rows`` (a bank written by a calibration run), each
-particle searches only the bank's directions (orientation_bank_v1.py:62-79);
+time. Given ``orientation_rows`` (the rows of a bank written by a
+calibration run; see orientation_bank), each particle searches only the
+bank's directions (orientation_bank_v1.py:71-90);
 the prepared particle spectra stay resident and only the direction lists
 change.
 
@@ -37,6 +38,7 @@ import numpy as np
 import torch
 
 from .engine import BatchScoringJob, ScoringJob
+from .orientation_bank import ranked_row, restricted_indices
 from .pdb2mrc import MovedChainDensity, generate_volume
 from .standalone import ParticleMRCReader, job_config
 from .tables import (build_local_orientation_entries, read_fsc_map, read_model_angles, read_particle_table,
@@ -51,50 +53,6 @@ def file_key(path: str):
     """Identity of an input file: resolved path, size and modification time."""
     st = os.stat(path)
     return (os.path.realpath(path), st.st_size, st.st_mtime_ns)
-
-
-def restricted_indices(row, rec, allowed: Sequence[int], angles, keep: int) -> List[int]:
-    """Direction indices of one particle from a bank row, validated against
-    the particle's image, its allowed directions and the angle grid
-    (orientation_bank_v1.py:62-79)."""
-    if row is None or row["image"] != rec.image_name:
-        raise ValueError(f"Missing or mismatched bank entry at STAR line {rec.line_index}")
-    directions = row["directions"]
-    if (not directions and allowed) or len(directions) > min(keep, len(allowed)):
-        raise ValueError(f"Invalid direction count at STAR line {rec.line_index}")
-    allowed = set(allowed)
-    seen = set()
-    out = []
-    for i, rot, tilt, score in directions:
-        if (type(i) is not int or i not in allowed or (rot, tilt) in seen
-                or (rot, tilt) != (angles.rot[i], angles.tilt[i]) or not math.isfinite(score)):
-            raise ValueError(f"Invalid bank direction at STAR line {rec.line_index}")
-        seen.add((rot, tilt))
-        out.append(i)
-    return sorted(out)
-
-
-def ranked_row(rec, indices: Sequence[int], angles, peaks, keep: int) -> dict:
-    """Top ``keep`` distinct (rot, tilt) directions of one particle by their
-    peak over psi and translation, ties in grid order
-    (orientation_bank_v1.py:82-99). ``peaks``: one value per entry of
-    ``indices`` (already maximised over psi)."""
-    peaks = np.asarray(peaks.cpu() if torch.is_tensor(peaks) else peaks, dtype=np.float64).reshape(-1)
-    if np.isinf(peaks).any():
-        raise ValueError(f"Infinite directional peak at STAR line {rec.line_index}")
-    if np.isnan(peaks).any():
-        return dict(image=rec.image_name, directions=[], invalid_rawcc=True)
-    directions, seen = [], set()
-    for j in np.argsort(-peaks, kind="stable"):
-        i = int(indices[j])
-        pair = (angles.rot[i], angles.tilt[i])
-        if pair in seen:
-            continue
-        seen.add(pair)
-        directions.append([i, *pair, float(np.float32(peaks[j]))])
-        if len(directions) == keep:
-            break
-    return dict(image=rec.image_name, directions=directions)
 
 
 class _Context:

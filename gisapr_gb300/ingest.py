@@ -197,10 +197,10 @@ def create_gridsearch_parser() -> argparse.ArgumentParser:
 
 def _star_blocks(lines: List[str]):
     """Loops of a STAR file: (labels -> column, header end, data line indices)."""
-    from .tables import find_star_loop
-    parts = find_star_loop(lines, ["_rlnImageName"])
+    from .tables import find_star_table
+    parts = find_star_table(lines, ["_rlnImageName"])
     try:
-        optics = find_star_loop(lines, ["_rlnImagePixelSize"])
+        optics = find_star_table(lines, ["_rlnImagePixelSize"])
     except ValueError:
         optics = None
     return parts, optics
@@ -221,14 +221,14 @@ def run_preprocess(args) -> Dict[str, object]:
     from .tables import read_text_lines
     lines = read_text_lines(args.star_name)
     parts, optics = _star_blocks(lines)
-    lab = parts.labels
+    lab = parts.columns
     ii = lab["_rlnImageName"]
     ox, oy = lab.get("_rlnOriginXAngst", -1), lab.get("_rlnOriginYAngst", -1)
     if optics is None:
         raise ValueError("the STAR file has no optics loop with _rlnImagePixelSize")
-    opt_rows = list(optics.data_line_indices)
-    pixel = float(optics.tokens(opt_rows[0])[optics.labels["_rlnImagePixelSize"]])
-    rows = list(parts.data_line_indices)
+    opt_rows = list(optics.row_lines)
+    pixel = float(optics.tokens(opt_rows[0])[optics.columns["_rlnImagePixelSize"]])
+    rows = list(parts.row_lines)
     names = [parts.tokens(r)[ii] for r in rows]
     root = args.output_root_name + "_"
     crop = int(args.newboxsize)
@@ -301,8 +301,8 @@ def run_preprocess(args) -> Dict[str, object]:
                     line = _set_token(line, ox, "0.0")
                 if oy >= 0:
                     line = _set_token(line, oy, "0.0")
-        elif i in opt_rows and "_rlnImageSize" in optics.labels and size > 0:
-            line = _set_token(line, optics.labels["_rlnImageSize"], str(size))
+        elif i in opt_rows and "_rlnImageSize" in optics.columns and size > 0:
+            line = _set_token(line, optics.columns["_rlnImageSize"], str(size))
         out_lines.append(line if line.endswith("\n") else line + "\n")
     star_out = args.output_root_name + ".star"
     with open(star_out, "w") as fh:

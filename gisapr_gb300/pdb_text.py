@@ -9,86 +9,148 @@ round trip of the moved chain run on the GPU inside the splat launch
 """
 from __future__ import annotations
 
+import math
 import os
 from dataclasses import dataclass
+from functools import lru_cache
 
 import numpy as np
 
-_ELEMENTS = set((
-    "H HE LI BE B C N O F NE NA MG AL SI P S CL AR K CA SC TI V CR MN FE "
-    "CO NI CU ZN GA GE AS SE BR KR RB SR Y ZR NB MO TC RU RH PD AG CD IN "
-    "SN SB TE I XE CS BA LA CE PR ND PM SM EU GD TB DY HO ER TM YB LU HF "
-    "TA W RE OS IR PT AU HG TL PB BI PO AT RN FR RA AC TH PA U NP PU AM "
-    "CM BK CF ES FM MD NO LR RF DB SG BH HS MT DS RG CN NH FL MC LV TS OG D").split())
+# Element symbols by period of the periodic table (Z = 1..118), plus "D"
+# for deuterium. The element column and the atom-name rules below pick from
+# this set; anything else counts as no element (weight 0 in the density).
+_PERIODS = (
+    "H He",
+    "Li Be B C N O F Ne",
+    "Na Mg Al Si P S Cl Ar",
+    "K Ca Sc Ti V Cr Mn Fe Co Ni Cu Zn Ga Ge As Se Br Kr",
+    "Rb Sr Y Zr Nb Mo Tc Ru Rh Pd Ag Cd In Sn Sb Te I Xe",
+    "Cs Ba La Ce Pr Nd Pm Sm Eu Gd Tb Dy Ho Er Tm Yb Lu Hf Ta W Re Os Ir Pt Au Hg Tl Pb Bi Po At Rn",
+    "Fr Ra Ac Th Pa U Np Pu Am Cm Bk Cf Es Fm Md No Lr Rf Db Sg Bh Hs Mt Ds Rg Cn Nh Fl Mc Lv Ts Og",
+)
+KNOWN_ELEMENTS = frozenset(sym.upper() for period in _PERIODS for sym in period.split()) | {"D"}
+
+# Atom names that start in column 13 with one of these letters are that
+# element in ATOM records (protein and nucleic-acid atom names), even when
+# the first two letters would spell another element (" CA " vs "CA  ").
+_ORGANIC_LEADS = frozenset("CNOHPS")
+
+
+@lru_cache(maxsize=4096)
+def _element_of(element_field: str, name_field: str, is_atom: bool) -> str:
+    """Element of one atom from its element columns (77-78), its atom-name
+    columns (13-16) and whether the record is ATOM. Decision order:
+
+    1. a recognised symbol in the element columns wins;
+    2. the alphabetic characters of the name decide otherwise, none -> "";
+    3. a name whose first column is blank or a digit is aligned as a
+       one-letter element: its first letter;
+    4. in ATOM records a leading C, N, O, H, P or S is that element;
+    5. else the first two letters if they spell an element, else the first.
+    """
+    sym = element_field.strip().upper()
+    if sym in KNOWN_ELEMENTS:
+        return sym
+    name = name_field.ljust(4).upper()
+    alpha = [ch for ch in name if ch.isalpha()]
+    if not alpha:
+        return ""
+    lead = name[0]
+    if lead.isspace() or lead.isdigit():
+        choices = (alpha[0],)
+    elif is_atom and alpha[0] in _ORGANIC_LEADS:
+        choices = (alpha[0],)
+    else:
+        choices = ("".join(alpha[:2]), alpha[0])
+    return next((c for c in choices if c in KNOWN_ELEMENTS), "")
 
 
 def infer_element(line: str) -> str:
-    explicit = line[76:78].strip().upper()
-    if explicit in _ELEMENTS:
-        return explicit
-    name = line[12:16].ljust(4).upper()
-    letters = "".join(ch for ch in name if ch.isalpha())
-    if not letters:
-        return ""
-    if name[0].isspace() or name[0].isdigit():
-        return letters[0] if letters[0] in _ELEMENTS else ""
-    if line[:6] == "ATOM  " and letters[0] in "CNOHPS":
-        return letters[0]
-    if letters[:2] in _ELEMENTS:
-        return letters[:2]
-    return letters[0] if letters[0] in _ELEMENTS else ""
+    """Element of one ATOM/HETATM line (upper case, "" when unknown)."""
+    return _element_of(line[76:78], line[12:16], line[:6] == "ATOM  ")
 
 
-@dataclass
-class PDBText:
+@dataclass(frozen=True)
+class PdbAtoms:
+    """The selected atom records of a PDB text, in file order: the text's
+    lines, xyz (float32), element, chain id and the line each atom came from.
+    Identifiers other than the chain are never interpreted."""
+
     lines: list
-    coords: np.ndarray          # [n, 3] float32
-    elements: np.ndarray        # [n] U2
-    chains: np.ndarray          # [n] U1
-    atom_line_indices: np.ndarray
+    coords: np.ndarray             # [n, 3] float32
+    elements: np.ndarray           # [n] U2
+    chains: np.ndarray             # [n] U1
+    atom_line_indices: np.ndarray  # [n] int64
+
+    def __len__(self) -> int:
+        return int(self.coords.shape[0])
 
 
-def parse_pdb_lines(lines, include_hetatm=True, first_model_only=True, source="<text>") -> PDBText:
-    first_model = next((i for i, l in enumerate(lines) if l[:6].strip() == "MODEL"), None)
-    active = first_model is None
-    coords, els, chains, idx = [], [], [], []
-    kinds = ("ATOM", "HETATM") if include_hetatm else ("ATOM",)
-    for i, line in enumerate(lines):
-        rec = line[:6].strip()
-        if rec == "MODEL":
-            if first_model_only and i != first_model:
-                break
-            active = True
-            continue
-        if rec == "ENDMDL" and first_model is not None:
-            if first_model_only:
-                break
-            active = False
-            continue
-        if not active or rec not in kinds:
-            continue
+# the reference's name for the same record set
+PDBText = PdbAtoms
+
+
+def _selected_line_mask(tags, first_model_only: bool) -> np.ndarray:
+    """Lines inside the selected models. ``tags`` are the stripped record
+    names (columns 1-6). Without MODEL records the whole text is one model.
+    Otherwise lines count only inside a MODEL ... ENDMDL span; with
+    ``first_model_only`` reading ends at the first ENDMDL or at the second
+    MODEL, whichever comes first."""
+    n = len(tags)
+    model_at = [i for i, t in enumerate(tags) if t == "MODEL"]
+    if not model_at:
+        return np.ones(n, dtype=bool)
+    inside = np.zeros(n, dtype=bool)
+    if first_model_only:
+        ends = [i for i, t in enumerate(tags) if t == "ENDMDL"] + model_at[1:2]
+        stop = min(ends) if ends else n
+        if stop > model_at[0]:
+            inside[model_at[0] + 1:stop] = True
+        return inside
+    state = False
+    for i, t in enumerate(tags):
+        if t == "MODEL":
+            state = True
+        elif t == "ENDMDL":
+            state = False
+        else:
+            inside[i] = state
+    return inside
+
+
+def parse_pdb_lines(lines, include_hetatm=True, first_model_only=True, source="<text>") -> PdbAtoms:
+    """Atom records of ``lines`` (ATOM, and HETATM unless excluded) in the
+    selected models. Raises ValueError naming the line when a coordinate
+    field does not parse or is not finite."""
+    tags = [ln[:6].strip() for ln in lines]
+    wanted = {"ATOM", "HETATM"} if include_hetatm else {"ATOM"}
+    inside = _selected_line_mask(tags, first_model_only)
+    rows = [i for i, t in enumerate(tags) if inside[i] and t in wanted]
+    xyz = np.empty((len(rows), 3), dtype=np.float64)
+    for k, i in enumerate(rows):
+        ln = lines[i]
         try:
-            xyz = [float(line[s:s + 8]) for s in (30, 38, 46)]
+            v = (float(ln[30:38]), float(ln[38:46]), float(ln[46:54]))
         except ValueError as exc:
-            raise ValueError("Invalid PDB coordinates in %s, line %d" % (source, i + 1)) from exc
-        if not np.all(np.isfinite(xyz)):
-            raise ValueError("Non-finite PDB coordinates in %s, line %d" % (source, i + 1))
-        coords.append(xyz)
-        els.append(infer_element(line))
-        chains.append(line[21:22] or " ")
-        idx.append(i)
-    return PDBText(lines, np.asarray(coords, dtype=np.float32).reshape(-1, 3),
-                   np.asarray(els, dtype="U2"), np.asarray(chains, dtype="U1"),
-                   np.asarray(idx, dtype=np.int64))
+            raise ValueError(f"{source}, line {i + 1}: columns 31-54 do not hold three coordinates") from exc
+        if not all(map(math.isfinite, v)):
+            raise ValueError(f"{source}, line {i + 1}: coordinates are not finite")
+        xyz[k] = v
+    elements = [infer_element(lines[i]) for i in rows]
+    chains = [lines[i][21:22] or " " for i in rows]
+    return PdbAtoms(list(lines), xyz.astype(np.float32).reshape(-1, 3), np.asarray(elements, dtype="U2"),
+                    np.asarray(chains, dtype="U1"), np.asarray(rows, dtype=np.int64))
 
 
-def read_pdb(path, include_hetatm=True, first_model_only=True) -> PDBText:
+def read_pdb(path, include_hetatm=True, first_model_only=True) -> PdbAtoms:
+    """Atom records of a PDB file (see parse_pdb_lines); the text is kept
+    byte for byte (undecodable bytes survive as surrogates)."""
     with open(path, "r", encoding="utf-8", errors="surrogateescape", newline="") as fh:
         lines = fh.readlines()
     return parse_pdb_lines(lines, include_hetatm, first_model_only, os.fspath(path))
 
 
-def read_pdb_text(text: str, include_hetatm=True, first_model_only=True) -> PDBText:
+def read_pdb_text(text: str, include_hetatm=True, first_model_only=True) -> PdbAtoms:
     return parse_pdb_lines(text.splitlines(keepends=True), include_hetatm, first_model_only)
 
 
@@ -141,8 +203,8 @@ class ChainSplit:
     pivot: np.ndarray           # [3] float32 mean of the chain's first-model atoms (HETATM included)
 
 
-def split_moving_chain(pdb: PDBText, chain_id: str, include_hetatm: bool = False,
-                       density_pdb: PDBText = None) -> ChainSplit:
+def split_moving_chain(pdb: PdbAtoms, chain_id: str, include_hetatm: bool = False,
+                       density_pdb: PdbAtoms = None) -> ChainSplit:
     """Split density atoms into the moving chain and the fixed rest, keeping
     the pose pivot of transformed_density_atoms (Lite pdb_text.py:204-223):
     the float32 mean over the chain's first-model atoms."""

@@ -19,7 +19,10 @@ one records launch. Text is formatted on the host from the per-particle
 maxima. Tuning switches of the reference that select its own batching
 (``--ctfBatchSize``, ``--chunkSizeA/B``, ``--projectionBatchSize``,
 ``--psiGridBuildBatch``, ``--ctfBackend``, ``--torchThreads``) are accepted
-and have no effect on the result.
+and have no effect on the result. ``--orientations-out`` writes each
+particle's Top-K directions (``--keep-orientations``) to a bank file and
+``--orientations-in`` restricts every particle to its bank's directions, in
+the Lite tree's bank format (see orientation_bank).
 """
 from __future__ import annotations
 
@@ -29,6 +32,7 @@ import pickle
 import sys
 import threading
 import time
+from pathlib import Path
 from typing import Dict, List, Optional, Sequence
 
 import numpy as np
@@ -36,6 +40,7 @@ import torch
 
 from .engine import JobConfig, ScoringJob
 from .mrc import read_mrc, read_mrc_volume
+from .orientation_bank import bank_settings, pack_bank, ranked_row, read_bank, restricted_indices, write_bank
 from .tables import (ModelAngles, ParticleRecord, build_local_orientation_entries, psi_sampling_for_record,
                      read_fsc_map, read_model_angles, read_particle_table, select_particle_records)
 
@@ -84,7 +89,21 @@ def create_search_parser() -> argparse.ArgumentParser:
     p.add_argument("--profileStages", action="store_true")
     p.add_argument("--particleChunkMB", type=float, default=16384.0,
                    help="Device memory for one chunk of prepared particle spectra")
+    p.add_argument("--keep-orientations", dest="keep_orientations", type=_positive_int, default=3,
+                   help="K of the Top-K direction bank")
+    bank = p.add_mutually_exclusive_group()
+    bank.add_argument("--orientations-in", dest="orientations_in", metavar="JSON",
+                      help="Score only the directions saved in this calibration bank")
+    bank.add_argument("--orientations-out", dest="orientations_out", metavar="JSON",
+                      help="Calibrate: write each particle's Top-K directions to this bank")
     return p
+
+
+def _positive_int(text: str) -> int:
+    v = int(text)
+    if v < 1:
+        raise argparse.ArgumentTypeError("must be >= 1")
+    return v
 
 
 def choose_device(gpuid) -> torch.device:
@@ -268,7 +287,7 @@ def run_search(args, *, model_volume=None, verbose: bool = True) -> Dict[str, fl
     selected = select_particle_records(table, args.start, args.end)
     say("Model orientation count:", len(angles.rot))
     say("Selected particle count:", len(selected))
-    say("Particle STAR data start line:", table.loop.data_start)
+    say("Particle STAR data start line:", table.loop.first_row)
     t_local = time.perf_counter()
     if args.doLocalSearch:
         local_map = load_or_build_local_orientation_map(args.p, table.records, angles, float(args.localRange))
@@ -276,6 +295,18 @@ def run_search(args, *, model_volume=None, verbose: bool = True) -> Dict[str, fl
     else:
         every = list(range(len(angles.rot)))
         local_map = {rec.line_index: every for rec in selected}
+    bank_in, bank_out = getattr(args, "orientations_in", None), getattr(args, "orientations_out", None)
+    keep = int(getattr(args, "keep_orientations", 3))
+    settings = None
+    if bank_in or bank_out:
+        settings = bank_settings(args.p, args.ang, keep, bool(args.doLocalSearch), float(args.localRange),
+                                 float(args.psiStep))
+    if bank_in:
+        rows = read_bank(bank_in, settings)
+        local_map = {rec.line_index: restricted_indices(rows.get(str(rec.line_index)), rec,
+                                                        local_map.get(rec.line_index, []), angles, keep)
+                     for rec in selected}
+    ranked: Dict[str, dict] = {}
     for rec in selected:
         if not local_map.get(rec.line_index):
             print(f"WARNING: no model orientations for particle STAR line {rec.line_index}; skipping",
@@ -313,6 +344,8 @@ def run_search(args, *, model_volume=None, verbose: bool = True) -> Dict[str, fl
                 times["setup_s"] += time.perf_counter() - t0
                 t0 = time.perf_counter()
                 score += job.score_volume(volume)
+                if bank_out:
+                    ranked.update(_bank_rows(job, angles, keep))
                 times["search_s"] += time.perf_counter() - t0
                 t0 = time.perf_counter()
                 out.write(job.search_text())
@@ -324,6 +357,10 @@ def run_search(args, *, model_volume=None, verbose: bool = True) -> Dict[str, fl
             prefetch.thread.join()
         reader.close()
     torch.cuda.synchronize(device)
+    if bank_out:
+        if any(r.get("invalid_rawcc") for r in ranked.values()):
+            raise ValueError("a calibration peak is NaN: no orientation bank is written")
+        write_bank(bank_out, pack_bank(settings, ranked, mrc=str(Path(args.mrc).resolve())))
     times["total_search_s"] = time.perf_counter() - t_search
     times["total_s"] = time.perf_counter() - t_total
     times["particles"] = float(len(selected))
@@ -335,6 +372,19 @@ def run_search(args, *, model_volume=None, verbose: bool = True) -> Dict[str, fl
         say("Particle preparation (setup) time =", round(times["setup_s"], 6), "seconds")
         say("Templates + correlation + records time =", round(times["search_s"], 6), "seconds")
     return times
+
+
+def _bank_rows(job: ScoringJob, angles, keep: int) -> Dict[str, dict]:
+    """Top-K bank rows of one chunk's particles from its per-map maxima
+    (maximised over psi per direction)."""
+    ptr = job.local_ptr.cpu().numpy()
+    peaks = job.score_buf[:max(1, job.nnz) * job.n_psi].view(-1, job.n_psi).amax(dim=1).cpu().numpy()
+    rows = {}
+    for i, rec in enumerate(job.records):
+        a, b = int(ptr[i]), int(ptr[i + 1])
+        rows[str(rec.line_index)] = (ranked_row(rec, job.local[i], angles, peaks[a:b], keep) if b > a
+                                     else {"image": rec.image_name, "directions": []})
+    return rows
 
 
 def main(argv=None) -> None:

@@ -19,82 +19,104 @@ _PI_REF = 3.14159265359  # literal used by the reference's Euler code (v606:170-
 
 # ---------------------------------------------------------------------------
 # STAR parsing (gisapr_star.py / v606:75-224)
+#
+# Every line is classified once; a table is then a "loop_" line, the label
+# lines after it and the data rows after those. The rules follow the
+# reference's reader, which the search's line indices depend on (records
+# are keyed by their STAR line): blank and "#" lines are skipped anywhere; a
+# label is "_name" optionally followed by "#k" (1-based column), otherwise
+# it takes the next column in order; rows end at the next "loop_", "data_"
+# or label line once a row has been seen (before the first row those lines
+# are skipped); a loop without every requested label is passed over.
 # ---------------------------------------------------------------------------
+
+_SKIP, _LOOP, _LABEL, _BLOCK, _ROW = range(5)
+
+
+def _line_kind(line: str) -> int:
+    s = line.strip()
+    if not s or s[0] == "#":
+        return _SKIP
+    low = s.lower()
+    if low == "loop_":
+        return _LOOP
+    if s[0] == "_":
+        return _LABEL
+    if low.startswith("data_"):
+        return _BLOCK
+    return _ROW
+
+
+def _label_column(tokens: Sequence[str], default: int) -> int:
+    """0-based column of a label line's tokens: the first "#k" token with
+    an integer k gives k - 1, else ``default``."""
+    for tok in tokens[1:]:
+        if tok[:1] != "#":
+            continue
+        try:
+            return int(tok[1:]) - 1
+        except ValueError:
+            continue
+    return default
 
 
 @dataclass
-class StarLoop:
+class StarTable:
+    """One STAR loop: the file's lines, each label's column and the line
+    indices of its data rows (``first_row`` is the first of them)."""
+
     lines: List[str]
-    labels: Dict[str, int]
-    data_line_indices: List[int]
-    data_start: int
+    columns: Dict[str, int]
+    row_lines: List[int]
+    first_row: int
 
     def tokens(self, line_index: int) -> List[str]:
         return self.lines[line_index].split()
 
 
-def _label_index(tokens: Sequence[str], fallback: int) -> int:
-    for tok in tokens[1:]:
-        if tok.startswith("#"):
-            try:
-                return int(tok[1:]) - 1
-            except ValueError:
-                pass
-    return fallback
-
-
-def find_star_loop(lines: List[str], required_labels: Sequence[str]) -> StarLoop:
-    """First loop_ holding every required label (v606:96-143)."""
-    required = set(required_labels)
+def find_star_table(lines: List[str], required_labels: Sequence[str]) -> StarTable:
+    """The first loop whose labels include every one of ``required_labels``
+    (v606:96-143). ValueError when no loop has them all, or when that loop
+    has no data rows."""
+    kinds = [_line_kind(ln) for ln in lines]
     n = len(lines)
-    i = 0
-    while i < n:
-        if lines[i].strip().lower() != "loop_":
-            i += 1
-            continue
-        labels: Dict[str, int] = {}
-        j = i + 1
-        fallback = 0
-        while j < n:
-            s = lines[j].strip()
-            if not s or s.startswith("#"):
-                j += 1
-                continue
-            if not s.startswith("_"):
-                break
-            toks = s.split()
-            labels[toks[0]] = _label_index(toks, fallback)
-            fallback += 1
-            j += 1
-        if not required.issubset(labels):
-            i = max(j, i + 1)
-            continue
-        data: List[int] = []
-        k = j
-        start = -1
-        while k < n:
-            s = lines[k].strip()
-            low = s.lower()
-            if low == "loop_" or low.startswith("data_") or s.startswith("_"):
-                if data:
-                    break
-                k += 1
-                continue
-            if not s or s.startswith("#"):
-                k += 1
-                continue
-            if start < 0:
-                start = k
-            data.append(k)
+    need = set(required_labels)
+    pos = 0
+    while True:
+        try:
+            head = kinds.index(_LOOP, pos)
+        except ValueError:
+            raise ValueError("no STAR loop has all of the labels " + ", ".join(required_labels)) from None
+        columns: Dict[str, int] = {}
+        k, n_labels = head + 1, 0
+        while k < n and kinds[k] in (_SKIP, _LABEL):
+            if kinds[k] == _LABEL:
+                toks = lines[k].split()
+                columns[toks[0]] = _label_column(toks, n_labels)  # a repeated label keeps its last column
+                n_labels += 1
             k += 1
-        if start < 0:
-            raise ValueError("Found a STAR loop with the required labels but no data rows: "
-                             + ", ".join(required_labels))
-        return StarLoop(lines, labels, data, start)
-    raise ValueError("Cannot find a STAR loop containing: " + ", ".join(required_labels))
+        if not need <= columns.keys():
+            pos = max(k, head + 1)
+            continue
+        rows: List[int] = []
+        while k < n:
+            kind = kinds[k]
+            if kind == _ROW:
+                rows.append(k)
+            elif kind != _SKIP and rows:
+                break
+            k += 1
+        if not rows:
+            raise ValueError("the STAR loop with labels " + ", ".join(required_labels) + " has no data rows")
+        return StarTable(lines, columns, rows, rows[0])
+
+
+# the reference's name of the same lookup
+find_star_loop = find_star_table
 
 
 def read_text_lines(filename: str) -> List[str]:
+    """Lines of a text file with their line ends (bad bytes replaced)."""
     with open(filename, "r", encoding="utf-8", errors="replace") as fh:
         return fh.readlines()
 
@@ -134,11 +156,11 @@ def model_angles_from_lists(rot: Sequence[float], tilt: Sequence[float],
 def read_model_angles(angle_star: str) -> ModelAngles:
     """Direction list of a RELION angle STAR (v606:190-224)."""
     lines = read_text_lines(angle_star)
-    loop = find_star_loop(lines, ["_rlnAngleRot", "_rlnAngleTilt"])
-    ri, ti = loop.labels["_rlnAngleRot"], loop.labels["_rlnAngleTilt"]
-    pi = loop.labels.get("_rlnAnglePsi", -1)
+    loop = find_star_table(lines, ["_rlnAngleRot", "_rlnAngleTilt"])
+    ri, ti = loop.columns["_rlnAngleRot"], loop.columns["_rlnAngleTilt"]
+    pi = loop.columns.get("_rlnAnglePsi", -1)
     rot, tilt, psi = [], [], []
-    for li in loop.data_line_indices:
+    for li in loop.row_lines:
         toks = loop.tokens(li)
         if max(ri, ti) >= len(toks):
             continue
@@ -165,7 +187,7 @@ class ParticleRecord:
 @dataclass
 class ParticleTable:
     lines: List[str]
-    loop: StarLoop
+    loop: StarTable
     records: List[ParticleRecord]
     records_by_line: Dict[int, ParticleRecord]
     has_ctf: bool
@@ -174,16 +196,16 @@ class ParticleTable:
 def read_particle_table(particle_star: str) -> ParticleTable:
     """Particle rows of a RELION STAR (v606:227-306)."""
     lines = read_text_lines(particle_star)
-    loop = find_star_loop(lines, ["_rlnImageName", "_rlnAngleRot", "_rlnAngleTilt"])
-    ii = loop.labels["_rlnImageName"]
-    ri, ti = loop.labels["_rlnAngleRot"], loop.labels["_rlnAngleTilt"]
-    pi = loop.labels.get("_rlnAnglePsi", -1)
-    du, dv, da = (loop.labels.get(k, -1) for k in ("_rlnDefocusU", "_rlnDefocusV", "_rlnDefocusAngle"))
+    loop = find_star_table(lines, ["_rlnImageName", "_rlnAngleRot", "_rlnAngleTilt"])
+    ii = loop.columns["_rlnImageName"]
+    ri, ti = loop.columns["_rlnAngleRot"], loop.columns["_rlnAngleTilt"]
+    pi = loop.columns.get("_rlnAnglePsi", -1)
+    du, dv, da = (loop.columns.get(k, -1) for k in ("_rlnDefocusU", "_rlnDefocusV", "_rlnDefocusAngle"))
     has_ctf = min(du, dv, da) >= 0
     recs: List[ParticleRecord] = []
     by_line: Dict[int, ParticleRecord] = {}
     need = max(ii, ri, ti)
-    for li in loop.data_line_indices:
+    for li in loop.row_lines:
         toks = loop.tokens(li)
         if need >= len(toks):
             continue
@@ -200,10 +222,10 @@ def read_particle_table(particle_star: str) -> ParticleTable:
 
 def select_particle_records(table: ParticleTable, start_line: int, end_line: int) -> List[ParticleRecord]:
     """Rows in [start, end) by STAR line (v606:309-318)."""
-    start = max(start_line, table.loop.data_start) if start_line >= 0 else table.loop.data_start
+    first = table.loop.first_row
+    start = max(start_line, first) if start_line >= 0 else first
     end = len(table.lines) if end_line < 0 else min(end_line, len(table.lines))
-    if end < table.loop.data_start:
-        end = table.loop.data_start
+    end = max(end, first)
     return [r for r in table.records if start <= r.line_index < end]
 
 
@@ -248,43 +270,54 @@ def build_local_orientation_entries(particle_records, model_rot, model_tilt, loc
 # ---------------------------------------------------------------------------
 
 
+def _centre_distance(shape: Tuple[int, int]) -> np.ndarray:
+    """Distance of every pixel from the centre pixel (shape // 2), float64
+    (the square root of the exact integer sum of squares)."""
+    cy, cx = int(shape[0]) // 2, int(shape[1]) // 2
+    dy = np.arange(int(shape[0]), dtype=np.int64)[:, None] - cy
+    dx = np.arange(int(shape[1]), dtype=np.int64)[None, :] - cx
+    return np.sqrt(dx * dx + dy * dy)
+
+
 def generate_soft_mask(shape: Tuple[int, int], radius: int, edge_width: int) -> np.ndarray:
-    center = np.asarray(shape) // 2
-    y, x = np.indices(shape)
-    d = np.sqrt((x - center[1]) ** 2 + (y - center[0]) ** 2)
-    m = np.zeros_like(d)
-    m[d <= radius] = 1.0
+    """Circular mask with a raised-cosine edge (v606:446-457): 1 within
+    ``radius`` of the centre pixel, 0.5 (1 + cos(pi (d - radius) / edge))
+    out to ``radius + edge``, 0 beyond; float32."""
+    d = _centre_distance(shape)
+    inside = d <= radius
     if edge_width > 0:
-        e = (d > radius) & (d <= radius + edge_width)
-        m[e] = 0.5 * (1.0 + np.cos(np.pi * (d[e] - radius) / edge_width))
-    return m.astype(np.float32, copy=False)
+        rim = ~inside & (d <= radius + edge_width)
+        taper = 0.5 * (1.0 + np.cos(np.pi * (d - radius) / edge_width))
+        m = np.where(inside, 1.0, np.where(rim, taper, 0.0))
+    else:
+        m = inside.astype(np.float64)
+    return m.astype(np.float32)
 
 
 def expand_radial_values(values, size: int) -> np.ndarray:
+    """size x size float32 map whose pixel holds values[k], k the integer
+    part of its distance from the centre pixel; 0 where k runs past the
+    values (v606:460-468)."""
     v = np.asarray(values, dtype=np.float32).reshape(-1)
-    c = size // 2
-    y, x = np.indices((size, size))
-    r = np.sqrt((y - c) ** 2 + (x - c) ** 2).astype(np.int64)
-    out = np.zeros((size, size), dtype=np.float32)
-    ok = r < v.shape[0]
-    out[ok] = v[r[ok]]
-    return out
+    k = _centre_distance((size, size)).astype(np.int64)
+    if v.size == 0:
+        return np.zeros((size, size), dtype=np.float32)
+    return np.where(k < v.size, v[np.minimum(k, v.size - 1)], np.float32(0.0)).astype(np.float32)
 
 
 def read_fsc_map(fsc_filename: str, original_box: int, new_box: int, ignore_fsc: bool) -> np.ndarray:
+    """Centred new_box x new_box FSC weights from an FSC text (the second
+    column of every non-blank line is the value of shell 0, 1, ...), all
+    ones per shell when ``ignore_fsc`` or without a file (v606:471-491)."""
     if not fsc_filename:
-        values = np.ones(original_box, dtype=np.float32)
+        shells = np.ones(original_box, dtype=np.float32)
     else:
-        parsed = []
         with open(fsc_filename, "r", encoding="utf-8", errors="replace") as fh:
-            for line in fh:
-                toks = line.split()
-                if toks:
-                    parsed.append(1.0 if ignore_fsc else float(toks[1]))
-        if not parsed:
-            raise ValueError(f"No FSC values found in {fsc_filename}")
-        values = np.asarray(parsed, dtype=np.float32)
-    return expand_radial_values(values, new_box)
+            rows = [ln.split() for ln in fh]
+        shells = np.asarray([1.0 if ignore_fsc else float(r[1]) for r in rows if r], dtype=np.float32)
+        if shells.size == 0:
+            raise ValueError(f"{fsc_filename} holds no FSC values")
+    return expand_radial_values(shells, new_box)
 
 
 def centered_to_packed_np(centered: np.ndarray) -> np.ndarray:

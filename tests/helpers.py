@@ -186,9 +186,13 @@ def box128_case(g):
     data = syn.make_job(spec, seed=int(g["seed"]), n_particles=int(g["n_particles"]))
     im = data.images.astype(np.float64)
     # numpy's transforms may round differently on another CPU architecture,
-    # so the regenerated images are compared to float32 precision
-    np.testing.assert_allclose([im.sum(), (im ** 2).sum()], g["image_checksum"], rtol=1e-6, atol=1e-6)
-    np.testing.assert_allclose(data.images[:, 64, 64], g["image_probe"], rtol=1e-5, atol=1e-6)
+    # so the regenerated images are compared to float32 precision (the
+    # whitened images have zero mean: their plain sum is rounding noise on
+    # the scale of the sum of squares)
+    energy = float(g["image_checksum"][1])
+    assert abs(im.sum() - float(g["image_checksum"][0])) <= 1e-8 * energy
+    np.testing.assert_allclose((im ** 2).sum(), energy, rtol=1e-6)
+    np.testing.assert_allclose(data.images[:, 64, 64], g["image_probe"], rtol=1e-5, atol=1e-5)
     rd = data.records
     ora = O.evaluate_candidate(data.model.pdb_text, g["pose"], spec.box, spec.apix, spec.res, data.model_rot,
                                data.model_tilt, data.images, rd.line_index, rd.rot, rd.tilt, rd.psi,

@@ -71,7 +71,7 @@ def test_chunks_are_bitwise_equal(golden):
 
 def test_command_writes_stacks_and_star(golden, tmp_path):
     from gisapr_gb300.mrc import read_mrc, write_mrc
-    from gisapr_gb300.tables import find_star_loop, read_text_lines
+    from gisapr_gb300.tables import find_star_table, read_text_lines
     g = golden
     write_mrc(tmp_path / "in.mrcs", g["images"], 1.5)
     star = tmp_path / "in.star"
@@ -89,9 +89,9 @@ def test_command_writes_stacks_and_star(golden, tmp_path):
                           read_mrc(tmp_path / "out_0002.mrcs", mmap=False)])
     _close(got, g["whiten"])
     lines = read_text_lines(str(tmp_path / "out.star"))
-    parts = find_star_loop(lines, ["_rlnImageName"])
-    names = [parts.tokens(r)[0] for r in parts.data_line_indices]
+    parts = find_star_table(lines, ["_rlnImageName"])
+    names = [parts.tokens(r)[0] for r in parts.row_lines]
     assert names == [f"{k % 3 + 1}@{tmp_path / 'out'}_{k // 3 + 1:04d}.mrcs" for k in range(5)]
-    assert all(parts.tokens(r)[1] == "0.0" and parts.tokens(r)[2] == "0.0" for r in parts.data_line_indices)
-    optics = find_star_loop(lines, ["_rlnImagePixelSize"])
-    assert optics.tokens(optics.data_line_indices[0])[2] == "48"
+    assert all(parts.tokens(r)[1] == "0.0" and parts.tokens(r)[2] == "0.0" for r in parts.row_lines)
+    optics = find_star_table(lines, ["_rlnImagePixelSize"])
+    assert optics.tokens(optics.row_lines[0])[2] == "48"

@@ -170,3 +170,37 @@ def test_batch_search_engine_volume_models(golden32, tmp_path):
     from gisapr_gb300.pdb2mrc import generate_volume
     vol = generate_volume(pdb, spec.box, spec.apix, spec.res, device=DEV)
     assert out[0]["score"] == eng.context.job.score_volume(vol)
+
+
+def test_run_search_bank_files_calibrate_then_restricted(golden32, tmp_path):
+    """--orientations-out writes a bank in the reference's format (settings
+    by input hashes, digest) whose best direction per particle is the
+    reference's; --orientations-in then searches only the bank's directions
+    and writes the reference's records again, with the same score."""
+    import json
+    from gisapr_gb300 import orientation_bank as ob
+    g = golden32
+    bank_path = tmp_path / "bank.json"
+    args = write_search_inputs(tmp_path, g, extra=("--keep-orientations", "2", "--orientations-out",
+                                                   str(bank_path)))
+    cal = run_search(args, verbose=False)
+    settings = ob.bank_settings(args.p, args.ang, 2, True, args.localRange, args.psiStep)
+    bank = json.loads(bank_path.read_text())
+    ob.check_bank(bank, settings)
+    assert bank["mrc"] == str((tmp_path / "model.mrc").resolve())
+    for k, line in enumerate(g["rec_line"]):
+        row = bank["rows"][str(int(line))]
+        assert 1 <= len(row["directions"]) <= 2
+        assert row["directions"][0][0] == int(g["best_dir"][k])
+    args = write_search_inputs(tmp_path, g, extra=("--keep-orientations", "2", "--orientations-in",
+                                                   str(bank_path)))
+    res = run_search(args, verbose=False)
+    assert res["score"] == cal["score"]
+    # the records keep the reference's direction, psi and shifts (the z-score
+    # now runs over the bank's directions only)
+    _check_against_golden(parse_search_text(tmp_path / "search.txt"), g)
+    # a bank for other settings is refused
+    args = write_search_inputs(tmp_path, g, extra=("--keep-orientations", "3", "--orientations-in",
+                                                   str(bank_path)))
+    with pytest.raises(ValueError):
+        run_search(args, verbose=False)

@@ -67,7 +67,7 @@ def test_box128_templates(golden128, box128_case):
     packed_fsc = np.ascontiguousarray(O.centered_to_packed(O.radial_map(data.fsc, n)))
     proj = IntegratedProjector(DEV, n, n, PackedFourierLayout(n, spec.crop, DEV), _t(mask), _t(packed_fsc))
     sel = [int(k) for k in g["template_index"]]
-    tm = proj.build_templates(_t(ora["density"]), angles, orientation_indices=sel).cpu().numpy()
+    tm = proj.build_templates(_t(ora["density"].astype(np.float32)), angles, orientation_indices=sel).cpu().numpy()
     e_or = [rrms(tm[i], ora["templates"][k]) for i, k in enumerate(sel)]
     e_ref = [rrms(tm[i], g["templates"][i]) for i in range(len(sel))]
     print(f"box 128 templates: max rRMS {max(e_or):.2e} from the oracle, {max(e_ref):.2e} from the reference")

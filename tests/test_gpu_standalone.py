@@ -26,8 +26,9 @@ def _built():
     g.build()
 
 
-def _check_against_golden(rows, g):
-    """Search text records against the reference's values of the fixture."""
+def _check_against_golden(rows, g, check_z=True):
+    """Search text records against the reference's values of the fixture
+    (the z-score only with ``check_z``: it runs over the searched maps)."""
     assert len(rows) == len(g["z"])
     rot, tilt = np.asarray(g["model_rot"]), np.asarray(g["model_tilt"])
     for k, (cc, psi, raw) in enumerate(rows):
@@ -39,7 +40,8 @@ def _check_against_golden(rows, g):
         assert (cc[3], cc[4]) == (int(g["l3"][k]), int(g["accu"][k])), k
         assert abs(cc[7] - float(g["angdist"][k])) <= 1e-9 * max(1.0, abs(float(g["angdist"][k])))
         assert abs(raw[2] / float(g["peak"][k]) - 1.0) < PEAK_REL, k
-        assert abs(cc[2] - float(g["z"][k])) < 1e-3 * max(1.0, abs(float(g["z"][k]))), k
+        if check_z:
+            assert abs(cc[2] - float(g["z"][k])) < 1e-3 * max(1.0, abs(float(g["z"][k]))), k
 
 
 def test_run_search_matches_reference_records_golden32(golden32, tmp_path):
@@ -198,7 +200,7 @@ def test_run_search_bank_files_calibrate_then_restricted(golden32, tmp_path):
     assert res["score"] == cal["score"]
     # the records keep the reference's direction, psi and shifts (the z-score
     # now runs over the bank's directions only)
-    _check_against_golden(parse_search_text(tmp_path / "search.txt"), g)
+    _check_against_golden(parse_search_text(tmp_path / "search.txt"), g, check_z=False)
     # a bank for other settings is refused
     args = write_search_inputs(tmp_path, g, extra=("--keep-orientations", "3", "--orientations-in",
                                                    str(bank_path)))

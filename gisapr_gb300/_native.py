@@ -42,6 +42,8 @@ SIGNATURES = {
     "gisapr_tc_plan_work": [_p, _p, _i, _i, _i, _i, _p, _i, _p],
     "gisapr_correlate_tc_batch": [_p, _p, _p, C.c_longlong, _i, _i, _p, _p, _p, _p, _p, _i, _i, _i, _i, _i, _i,
                                   _p, _p, _p, _p],
+    "gisapr_correlate_tc_batch_ex": [_p, _p, _p, C.c_longlong, _i, _i, _p, _p, _p, _p, _p, _i, _i, _i, _i, _i, _i,
+                                     _p, _p, C.c_uint, _p, _p, _p, _p],
     "gisapr_restraint_edt": [_p, _p, _p, _i, _f, _p, _p, _p],
     "gisapr_ingest_stack": [_p, _p, _p, _i, _i, _i, _p, _i, _i, _i, _p, _p, _p, _i, _p, _p, _p],
     "gisapr_restraint_init": [_p, _p, _i],

@@ -78,11 +78,12 @@ int correlate_tc_max_n();
 size_t correlate_tc_smem_bytes(int n, int crop);
 long long correlate_tc_bank_halves(int n_slot, int n);
 int correlate_tc_plan(const int*, const int*, int, int, int, int, int*, int);
-cudaError_t launch_bank_to_fp16(cudaStream_t, const float2*, long long, int, int, int, void*);
+cudaError_t launch_bank_to_operands(cudaStream_t, const float2*, long long, int, int, int, int, const float*, void*,
+                                    int*);
 int correlate_tc_max_cand();
 cudaError_t launch_correlate_tc(cudaStream_t, const void*, int, const float2*, const int*, const int*, const int*,
-                                int, int, int, int, int, int, const float2*, const float2*, float*, int*, int*, int*,
-                                int);
+                                int, int, int, int, int, int, int, const float*, const float*, unsigned,
+                                const float2*, const float2*, float*, int*, int*, int*, int);
 
 namespace {
 
@@ -675,13 +676,16 @@ int gisapr_tc_plan_work(const int* local_ptr, const int* local_idx, int n_partic
   return GISAPR_OK;
 }
 
-int gisapr_correlate_tc_batch(gisapr_ctx ctx, void* stream, const float* bank, long long bank_stride, int n_cand,
-                              int n_slot, void* tbank, const float* stack, const int* local_ptr,
-                              const int* local_idx, const int* work, int n_work, int nnz, int n_psi, int n, int crop,
-                              int split, float* out_score, int* out_y, int* out_x, int* status) {
+int gisapr_correlate_tc_batch_ex(gisapr_ctx ctx, void* stream, const float* bank, long long bank_stride,
+                                 int n_cand, int n_slot, void* tbank, const float* stack, const int* local_ptr,
+                                 const int* local_idx, const int* work, int n_work, int nnz, int n_psi, int n,
+                                 int crop, int precision, const float* col_scale_t, const float* col_scale_p,
+                                 unsigned wait_limit, float* out_score, int* out_y, int* out_x, int* status) {
   if (!ctx) return fail(GISAPR_ERR_ARGUMENT, "context is NULL");
   if (n_cand < 0 || n_slot < 0 || n_work < 0 || nnz < 0 || n_psi <= 0)
     return fail(GISAPR_ERR_ARGUMENT, "n_cand, n_slot, n_work or nnz < 0, or n_psi <= 0");
+  if (precision < GISAPR_TC_FP16 || precision > GISAPR_TC_BF16X3)
+    return fail(GISAPR_ERR_ARGUMENT, "precision must be GISAPR_TC_FP16, _FP16X3, _BF16 or _BF16X3");
   if (n_cand == 0 || n_work == 0) return GISAPR_OK;
   if (!bank || !tbank || !stack || !local_ptr || !local_idx || !work || !out_score || !out_y || !out_x)
     return fail(GISAPR_ERR_ARGUMENT, "a required pointer is NULL");
@@ -702,14 +706,27 @@ int gisapr_correlate_tc_batch(gisapr_ctx ctx, void* stream, const float* bank, l
   rc = get_corr_tables(ctx, n, crop, &t);
   if (rc) return rc;
   const cudaStream_t st = (cudaStream_t)stream;
-  GISAPR_CHECK_CUDA(launch_bank_to_fp16(st, (const float2*)bank, bank_stride, n_cand, n_slot, n, tbank),
-                    "bank_to_fp16");
+  const int bf16 = (precision == GISAPR_TC_BF16 || precision == GISAPR_TC_BF16X3) ? 1 : 0;
+  const int split = (precision == GISAPR_TC_FP16X3 || precision == GISAPR_TC_BF16X3) ? 1 : 0;
+  GISAPR_CHECK_CUDA(launch_bank_to_operands(st, (const float2*)bank, bank_stride, n_cand, n_slot, n, bf16,
+                                            col_scale_t, tbank, status),
+                    "bank_to_operands");
   const int grid = std::min(n_work, ctx->sm_count);
   GISAPR_CHECK_CUDA(launch_correlate_tc(st, tbank, n_cand, (const float2*)stack, local_ptr, local_idx, work, n_work,
-                                        n_psi, n, crop, nnz, split, t.row, t.col, out_score, out_y, out_x, status,
-                                        grid),
+                                        n_psi, n, crop, nnz, split, bf16, col_scale_t, col_scale_p, wait_limit,
+                                        t.row, t.col, out_score, out_y, out_x, status, grid),
                     "correlate_tc");
   return GISAPR_OK;
+}
+
+int gisapr_correlate_tc_batch(gisapr_ctx ctx, void* stream, const float* bank, long long bank_stride, int n_cand,
+                              int n_slot, void* tbank, const float* stack, const int* local_ptr,
+                              const int* local_idx, const int* work, int n_work, int nnz, int n_psi, int n, int crop,
+                              int split, float* out_score, int* out_y, int* out_x, int* status) {
+  return gisapr_correlate_tc_batch_ex(ctx, stream, bank, bank_stride, n_cand, n_slot, tbank, stack, local_ptr,
+                                      local_idx, work, n_work, nnz, n_psi, n, crop,
+                                      split ? GISAPR_TC_FP16X3 : GISAPR_TC_FP16, nullptr, nullptr, 0, out_score, out_y,
+                                      out_x, status);
 }
 
 int gisapr_particle_results_batch(void* stream, const int* local_ptr, const float* score, const int* ys,

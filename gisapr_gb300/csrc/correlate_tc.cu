@@ -6,34 +6,45 @@
 // for rows m = (local direction, candidate) of one particle and its psi
 // angles s. For a fixed particle and column, stage 1 is a complex GEMM
 // between the rows' template columns T_m(., c) and U_{s,y}(r) = P_s(r,c) w^{ry},
-// shared by every candidate: in real form D[m][j] = sum_k A[m][k] B[j][k] with
-// A = [Re T | Im T] and B's row j = (s, y, part) holding [Re U | -Im U]
-// (part 0, Re Z) or [Im U | Re U] (part 1, Im Z). K (2n) is split into two
-// halves by row r (r < n/2, r >= n/2), each holding [Re | Im] of its rows.
+// shared by every candidate: in real form D[m][j] = sum_k A[m][k] B[j][k]. A
+// K step covers 32 rows r: its 64 K elements are [Re T of the 32 rows | Im T
+// of the 32 rows], and B's rows j = (s, crop-row pair, part) hold
+// [Re U | -Im U] (part 0, Re Z) or [Im U | Re U] (part 1, Im Z) on the same
+// K positions.
 //
-// Precision: both operands are scaled by 2^13 (every entry has modulus <= 1,
-// the packed spectra having unit L2 norm) and split into fp16 hi + lo parts;
-// the split form accumulates hi*hi + hi*lo + lo*hi in FP32 (three passes of
-// tcgen05.mma), which keeps about 22 significant bits per product. The single
-// form uses hi*hi only.
+// Precision. Operands are fp16 or bf16 (kind::f16 takes either, both sides
+// of one MMA the same type). Both are scaled by 2^13 times a power of two per
+// packed column (the template side's from the FSC weights of the column, the
+// particle side's from the job's largest coefficient of the column), so that
+// high-frequency columns keep fp16's normal range; stage 2 undoes the column
+// scales in FP32 through its twiddle table. The split forms store hi and lo
+// parts (x = hi + lo, both rounded to the operand type) and accumulate
+// hi*hi + hi*lo + lo*hi in FP32 over three MMA passes; the single forms keep
+// hi*hi.
 //
 // Work item: one particle, a tile of whole directions x all candidates
-// (row = direction_in_tile * n_cand + cand, n_cand <= 128) and a group of up
-// to three psi angles; the work list is sorted by direction so CTAs running
-// together share template columns in L2. Per column and K half, one lane
-// group of warp 0 issues bulk async copies of the rows' template chunks (the
-// fp16 bank copy is laid out [slot][col][half][part][k/8][cand][8], so each
-// direction's chunk is contiguous) into a two-stage shared-memory ring, all
-// warps build B for that half, and one thread issues the MMAs into one of two
-// TMEM accumulators (M=128, N=kN, K=16) and commits to mbarriers. The MMAs of
-// one half overlap the B build of the next; twelve warps read the previous
-// column from TMEM (tcgen05.ld) and accumulate stage 2 with packed FP32 FMAs
-// in registers; after the last column each thread takes the row-major first
-// maximum of its (row, psi) map. Operands use the K-major no-swizzle layout
-// with core matrices (8 rows x 16 bytes) stored K-chunk-major: SBO = 128 B
-// between 8-row groups, LBO = rows * 16 B between K chunks. Every mbarrier
-// wait is bounded; on timeout the kernel sets *status, waits (bounded) for
-// the MMAs in flight, frees TMEM and returns.
+// (row = direction_in_tile * ceil8(n_cand) + cand, n_cand <= 128) and a group
+// of up to three psi angles (two at crop 14); the work list is sorted by
+// direction so CTAs running together share template columns in L2.
+//
+// Warp roles (640 threads, 20 warps): warp 0 issues the MMAs (one lane),
+// warp 1 the bulk async copies (cp.async.bulk, mbarrier complete_tx) of the
+// rows' template chunks two steps ahead into a ring of shared-memory stages
+// (the operand bank is laid out [slot][col][step][part][cand][128 B], so
+// each direction's rows of a step are one contiguous copy), warps 2-7 build
+// B for each K step from the particle column (prefetched with cp.async two
+// columns ahead) and a twiddle recurrence, and warps 8-19 run stage 2: each
+// thread owns one (row, psi) map, reads the finished column accumulator from
+// TMEM (tcgen05.ld) and accumulates its crop rows, some in registers and the
+// rest in free TMEM columns. Two TMEM accumulators let the MMAs of a column
+// overlap stage 2 of the previous one. Operand tiles use the K-major
+// 128-byte-swizzle layout (8-row atoms of 1024 B).
+//
+// Every mbarrier hand-off wait is bounded by a launch parameter; when one
+// runs out the kernel sets *status, every role leaves its loop, the kernel
+// waits (with the default bound) for the bulk copies and MMAs it issued,
+// frees its TMEM and returns.
+#include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
 #include <algorithm>
@@ -43,11 +54,13 @@
 
 namespace {
 
-constexpr int kTcThreads = 512;   // 16 warps in four warpgroups (roles below)
+constexpr int kTcThreads = 640;   // 20 warps (roles above)
+constexpr int kTcBuildWarp0 = 2, kTcBuildWarps = 6;
+constexpr int kTcBuilders = kTcBuildWarps * 32;
+constexpr int kTcEpiWarp0 = 8, kTcEpiWarps = 12;
 constexpr int kTcM = 128;         // rows per tile (TMEM lanes)
 constexpr int kTcPsi = 3;         // psi angles per particle a tile holds at most
 constexpr int kTcMaxN = 256;      // K = 2n <= 512, in steps of 64 (32 rows r)
-constexpr int kTcStages = 4;      // shared-memory ring of K steps (at most)
 
 // psi angles per tile: three up to crop 12; at crop 14 two, so that the MMA
 // accumulators and the stage-2 rows kept in TMEM fit its 512 columns.
@@ -55,50 +68,58 @@ __host__ __device__ constexpr int tc_psi_group(int C) { return C <= 12 ? 3 : 2; 
 // shared-memory stages: four, three above n = 128 (larger particle columns and tables)
 __host__ __device__ constexpr int tc_stages(int N) { return N > 128 ? 3 : 4; }
 constexpr int kTcMaxCand = 128;   // candidates per launch
-constexpr int kTcTmemCols = 512;  // two MMA accumulators of kN <= 80 columns + stage-2 rows
-constexpr float kTcScale = 8192.0f;               // 2^13 on each operand
-constexpr float kTcUnscale = 1.0f / 67108864.0f;  // 2^-26 for the product
-constexpr unsigned kWaitLimit = 1u << 24;         // bounded mbarrier spin
+constexpr int kTcTmemCols = 512;
+constexpr float kTcScale = 8192.0f;       // 2^13 on each operand (times the column scale)
+constexpr unsigned kWaitLimit = 1u << 24; // default bound of a barrier wait (iterations)
 
 // TMEM / B-row stride of one psi angle: crop x (re, im), rounded up to 8 so
 // every tcgen05.ld starts on an 8-column boundary.
 __host__ __device__ constexpr int tc_psi_stride(int C) { return ((2 * C + 7) / 8) * 8; }
 // MMA N: all psi angles, rounded up to a multiple of 16.
 __host__ __device__ constexpr int tc_n(int C) { return ((tc_psi_group(C) * tc_psi_stride(C) + 15) / 16) * 16; }
+// crop rows of a stage-2 map held in registers (96 registers a thread);
+// the rest live in TMEM columns after the two MMA accumulators
+template <int C>
+__host__ __device__ constexpr int tc_reg_rows() { return C <= 6 ? C : (C == 8 || C == 12 ? 4 : 2); }
 
 struct TcParams {
-  const __half* tbank;    // [n_slot][H][2 halves][2 parts][n/8][n_cand][8], scaled
+  const void* tbank;      // [n_slot][H][NQ][2 parts][n_cand][128 B] operand bank (hi, lo)
   const float2* stack;    // [n_particles][n_psi][n][H]
   const int* local_ptr;
   const int* local_idx;
   const int* work;        // [n_work][2]: particle, tile * n_groups + psi group
-  int n_work, n_cand, n_psi, n, nnz, split, dpt;  // dpt: directions per tile
+  int n_work, n_cand, n_psi, n, nnz, split, bf16, dpt;  // dpt: directions per tile
   const float2* tw_row;   // [n]  exp(+2 pi i t / n)
   const float2* tw_col;   // [H][C]  w_c exp(+2 pi i c (x - h) / n)
+  const float* t_scale;   // [H] per-column template scale (power of two) or null
+  const float* p_scale;   // [H] per-column particle scale (power of two) or null
+  unsigned wait_limit;    // bound of a hand-off wait (iterations)
   float* out_score;       // [n_cand][nnz][n_psi]
   int* out_y;
   int* out_x;
-  int* status;            // set to 1 when an mbarrier wait ran out
+  int* status;            // set to 1 when a barrier wait ran out
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-// kind::f16 instruction descriptor: FP32 accumulate, F16 A and B, both K-major.
-__host__ __device__ constexpr uint32_t make_idesc(int M, int N) {
-  return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+// kind::f16 instruction descriptor: FP32 accumulate, A and B K-major, both
+// fp16 (formats 0) or both bf16 (formats 1).
+__host__ __device__ constexpr uint32_t make_idesc(int M, int N, int bf16) {
+  return (1u << 4) | ((uint32_t)bf16 << 7) | ((uint32_t)bf16 << 10) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(M >> 4) << 24);
 }
 
 __device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
 }
 
-// Wait for the barrier phase of the given parity with an iteration limit;
-// returns false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// Wait for the barrier phase of the given parity, at most ``limit``
+// attempts; returns false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned limit) {
   const uint32_t a = smem_u32(bar);
-  for (unsigned it = 0; it < kWaitLimit; ++it) {
+  for (unsigned it = 0; it < limit; ++it) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -111,6 +132,10 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
 
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes));
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
 // contiguous global -> shared copy on the async proxy, completion counted in bytes on bar
@@ -130,21 +155,26 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar)));
 }
 
-// fp16 hi/lo of 8 floats as 4 half2 words each
-__device__ __forceinline__ void split8(const float (&v)[8], uint4& hi, uint4& lo) {
-  uint32_t h[4], l[4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const __half2 a = __floats2half2_rn(v[2 * i], v[2 * i + 1]);
-    const float2 af = __half22float2(a);
-    const __half2 b = __floats2half2_rn(v[2 * i] - af.x, v[2 * i + 1] - af.y);
-    h[i] = *reinterpret_cast<const uint32_t*>(&a);
-    l[i] = *reinterpret_cast<const uint32_t*>(&b);
+// hi and lo words of two floats in the operand type: hi = round(a, b),
+// lo = round(a - hi, b - hi)
+template <bool BF>
+__device__ __forceinline__ void split2(float a, float b, uint32_t& hi, uint32_t& lo) {
+  if constexpr (BF) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    const float2 hf = __bfloat1622float2(h);
+    const __nv_bfloat162 l = __floats2bfloat162_rn(a - hf.x, b - hf.y);
+    hi = *reinterpret_cast<const uint32_t*>(&h);
+    lo = *reinterpret_cast<const uint32_t*>(&l);
+  } else {
+    const __half2 h = __floats2half2_rn(a, b);
+    const float2 hf = __half22float2(h);
+    const __half2 l = __floats2half2_rn(a - hf.x, b - hf.y);
+    hi = *reinterpret_cast<const uint32_t*>(&h);
+    lo = *reinterpret_cast<const uint32_t*>(&l);
   }
-  hi = make_uint4(h[0], h[1], h[2], h[3]);
-  lo = make_uint4(l[0], l[1], l[2], l[3]);
 }
 
+// sign flip of both 16-bit values (fp16 and bf16 keep the sign in bit 15)
 __device__ __forceinline__ uint4 neg8(uint4 v) {
   return make_uint4(v.x ^ 0x80008000u, v.y ^ 0x80008000u, v.z ^ 0x80008000u, v.w ^ 0x80008000u);
 }
@@ -156,19 +186,20 @@ __device__ __forceinline__ uint4 neg8(uint4 v) {
 // directly. Accumulator slots per crop row: 0: A_0, 1: raw(0), 2..h: A_1..A_{h-1},
 // h+1..2h-1: B_1..B_{h-1}. The per-column twiddle table (floats, 16-byte
 // groups) holds Re E(h), Re E(0), -Im E(0), a pad entry, then Re E(h+k),
-// Im E(h+k) for k = 1..h-1.
+// Im E(h+k) for k = 1..h-1, each divided by the column's operand scales.
 __host__ __device__ constexpr int tc_tw_entries(int C) { return ((C + 2 + 3) / 4) * 4; }
 
 // The twiddle loads are volatile so that they are not hoisted out of the
 // crop-row loop (that would hold the table in registers next to the
-// accumulators).
+// accumulators and spill).
 __device__ __forceinline__ float4 lds_v4(uint32_t addr) {
   float4 r;
   asm volatile("ld.shared.v4.f32 {%0,%1,%2,%3}, [%4];" : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w) : "r"(addr));
   return r;
 }
 
-// stage 2 for one crop row held in a[C] (Re Z = zr, Im Z = zi)
+// stage 2 for one crop row held in a[C] (Re Z = zr, Im Z = zi); tw: shared
+// address of the column's twiddle table
 template <int C>
 __device__ __forceinline__ void stage2_row(float (&a)[C], float zr, float zi, uint32_t tw) {
   constexpr int h = C / 2;
@@ -236,7 +267,7 @@ __device__ __forceinline__ void tmem_st_row(const float (&a)[C], uint32_t ta) {
   }
 }
 
-// raw(y, x) of a crop row from its accumulator slots (see stage2_pair)
+// raw(y, x) of a crop row from its accumulator slots (see stage2_row)
 template <int C>
 __device__ __forceinline__ float raw_at(const float (&a)[C], int x) {
   constexpr int h = C / 2;
@@ -246,9 +277,10 @@ __device__ __forceinline__ float raw_at(const float (&a)[C], int x) {
   return a[1 + (x - h)] - a[h + (x - h)];
 }
 
-// Entry j of column col's stage-2 twiddle table (see stage2_pair), times 2^-26.
+// Entry j of column col's stage-2 twiddle table (see stage2_row), divided by
+// the column's two operand scales.
 template <int C>
-__device__ __forceinline__ float tw_entry(const float2* __restrict__ tw_col, int col, int j) {
+__device__ __forceinline__ float tw_entry(const float2* __restrict__ tw_col, int col, int j, float unscale) {
   constexpr int h = C / 2;
   const float2* e = tw_col + (size_t)col * C;
   float v = 0.f;
@@ -259,7 +291,7 @@ __device__ __forceinline__ float tw_entry(const float2* __restrict__ tw_col, int
     const int k = 1 + (j - 4) / 2;
     v = ((j - 4) & 1) ? e[h + k].y : e[h + k].x;
   }
-  return v * kTcUnscale;
+  return v * unscale;
 }
 
 // tcgen05 shared-memory descriptor of a 128-byte-swizzled K-major tile
@@ -320,33 +352,64 @@ __device__ __forceinline__ uint32_t sw128(int j, int c) {
   return (uint32_t)(j * 128 + ((c ^ (j & 7)) << 4));
 }
 
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+// B for one K step: one task per (psi, crop row, 8-row block). Its eight
+// twiddles w^{r y} (a recurrence from the table entry of the block's first
+// row, times the operand and column scale) multiply the particle column's
+// eight rows; Re U and Im U go to the psi's Re-Z and Im-Z rows (Re U, -Im U
+// on the imaginary half of the Re-Z row).
+template <int C, int N, bool BF>
+__device__ __forceinline__ void build_b_step(unsigned char* stB, uint32_t b_part, const float2* sp,
+                                             const float2* s_twr, float scale, int qq, int g_psi, bool split,
+                                             int bt) {
+  constexpr int h = C / 2, n = N, kPS = tc_psi_stride(C);
+  const int tasks = g_psi * C * 4;
+  for (int t = bt; t < tasks; t += kTcBuilders) {
+    const int yi = t % C, rc = (t / C) & 3, s = t / (4 * C);
+    const int y = yi - h;
+    const int r0 = qq * 32 + rc * 8;
+    float2 tw = cscale(s_twr[((r0 * y) % n + n) % n], scale);
+    const float2 step = s_twr[(y % n + n) % n];
+    const float2* pp = sp + s * n + r0;
+    uint32_t hr[4], lr[4], hi_[4], li_[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const float2 u0 = cmul(pp[2 * i], tw);
+      tw = cmul(tw, step);
+      const float2 u1 = cmul(pp[2 * i + 1], tw);
+      tw = cmul(tw, step);
+      split2<BF>(u0.x, u1.x, hr[i], lr[i]);
+      split2<BF>(u0.y, u1.y, hi_[i], li_[i]);
+    }
+    // rows of psi s: per crop-row pair (Re y, Re y+1, Im y, Im y+1)
+    const int jr = s * kPS + 4 * (yi >> 1) + (yi & 1), ji = jr + 2;
+    const uint4 hre = make_uint4(hr[0], hr[1], hr[2], hr[3]), him = make_uint4(hi_[0], hi_[1], hi_[2], hi_[3]);
+    *reinterpret_cast<uint4*>(stB + sw128(jr, rc)) = hre;
+    *reinterpret_cast<uint4*>(stB + sw128(ji, 4 + rc)) = hre;
+    *reinterpret_cast<uint4*>(stB + sw128(ji, rc)) = him;
+    *reinterpret_cast<uint4*>(stB + sw128(jr, 4 + rc)) = neg8(him);
+    if (split) {
+      const uint4 lre = make_uint4(lr[0], lr[1], lr[2], lr[3]), lim = make_uint4(li_[0], li_[1], li_[2], li_[3]);
+      *reinterpret_cast<uint4*>(stB + b_part + sw128(jr, rc)) = lre;
+      *reinterpret_cast<uint4*>(stB + b_part + sw128(ji, 4 + rc)) = lre;
+      *reinterpret_cast<uint4*>(stB + b_part + sw128(ji, rc)) = lim;
+      *reinterpret_cast<uint4*>(stB + b_part + sw128(jr, 4 + rc)) = neg8(lim);
+    }
+  }
 }
 
-// Warp roles (16 warps, 128 registers a thread): warp 0 issues the MMAs (one
-// elected lane), warp 1 the bulk copies of A, warps 2-3 build B, and warps
-// 4-15 accumulate stage 2 (warp 4 + 4 s + q reads TMEM lane quarter q for
-// psi s). Stage-2 rows [0, tc_reg_rows) live in registers and the rest in
-// TMEM columns after the two MMA accumulators, so every role fits the
-// 65,536-register file without spilling.
-template <int C>
-__host__ __device__ constexpr int tc_reg_rows() { return C * C <= 100 ? C : ((96 / C) & ~1); }
-constexpr int kTcEpiWarps = 12;
-constexpr int kTcBuilders = 64;  // threads of warps 2-3
-
-template <int C, int N>
+template <int C, int N, bool BF>
 __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   static_assert(C % 2 == 0 && C <= 14, "even crop up to 14");
-  static_assert(kTcThreads == 512, "four warpgroups");
+  static_assert(kTcThreads == 32 * (kTcEpiWarp0 + kTcEpiWarps), "warp roles");
+  static_assert(kTcEpiWarps == 4 * 3, "three psi angles of four TMEM lane quarters");
   static_assert(2 * tc_n(C) + tc_psi_group(C) * (C - tc_reg_rows<C>()) * C <= kTcTmemCols, "TMEM columns");
   constexpr int kN = tc_n(C);
   constexpr int kPS = tc_psi_stride(C);
-  constexpr int h = C / 2;
   constexpr int S = tc_stages(N);
   constexpr int NQ = N / 32;               // K steps per column: 32 rows r (64 K) each
   constexpr int n = N, H = N / 2 + 1;
+  constexpr int TWE = tc_tw_entries(C);
   constexpr uint32_t a_part = kTcM * 128;  // bytes of A (hi or lo) per stage: 128 rows x 128 B
   constexpr uint32_t b_part = kN * 128;
   constexpr uint32_t stage_bytes = 2 * a_part + 2 * b_part;
@@ -356,26 +419,33 @@ __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
   unsigned char* stages = smem_raw;        // [S][A hi, A lo, B hi, B lo]
   float2* s_p = reinterpret_cast<float2*>(smem_raw + S * stage_bytes);  // [3][kTcPsi][n] particle columns
   float2* s_twr = s_p + 3 * kTcPsi * n;                        // [n]
-  float* s_twall = reinterpret_cast<float*>(s_twr + n);      // [H][tc_tw_entries] column tables
-  uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_twall + H * tc_tw_entries(C));
+  float* s_twall = reinterpret_cast<float*>(s_twr + n);      // [H][TWE] column tables
+  float* s_psc = s_twall + H * TWE;                           // [H] particle-side scale per column
+  uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_psc + ((H + 1) & ~1));
   uint64_t* bar_afull = s_bar;           // [S] A bytes landed (copy warp's expect_tx)
-  uint64_t* bar_bfull = s_bar + S;       // [S] both builder warps wrote B
+  uint64_t* bar_bfull = s_bar + S;       // [S] every builder warp wrote B
   uint64_t* bar_empty = s_bar + 2 * S;   // [S] the MMAs reading the stage are done
   uint64_t* bar_tfull = s_bar + 3 * S;   // [2] a column's accumulator is final
   uint64_t* bar_tempty = s_bar + 3 * S + 2;  // [2] every stage-2 warp read its accumulator
   uint32_t* s_taddr = reinterpret_cast<uint32_t*>(s_bar + 3 * S + 4);
   int* s_fail = reinterpret_cast<int*>(s_taddr + 1);
+  uint32_t* s_mma_steps = reinterpret_cast<uint32_t*>(s_fail + 1);   // K steps whose MMAs were committed
+  uint32_t* s_copy_steps = s_mma_steps + 1;                           // K steps whose A copies were issued
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   for (int t = tid; t < n; t += blockDim.x) s_twr[t] = P.tw_row[t];
-  for (int t = tid; t < H * tc_tw_entries(C); t += blockDim.x)
-    s_twall[t] = tw_entry<C>(P.tw_col, t / tc_tw_entries(C), t % tc_tw_entries(C));
+  for (int t = tid; t < H * TWE; t += blockDim.x) {
+    const int c = t / TWE;
+    const float ts = P.t_scale ? P.t_scale[c] : 1.0f, ps = P.p_scale ? P.p_scale[c] : 1.0f;
+    s_twall[t] = tw_entry<C>(P.tw_col, c, t % TWE, 1.0f / (kTcScale * kTcScale * ts * ps));
+  }
+  for (int t = tid; t < H; t += blockDim.x) s_psc[t] = kTcScale * (P.p_scale ? P.p_scale[t] : 1.0f);
   for (uint32_t t = tid; t < S * stage_bytes / 16; t += blockDim.x)
     reinterpret_cast<uint4*>(stages)[t] = make_uint4(0, 0, 0, 0);
   if (tid == 0) {
     for (int i = 0; i < S; ++i) {
       mbar_init(bar_afull + i, 1);
-      mbar_init(bar_bfull + i, 2);
+      mbar_init(bar_bfull + i, kTcBuildWarps);
       mbar_init(bar_empty + i, 1);
     }
     for (int i = 0; i < 2; ++i) {
@@ -383,6 +453,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
       mbar_init(bar_tempty + i, kTcEpiWarps);
     }
     *s_fail = 0;
+    *s_mma_steps = 0;
+    *s_copy_steps = 0;
     asm volatile("fence.mbarrier_init.release.cluster;");
   }
   if (warp == 0) {
@@ -395,202 +467,149 @@ __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t taddr = *s_taddr;
+  const unsigned limit = P.wait_limit;
 
   // bounded wait that gives up at once after any failure in the CTA
   auto wait = [&](uint64_t* bar, uint32_t parity) -> bool {
     if (*reinterpret_cast<volatile int*>(s_fail) != 0) return false;
-    const bool r = mbar_wait(bar, parity);
+    const bool r = mbar_wait(bar, parity, limit);
     if (!r) *reinterpret_cast<volatile int*>(s_fail) = 1;
     return r;
   };
 
-  if (warp < 4) {
-    if (warp == 0) {
-      // ---------------- MMA issue (one lane)
-      if (lane == 0) {
-        uint32_t g = 0, tuse[2] = {0, 0};
-        const uint32_t idesc = make_idesc(kTcM, kN);
-        bool ok = true;
-        for (int wi = blockIdx.x; wi < P.n_work && ok; wi += gridDim.x) {
-          for (int col = 0; col < H && ok; ++col) {
-            const int tb = col & 1;
-            for (int qq = 0; qq < NQ && ok; ++qq, ++g) {
-              const uint32_t st = g % S;
-              if (qq == 0 && tuse[tb] > 0) ok = wait(bar_tempty + tb, (tuse[tb] - 1) & 1u);
-              ok = ok && wait(bar_bfull + st, (g / S) & 1u) && wait(bar_afull + st, (g / S) & 1u);
-              if (!ok) break;
-              asm volatile("tcgen05.fence::after_thread_sync;");
-              const uint32_t a0s = smem_u32(stages + st * stage_bytes);
-              issue_mma_step(taddr + (uint32_t)(tb * kN), a0s, a0s + 2 * a_part, a_part, b_part, idesc,
-                             P.split ? 3 : 1, qq > 0);
-              mma_commit(bar_empty + st);
-              if (qq == NQ - 1) {
-                mma_commit(bar_tfull + tb);
-                ++tuse[tb];
-              }
-            }
-          }
-        }
-      }
-    } else if (warp == 1) {
-      // ---------------- A: one bulk copy of n_cand 128-byte rows per (part, direction) and step
-      const int parts = P.split ? 2 : 1;
-      const uint32_t bytes = (uint32_t)n_cand * 128;
-      uint32_t g = 0;
-      int zeroed[S];  // rows [zeroed[s], 128) of stage s read as zero
-#pragma unroll
-      for (int s = 0; s < S; ++s) zeroed[s] = 0;
+  if (warp == 0) {
+    // ---------------- MMA issue (one lane)
+    if (lane == 0) {
+      uint32_t g = 0, tuse[2] = {0, 0};
+      const uint32_t idesc = make_idesc(kTcM, kN, BF ? 1 : 0);
       bool ok = true;
       for (int wi = blockIdx.x; wi < P.n_work && ok; wi += gridDim.x) {
-        const TcItem it = tc_item(P, wi, n, H, tc_psi_group(C));
-        const int used = it.nd * nc8;
-        int slot = 0;
-        if (lane < parts * it.nd) slot = P.local_idx[it.e0 + it.a0 + lane % it.nd];
         for (int col = 0; col < H && ok; ++col) {
+          const int tb = col & 1;
           for (int qq = 0; qq < NQ && ok; ++qq, ++g) {
             const uint32_t st = g % S;
-            unsigned char* stA = stages + st * stage_bytes;
-            if (g >= (uint32_t)S) {
-              bool w = true;
-              if (lane == 0) w = wait(bar_empty + st, (g / S - 1) & 1u);
-              ok = __shfl_sync(0xffffffffu, w ? 1 : 0, 0) != 0;
-              if (!ok) break;
-            }
-#pragma unroll
-            for (int s = 0; s < S; ++s) {
-              if (s == (int)st && used < zeroed[s]) {
-                // rows this tile leaves empty must read as zero
-                for (int t = lane; t < 2 * (zeroed[s] - used) * 8; t += 32) {
-                  const int row = used + (t >> 3) % (zeroed[s] - used), part = (t >> 3) / (zeroed[s] - used);
-                  *reinterpret_cast<uint4*>(stA + part * a_part + row * 128 + (t & 7) * 16) =
-                      make_uint4(0, 0, 0, 0);
-                }
-                asm volatile("fence.proxy.async.shared::cta;");
-                __syncwarp();
-              }
-              if (s == (int)st) zeroed[s] = used;
-            }
-            if (lane == 0) mbar_expect_tx(bar_afull + st, (uint32_t)(parts * it.nd) * bytes);
-            __syncwarp();
-            if (lane < parts * it.nd) {
-              const int part = lane / it.nd, dl = lane - part * it.nd;
-              const __half* src =
-                  P.tbank + ((((size_t)slot * H + col) * NQ + qq) * 2 + part) * (size_t)n_cand * 64;
-              bulk_copy(stA + part * a_part + (uint32_t)dl * nc8 * 128, src, bytes, bar_afull + st);
+            if (qq == 0 && tuse[tb] > 0) ok = wait(bar_tempty + tb, (tuse[tb] - 1) & 1u);
+            ok = ok && wait(bar_bfull + st, (g / S) & 1u) && wait(bar_afull + st, (g / S) & 1u);
+            if (!ok) break;
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const uint32_t a0s = smem_u32(stages + st * stage_bytes);
+            issue_mma_step(taddr + (uint32_t)(tb * kN), a0s, a0s + 2 * a_part, a_part, b_part, idesc,
+                           P.split ? 3 : 1, qq > 0);
+            mma_commit(bar_empty + st);
+            *s_mma_steps = g + 1;
+            if (qq == NQ - 1) {
+              mma_commit(bar_tfull + tb);
+              ++tuse[tb];
             }
           }
         }
       }
-    } else {
-      // ---------------- B: U_{s,y}(r) = P_s(r, col) w^{r y}, scaled and split, per K step
-      // Both builder warps always run the same sequence of named barriers (no
-      // early exit): after a failure they only skip the work.
-      const int bt = tid - 64;  // 0..63
-      uint32_t g = 0;
-      bool ok = true;
-      for (int wi = blockIdx.x; wi < P.n_work; wi += gridDim.x) {
-        const TcItem it = tc_item(P, wi, n, H, tc_psi_group(C));
-        const int g_psi = it.g_psi;
-        // columns 0 and 1 of this particle; later columns arrive by cp.async two
-        // columns ahead (one group per column and thread)
-        asm volatile("bar.sync 1, 64;" ::: "memory");  // both builders left the previous item
-        for (int t = bt; t < g_psi * n; t += kTcBuilders) {
-          const int s = t / n, r = t - s * n;
-          const float2* pcol = it.pb + ((size_t)s * n + r) * H;
-          s_p[t] = __ldg(pcol);
-          s_p[kTcPsi * n + t] = __ldg(pcol + 1);
-        }
-        for (int col = 0; col < H; ++col) {
-          asm volatile("cp.async.wait_group 1;" ::: "memory");
-          asm volatile("bar.sync 1, 64;" ::: "memory");  // column col visible; column col-1 finished by both
-          if (col + 2 < H) {
-            for (int t = bt; t < g_psi * n; t += kTcBuilders) {
-              const int s = t / n, r = t - s * n;
-              cp_async8(s_p + ((col + 2) % 3) * kTcPsi * n + t, it.pb + ((size_t)s * n + r) * H + col + 2);
-            }
+    }
+  } else if (warp == 1) {
+    // ---------------- A: one bulk copy of n_cand 128-byte rows per (part, direction) and step
+    const int parts = P.split ? 2 : 1;
+    const uint32_t bytes = (uint32_t)n_cand * 128;
+    uint32_t g = 0;
+    int zeroed[S];  // rows [zeroed[s], 128) of stage s read as zero
+#pragma unroll
+    for (int s = 0; s < S; ++s) zeroed[s] = 0;
+    bool ok = true;
+    for (int wi = blockIdx.x; wi < P.n_work && ok; wi += gridDim.x) {
+      const TcItem it = tc_item(P, wi, n, H, tc_psi_group(C));
+      const int used = it.nd * nc8;
+      int slot = 0;
+      if (lane < parts * it.nd) slot = P.local_idx[it.e0 + it.a0 + lane % it.nd];
+      for (int col = 0; col < H && ok; ++col) {
+        for (int qq = 0; qq < NQ && ok; ++qq, ++g) {
+          const uint32_t st = g % S;
+          unsigned char* stA = stages + st * stage_bytes;
+          if (g >= (uint32_t)S) {
+            bool w = true;
+            if (lane == 0) w = wait(bar_empty + st, (g / S - 1) & 1u);
+            ok = __shfl_sync(0xffffffffu, w ? 1 : 0, 0) != 0;
+            if (!ok) break;
           }
-          asm volatile("cp.async.commit_group;");
-          const float2* sp = s_p + (col % 3) * kTcPsi * n;
-          for (int qq = 0; qq < NQ; ++qq, ++g) {
-            const uint32_t st = g % S;
-            unsigned char* stB = stages + st * stage_bytes + 2 * a_part;
-            if (g >= (uint32_t)S) ok = wait(bar_empty + st, (g / S - 1) & 1u) && ok;
-            // one task per (crop row, 8-row block): its eight twiddles serve every psi angle
-            const int b_tasks = ok ? C * 4 : 0;
-            for (int t = bt; t < b_tasks; t += kTcBuilders) {
-              const int yi = t % C, rc = t / C;
-              const int y = yi - h;
-              const int r0 = qq * 32 + rc * 8;
-              float2 twv[8];
-              {
-                // twiddle indices modulo n (y < 0 for the upper half of the crop rows)
-                float2 tw = cscale(s_twr[((r0 * y) % n + n) % n], kTcScale);  // the operand scale
-                const float2 step = s_twr[(y % n + n) % n];
 #pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                  twv[i] = tw;
-                  tw = cmul(tw, step);
-                }
+          for (int s = 0; s < S; ++s) {
+            if (s == (int)st && used < zeroed[s]) {
+              // rows this tile leaves empty must read as zero
+              for (int t = lane; t < 2 * (zeroed[s] - used) * 8; t += 32) {
+                const int row = used + (t >> 3) % (zeroed[s] - used), part = (t >> 3) / (zeroed[s] - used);
+                *reinterpret_cast<uint4*>(stA + part * a_part + row * 128 + (t & 7) * 16) =
+                    make_uint4(0, 0, 0, 0);
               }
-              for (int s = 0; s < g_psi; ++s) {
-                const float2* pp = sp + s * n + r0;
-                // rows of psi s: per crop-row pair (Re y, Re y+1, Im y, Im y+1)
-                const int jr = s * kPS + 4 * (yi >> 1) + (yi & 1), ji = jr + 2;
-                // the eight products of the step, once for both parts
-                float ur[8], ui[8];
-#pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                  const float2 u = cmul(pp[i], twv[i]);
-                  ur[i] = u.x;
-                  ui[i] = u.y;
-                }
-#pragma unroll
-                for (int part = 0; part < 2; ++part) {
-                  // part 0: Re U -> Re-Z row first half, Im-Z row second half;
-                  // part 1: Im U -> Im-Z row first half, -Im U in the Re-Z row second half
-                  uint32_t hw[4], lw[4];
-#pragma unroll
-                  for (int i = 0; i < 4; ++i) {
-                    const float a = part ? ui[2 * i] : ur[2 * i], b = part ? ui[2 * i + 1] : ur[2 * i + 1];
-                    const __half2 hv = __floats2half2_rn(a, b);
-                    const float2 hf = __half22float2(hv);
-                    const __half2 lv = __floats2half2_rn(a - hf.x, b - hf.y);
-                    hw[i] = *reinterpret_cast<const uint32_t*>(&hv);
-                    lw[i] = *reinterpret_cast<const uint32_t*>(&lv);
-                  }
-                  const uint4 hi = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-                  const uint4 lo = make_uint4(lw[0], lw[1], lw[2], lw[3]);
-                  const int j1 = part ? ji : jr, j2 = part ? jr : ji;
-                  *reinterpret_cast<uint4*>(stB + sw128(j1, rc)) = hi;
-                  *reinterpret_cast<uint4*>(stB + sw128(j2, 4 + rc)) = part ? neg8(hi) : hi;
-                  if (P.split) {
-                    *reinterpret_cast<uint4*>(stB + b_part + sw128(j1, rc)) = lo;
-                    *reinterpret_cast<uint4*>(stB + b_part + sw128(j2, 4 + rc)) = part ? neg8(lo) : lo;
-                  }
-                }
-              }
+              asm volatile("fence.proxy.async.shared::cta;");
+              __syncwarp();
             }
-            asm volatile("fence.proxy.async.shared::cta;");
-            __syncwarp();
-            if (lane == 0) mbar_arrive(bar_bfull + st);
+            if (s == (int)st) zeroed[s] = used;
           }
+          if (lane == 0) mbar_expect_tx(bar_afull + st, (uint32_t)(parts * it.nd) * bytes);
+          __syncwarp();
+          if (lane < parts * it.nd) {
+            const int part = lane / it.nd, dl = lane - part * it.nd;
+            const unsigned char* src = static_cast<const unsigned char*>(P.tbank) +
+                                       ((((size_t)slot * H + col) * NQ + qq) * 2 + part) * (size_t)n_cand * 128;
+            bulk_copy(stA + part * a_part + (uint32_t)dl * nc8 * 128, src, bytes, bar_afull + st);
+          }
+          if (lane == 0) *s_copy_steps = g + 1;
         }
-        asm volatile("cp.async.wait_all;" ::: "memory");
       }
+    }
+  } else if (warp < kTcEpiWarp0) {
+    // ---------------- B: U_{s,y}(r) = P_s(r, col) w^{r y}, scaled and split, per K step.
+    // The builder warps always run the same sequence of named barriers (no
+    // early exit): after a failure they only skip the work.
+    const int bt = tid - 32 * kTcBuildWarp0;
+    uint32_t g = 0;
+    bool ok = true;
+    for (int wi = blockIdx.x; wi < P.n_work; wi += gridDim.x) {
+      const TcItem it = tc_item(P, wi, n, H, tc_psi_group(C));
+      const int g_psi = it.g_psi;
+      // columns 0 and 1 of this particle; later columns arrive by cp.async two
+      // columns ahead (one group per column and thread)
+      asm volatile("bar.sync 1, %0;" ::"n"(kTcBuilders) : "memory");  // every builder left the previous item
+      for (int t = bt; t < g_psi * n; t += kTcBuilders) {
+        const int s = t / n, r = t - s * n;
+        const float2* pcol = it.pb + ((size_t)s * n + r) * H;
+        s_p[t] = __ldg(pcol);
+        s_p[kTcPsi * n + t] = __ldg(pcol + 1);
+      }
+      for (int col = 0; col < H; ++col) {
+        asm volatile("cp.async.wait_group 1;" ::: "memory");
+        asm volatile("bar.sync 1, %0;" ::"n"(kTcBuilders) : "memory");  // column col visible; col-1 done
+        if (col + 2 < H) {
+          for (int t = bt; t < g_psi * n; t += kTcBuilders) {
+            const int s = t / n, r = t - s * n;
+            cp_async8(s_p + ((col + 2) % 3) * kTcPsi * n + t, it.pb + ((size_t)s * n + r) * H + col + 2);
+          }
+        }
+        asm volatile("cp.async.commit_group;");
+        const float2* sp = s_p + (col % 3) * kTcPsi * n;
+        const float scale = s_psc[col];
+        for (int qq = 0; qq < NQ; ++qq, ++g) {
+          const uint32_t st = g % S;
+          unsigned char* stB = stages + st * stage_bytes + 2 * a_part;
+          if (g >= (uint32_t)S) ok = wait(bar_empty + st, (g / S - 1) & 1u) && ok;
+          if (ok) build_b_step<C, N, BF>(stB, b_part, sp, s_twr, scale, qq, g_psi, P.split != 0, bt);
+          asm volatile("fence.proxy.async.shared::cta;");
+          __syncwarp();
+          if (lane == 0) mbar_arrive(bar_bfull + st);
+        }
+      }
+      asm volatile("cp.async.wait_all;" ::: "memory");
     }
   } else {
     // ---------------- stage 2 and the first maximum per (row, psi)
     constexpr int RR = tc_reg_rows<C>();  // crop rows in registers; rows [RR, C) in TMEM
-    const int q4 = warp & 3, my_psi = (warp - 4) >> 2;
+    const int q4 = warp & 3, my_psi = (warp - kTcEpiWarp0) >> 2;
     const int my_row = 32 * q4 + lane;
     const uint32_t lane_off = (uint32_t)(32 * q4) << 16;
     const uint32_t ta_z = taddr + lane_off + (uint32_t)(my_psi * kPS);
     const uint32_t ta_acc = taddr + lane_off + (uint32_t)(2 * kN + my_psi * (C - RR) * C);
-    const uint32_t tw0 = smem_u32(s_twall);
     uint32_t tuse[2] = {0, 0};
     bool ok = true;
     for (int wi = blockIdx.x; wi < P.n_work && ok; wi += gridDim.x) {
-      const bool active = my_psi < tc_item(P, wi, n, H, tc_psi_group(C)).g_psi;  // warp-uniform; the rest is re-read at the end
+      const bool active = my_psi < tc_item(P, wi, n, H, tc_psi_group(C)).g_psi;  // warp-uniform
       float acc[RR][C];  // [crop row][slot]
 #pragma unroll
       for (int y = 0; y < RR; ++y)
@@ -611,7 +630,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
         if (!ok) break;
         asm volatile("tcgen05.fence::after_thread_sync;");
         if (active) {
-          const uint32_t tw = tw0 + (uint32_t)(col * tc_tw_entries(C) * 4);
+          const uint32_t e = smem_u32(s_twall + col * TWE);
           const uint32_t tz = ta_z + (uint32_t)(tb * kN);
 #pragma unroll
           for (int yp = 0; yp < C / 2; ++yp) {
@@ -625,11 +644,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
               const int y = 2 * yp + hy;
               const float zr = __uint_as_float(v[hy]), zi = __uint_as_float(v[2 + hy]);
               if (y < RR) {
-                stage2_row<C>(acc[y < RR ? y : 0], zr, zi, tw);
+                stage2_row<C>(acc[y < RR ? y : 0], zr, zi, e);
               } else {
                 float a[C];
                 tmem_ld_row<C>(a, ta_acc + (uint32_t)((y - RR) * C));
-                stage2_row<C>(a, zr, zi, tw);
+                stage2_row<C>(a, zr, zi, e);
                 tmem_st_row<C>(a, ta_acc + (uint32_t)((y - RR) * C));
               }
             }
@@ -678,13 +697,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
       }
     }
   }
-  // every role has left its loop; on a failure, MMAs still in flight get a
-  // last bounded chance to retire before TMEM is freed
+  // Every role has left its loop. After a failure, the bulk copies and the
+  // MMAs this CTA issued get a last bounded chance (the default bound) to
+  // finish before the CTA frees its TMEM and exits: the latest use of each
+  // stage is among the last S steps issued.
   __syncthreads();
   if (*reinterpret_cast<volatile int*>(s_fail) != 0) {
     if (tid == 0) {
       if (P.status != nullptr) atomicExch(P.status, 1);
-      for (int s = 0; s < S; ++s) mbar_wait(bar_empty + s, 0), mbar_wait(bar_empty + s, 1);
+      const uint32_t gm = *s_mma_steps, ga = *s_copy_steps;
+      for (uint32_t g = gm > (uint32_t)S ? gm - S : 0; g < gm; ++g)
+        mbar_wait(bar_empty + g % S, (g / S) & 1u, kWaitLimit);
+      for (uint32_t g = ga > (uint32_t)S ? ga - S : 0; g < ga; ++g)
+        mbar_wait(bar_afull + g % S, (g / S) & 1u, kWaitLimit);
     }
     __syncthreads();
   }
@@ -694,17 +719,21 @@ __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
   }
 }
 
-// fp16 hi/lo copy of template banks for the tensor-core kernel:
-// out[slot][col][step][part][cand][128 B]; step q covers rows r in
-// [32q, 32q + 32): logical 16-byte chunk c < 4 holds Re T of rows 32q + 8c..,
-// chunk 4 + c holds Im T of the same rows, scaled by 2^13; chunk c is stored
-// at position c ^ (cand & 7) (the 128-byte swizzle of the shared-memory tile,
-// whose direction blocks start on multiples of 8 rows). One block per
-// (slot, candidate); every candidate writes whole 128-byte rows.
+// Operand copy of template banks for the tensor-core kernel:
+// out[slot][col][step][part][cand][128 B]; part 0 hi, part 1 lo (split
+// forms only read part 1). Step q covers rows r in [32q, 32q + 32): logical
+// 16-byte chunk c < 4 holds Re T of rows 32q + 8c.., chunk 4 + c holds Im T
+// of the same rows, scaled by 2^13 times the column's scale; chunk c is
+// stored at position c ^ (cand & 7) (the 128-byte swizzle of the
+// shared-memory tile, whose direction blocks start on multiples of 8 rows).
+// One block per (slot, candidate); every candidate writes whole 128-byte
+// rows. A value that leaves the operand type's range sets *status to 2.
 __host__ __device__ inline int bank_fp16_ld(int n) { return n + n / 8 + 1; }
 
-__global__ void bank_to_fp16(const float2* __restrict__ bank, long long bank_stride, int n, int n_cand, int cb,
-                             __half* __restrict__ out) {
+template <bool BF>
+__global__ void bank_to_operands(const float2* __restrict__ bank, long long bank_stride, int n, int n_cand,
+                                 int cb, const float* __restrict__ t_scale, unsigned char* __restrict__ out,
+                                 int* status) {
   // [cb][ld]: columns [c0, c0 + cb) of the template, column-major with a
   // spare slot after every 8 rows, so the 16 row blocks a warp reads at once
   // fall on distinct banks
@@ -712,6 +741,7 @@ __global__ void bank_to_fp16(const float2* __restrict__ bank, long long bank_str
   const int H = n / 2 + 1, nq = n / 32, ld = bank_fp16_ld(n);
   const int slot = blockIdx.x, cand = blockIdx.y;
   const float2* src = bank + (size_t)cand * (size_t)bank_stride + (size_t)slot * n * H;
+  bool bad = false;
   for (int c0 = 0; c0 < H; c0 += cb) {
     const int w = min(cb, H - c0);
     __syncthreads();
@@ -726,33 +756,41 @@ __global__ void bank_to_fp16(const float2* __restrict__ bank, long long bank_str
       const bool imag = c >= 4;
       const int r0 = qq * 32 + (c & 3) * 8;
       const float2* sc = s_t + cl * ld + r0 + (r0 >> 3);
-      float v[8];
+      const float scale = kTcScale * (t_scale ? t_scale[col] : 1.0f);
+      uint32_t h[4], l[4];
 #pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        const float2 z = sc[i];
-        v[i] = (imag ? z.y : z.x) * kTcScale;
+      for (int i = 0; i < 4; ++i) {
+        const float2 z0 = sc[2 * i], z1 = sc[2 * i + 1];
+        const float a = (imag ? z0.y : z0.x) * scale, b = (imag ? z1.y : z1.x) * scale;
+        bad |= !(fabsf(a) <= (BF ? 3.0e38f : 65504.0f)) || !(fabsf(b) <= (BF ? 3.0e38f : 65504.0f));
+        split2<BF>(a, b, h[i], l[i]);
       }
-      uint4 hi, lo;
-      split8(v, hi, lo);
       const size_t row = (((size_t)slot * H + col) * nq + qq) * 2;  // part 0 row block
       const int pos = c ^ (cand & 7);
-      *reinterpret_cast<uint4*>(out + ((row * n_cand + cand) * 8 + pos) * 8) = hi;
-      *reinterpret_cast<uint4*>(out + (((row + 1) * n_cand + cand) * 8 + pos) * 8) = lo;
+      *reinterpret_cast<uint4*>(out + ((row * n_cand + cand) * 8 + pos) * 16) = make_uint4(h[0], h[1], h[2], h[3]);
+      *reinterpret_cast<uint4*>(out + (((row + 1) * n_cand + cand) * 8 + pos) * 16) =
+          make_uint4(l[0], l[1], l[2], l[3]);
     }
   }
+  if (bad && status != nullptr) atomicExch(status, 2);
+}
+
+template <int C, int N, bool BF>
+cudaError_t launch_tc_cnb(const TcParams& P, size_t smem, int grid, cudaStream_t st) {
+  static size_t set_smem = 0;
+  if (set_smem < smem) {
+    cudaError_t e =
+        cudaFuncSetAttribute(correlate_tc<C, N, BF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    set_smem = smem;
+  }
+  correlate_tc<C, N, BF><<<grid, kTcThreads, smem, st>>>(P);
+  return cudaGetLastError();
 }
 
 template <int C, int N>
 cudaError_t launch_tc_cn(const TcParams& P, size_t smem, int grid, cudaStream_t st) {
-  static size_t set_smem = 0;
-  if (set_smem < smem) {
-    cudaError_t e =
-        cudaFuncSetAttribute(correlate_tc<C, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    set_smem = smem;
-  }
-  correlate_tc<C, N><<<grid, kTcThreads, smem, st>>>(P);
-  return cudaGetLastError();
+  return P.bf16 ? launch_tc_cnb<C, N, true>(P, smem, grid, st) : launch_tc_cnb<C, N, false>(P, smem, grid, st);
 }
 
 template <int C>
@@ -775,14 +813,17 @@ cudaError_t launch_tc_c(const TcParams& P, size_t smem, int grid, cudaStream_t s
 int correlate_tc_max_psi() { return kTcPsi; }
 int correlate_tc_max_n() { return kTcMaxN; }
 int correlate_tc_max_cand() { return kTcMaxCand; }
+unsigned correlate_tc_default_wait() { return kWaitLimit; }
 
 size_t correlate_tc_smem_bytes(int n, int crop) {
   const size_t stage = 2 * (size_t)kTcM * 128 + 2 * (size_t)tc_n(crop) * 128;
+  const int H = n / 2 + 1;
   return tc_stages(n) * stage + 3 * (size_t)kTcPsi * n * sizeof(float2) + (size_t)n * sizeof(float2) +
-         (size_t)(n / 2 + 1) * tc_tw_entries(crop) * sizeof(float) + (3 * tc_stages(n) + 4) * 8 + 8;
+         (size_t)H * tc_tw_entries(crop) * sizeof(float) + (size_t)((H + 1) & ~1) * sizeof(float) +
+         (3 * tc_stages(n) + 4) * 8 + 16;
 }
 
-// halves in the fp16 hi/lo bank copy of one candidate
+// bytes of the operand copy of one candidate's bank: hi and lo halves
 long long correlate_tc_bank_halves(int n_slot, int n) {
   return (long long)n_slot * (n / 2 + 1) * 2 * (2LL * n);
 }
@@ -822,29 +863,40 @@ int correlate_tc_plan(const int* local_ptr, const int* local_idx, int n_particle
   return count;
 }
 
-cudaError_t launch_bank_to_fp16(cudaStream_t st, const float2* bank, long long bank_stride, int n_cand, int n_slot,
-                                int n, void* out) {
+cudaError_t launch_bank_to_operands(cudaStream_t st, const float2* bank, long long bank_stride, int n_cand,
+                                    int n_slot, int n, int bf16, const float* t_scale, void* out, int* status) {
   if (n_cand <= 0 || n_slot <= 0) return cudaSuccess;
   const int cb = std::min(n / 2 + 1, 128 * 1024 / (int)(bank_fp16_ld(n) * sizeof(float2)));  // columns per block
   const size_t smem = (size_t)bank_fp16_ld(n) * cb * sizeof(float2);
-  static size_t set_smem = 0;
-  if (set_smem < smem) {
-    cudaError_t e = cudaFuncSetAttribute(bank_to_fp16, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  static size_t set_smem[2] = {0, 0};
+  const int k = bf16 ? 1 : 0;
+  if (set_smem[k] < smem) {
+    cudaError_t e = bf16 ? cudaFuncSetAttribute(bank_to_operands<true>,
+                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                         : cudaFuncSetAttribute(bank_to_operands<false>,
+                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    set_smem = smem;
+    set_smem[k] = smem;
   }
-  bank_to_fp16<<<dim3(n_slot, n_cand), 256, smem, st>>>(bank, bank_stride, n, n_cand, cb, (__half*)out);
+  if (bf16)
+    bank_to_operands<true><<<dim3(n_slot, n_cand), 256, smem, st>>>(bank, bank_stride, n, n_cand, cb, t_scale,
+                                                                     (unsigned char*)out, status);
+  else
+    bank_to_operands<false><<<dim3(n_slot, n_cand), 256, smem, st>>>(bank, bank_stride, n, n_cand, cb, t_scale,
+                                                                      (unsigned char*)out, status);
   return cudaGetLastError();
 }
 
 cudaError_t launch_correlate_tc(cudaStream_t st, const void* tbank, int n_cand, const float2* stack,
                                 const int* local_ptr, const int* local_idx, const int* work, int n_work, int n_psi,
-                                int n, int crop, int nnz, int split, const float2* tw_row, const float2* tw_col,
-                                float* out_score, int* out_y, int* out_x, int* status, int grid) {
+                                int n, int crop, int nnz, int split, int bf16, const float* t_scale,
+                                const float* p_scale, unsigned wait_limit, const float2* tw_row,
+                                const float2* tw_col, float* out_score, int* out_y, int* out_x, int* status,
+                                int grid) {
   if (n_work <= 0 || n_cand <= 0) return cudaSuccess;
   if (n_cand > kTcMaxCand) return cudaErrorInvalidValue;
   TcParams P;
-  P.tbank = (const __half*)tbank;
+  P.tbank = tbank;
   P.stack = stack;
   P.local_ptr = local_ptr;
   P.local_idx = local_idx;
@@ -855,9 +907,13 @@ cudaError_t launch_correlate_tc(cudaStream_t st, const void* tbank, int n_cand, 
   P.n = n;
   P.nnz = nnz;
   P.split = split ? 1 : 0;
+  P.bf16 = bf16 ? 1 : 0;
   P.dpt = correlate_tc_dirs_per_tile(n_cand);
   P.tw_row = tw_row;
   P.tw_col = tw_col;
+  P.t_scale = t_scale;
+  P.p_scale = p_scale;
+  P.wait_limit = wait_limit ? wait_limit : kWaitLimit;
   P.out_score = out_score;
   P.out_y = out_y;
   P.out_x = out_x;

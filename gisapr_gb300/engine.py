@@ -370,7 +370,9 @@ class BatchScoringJob:
     (ZL gisapr_batch_search.py:251-364).
     """
 
-    PRECISIONS = ("fp32", "fp16x3", "fp16")
+    PRECISIONS = ("fp32", "fp16x3", "fp16", "bf16x3", "bf16")
+    # precision code of gisapr_correlate_tc_batch_ex (GISAPR_TC_*)
+    TC_CODES = {"fp16": 0, "fp16x3": 1, "bf16": 2, "bf16x3": 3}
 
     def __init__(self, job: ScoringJob, n_cand: int, models: Optional[Sequence] = None,
                  model_of: Optional[Sequence[int]] = None, use_graph: bool = True, precision: str = "fp32",
@@ -441,6 +443,37 @@ class BatchScoringJob:
         for _, cc in self.tc_chunks:
             self._tc_plan(cc)
         self.tc_status = torch.zeros(1, dtype=torch.int32, device=job.device)
+        self.t_scale, self.p_scale = self.column_scales(job)
+        self.tc_wait_limit = 0  # default bound of the kernel's on-chip waits
+
+    @staticmethod
+    def column_scales(job: ScoringJob):
+        """Per stored bank column, the powers of two that multiply the
+        template and the particle operands of the tensor-core correlation
+        (undone after accumulation), so that weak high-frequency columns
+        keep the 16-bit types' normal range. Particle side: from the job's
+        largest coefficient of the column (scaled into [0.25, 0.5]).
+        Template side: from the column's largest FSC weight (a template
+        coefficient is at most its FSC weight times its whitened amplitude
+        over the template norm), up to 2^8, only for weights below 1/4.
+        Both are job constants; a template value that still leaves fp16's
+        range is reported by the kernel's status word."""
+        nb = job.cfg.new_box
+        h = nb // 2 + 1
+        with torch.no_grad():
+            pmax = job.stack.abs().amax(dim=(0, 1, 2)).float().cpu().numpy()   # [H] stored columns
+        fsc = job.packed_fsc.cpu().numpy().reshape(nb, h)                         # packed (unshifted) columns
+        stored_of = (np.arange(h) + h // 2) % h                                    # packed column -> stored
+        fmax = np.zeros(h, np.float64)
+        fmax[stored_of] = np.abs(fsc).max(axis=0)
+        with np.errstate(divide="ignore"):
+            pe = np.where(pmax > 0, np.floor(np.log2(0.5 / np.maximum(pmax, 1e-30))), 0.0)
+            te = np.where(fmax > 0, np.floor(np.log2(0.25 / np.maximum(fmax, 1e-30))), 8.0)
+        pe = np.clip(pe, -8, 12)
+        te = np.clip(te, 0, 8)
+        dev = job.device
+        return (torch.from_numpy(np.exp2(te).astype(np.float32)).to(dev),
+                torch.from_numpy(np.exp2(pe).astype(np.float32)).to(dev))
 
     def _tc_plan(self, cc: int):
         """Work list of the tensor-core kernel for chunks of cc candidates (cached)."""
@@ -465,9 +498,18 @@ class BatchScoringJob:
         return [(c0, min(size, n_active - c0)) for c0 in range(0, n_active, size)]
 
     def check_status(self) -> None:
-        """Raise if an on-chip barrier wait of the tensor-core kernel ran out."""
-        if self.precision != "fp32" and int(self.tc_status.item()) != 0:
+        """Raise if an on-chip barrier wait of the tensor-core kernel ran out
+        (status 1) or a scaled template value left the operand type's range
+        (status 2)."""
+        if self.precision == "fp32":
+            return
+        st = int(self.tc_status.item())
+        if st == 1:
             raise RuntimeError("tensor-core correlation: an on-chip barrier wait ran out; results are incomplete")
+        if st == 2:
+            raise RuntimeError("tensor-core correlation: a scaled template value left the operand range")
+        if st != 0:
+            raise RuntimeError(f"tensor-core correlation: status {st}")
 
     KERNELS_PER_BATCH = 3      # correlation, records, score sums
 
@@ -515,12 +557,14 @@ class BatchScoringJob:
             m = max(1, job.nnz) * job.n_psi
             for c0, cc in self._chunks(n_act):
                 work, n_work = self._tc_plan(cc)
-                nat.call("gisapr_correlate_tc_batch", ctx, st, nat.c_ptr_offset(self.banks, c0 * self.bank_stride * 8),
-                         self.bank_stride, cc, self.n_slot, nat.ptr(self.tbank), nat.ptr(job.stack),
-                         nat.ptr(job.local_ptr), nat.ptr(job.local_idx), nat.ptr(work), n_work, job.nnz, job.n_psi,
-                         job.cfg.new_box, job.cfg.crop, 1 if self.precision == "fp16x3" else 0,
-                         nat.c_ptr_offset(self.score_buf, c0 * m * 4), nat.c_ptr_offset(self.y_buf, c0 * m * 4),
-                         nat.c_ptr_offset(self.x_buf, c0 * m * 4), nat.ptr(self.tc_status))
+                nat.call("gisapr_correlate_tc_batch_ex", ctx, st,
+                         nat.c_ptr_offset(self.banks, c0 * self.bank_stride * 8), self.bank_stride, cc, self.n_slot,
+                         nat.ptr(self.tbank), nat.ptr(job.stack), nat.ptr(job.local_ptr), nat.ptr(job.local_idx),
+                         nat.ptr(work), n_work, job.nnz, job.n_psi, job.cfg.new_box, job.cfg.crop,
+                         self.TC_CODES[self.precision], nat.ptr(self.t_scale), nat.ptr(self.p_scale),
+                         int(self.tc_wait_limit), nat.c_ptr_offset(self.score_buf, c0 * m * 4),
+                         nat.c_ptr_offset(self.y_buf, c0 * m * 4), nat.c_ptr_offset(self.x_buf, c0 * m * 4),
+                         nat.ptr(self.tc_status))
         mark("correlate")
         nat.call("gisapr_particle_results_batch", st, nat.ptr(job.local_ptr), nat.ptr(self.score_buf),
                  nat.ptr(self.y_buf), nat.ptr(self.x_buf), np_, job.n_psi, n_act, nat.ptr(self.best_entry),

@@ -140,8 +140,8 @@ class ScoringServer:
                  precision: str = "fp32"):
         import torch
         self.device = torch.device(device)
-        if precision not in ("fp32", "fp16x3", "fp16"):
-            raise ValueError(f"precision must be fp32, fp16x3 or fp16, got {precision!r}")
+        if precision not in ("fp32", "fp16x3", "fp16", "bf16x3", "bf16"):
+            raise ValueError(f"precision must be fp32, fp16x3, fp16, bf16x3 or bf16, got {precision!r}")
         self.cap = int(hbm_cap_bytes)
         self.max_batch = int(max_batch)
         self.precision = precision

@@ -197,26 +197,40 @@ int gisapr_get_tuning(gisapr_ctx ctx, int key, int size, int* value);
 /*
  * Tensor-core form of gisapr_correlate_batch (tcgen05 MMA, FP32 accumulate),
  * same inputs and output layout. The stage that contracts template and
- * particle columns over rows runs as a real GEMM on fp16 operands scaled by
- * 2^13; split != 0 adds the hi*lo and lo*hi products of an fp16 hi/lo split
- * (about 22 significant bits), split == 0 keeps hi*hi only. Replaces the
- * same reference interfaces as gisapr_correlate_batch (v606:1418-1449 per
+ * particle columns over rows runs as a real GEMM on 16-bit operands, scaled
+ * by 2^13 times a power of two per packed column. Replaces the same
+ * reference interfaces as gisapr_correlate_batch (v606:1418-1449 per
  * candidate; ZL/gisapr_batch_search.py:314-349 for the candidate loop); the
- * precision modes have no reference counterpart.
+ * precision modes have no reference counterpart:
+ *   GISAPR_TC_FP16    fp16 operands, hi*hi only;
+ *   GISAPR_TC_FP16X3  fp16 hi/lo split, hi*hi + hi*lo + lo*hi (about 22
+ *                     significant bits per product);
+ *   GISAPR_TC_BF16    bf16 operands, hi*hi only;
+ *   GISAPR_TC_BF16X3  bf16 hi/lo split (about 16 significant bits).
  *   tbank: caller scratch of n_cand * gisapr_tc_bank_bytes(n_slot, n) bytes,
- *     rewritten on every call (fp16 hi/lo copy of the banks);
+ *     rewritten on every call (the operand copy of the banks);
  *   work, n_work: device copy of the list made by gisapr_tc_plan_work
  *     (host arrays in, host array out: [n_work][2] (particle, tile of 128
  *     rows * psi groups + group of psi angles: three, two at crop 14),
  *     sorted by direction; work == NULL only counts; n_psi and crop must
  *     match the correlation call);
- *   status: device int, set to 1 if an on-chip barrier wait ran out (the
- *     outputs are then incomplete); the caller zeroes it.
+ *   col_scale_t, col_scale_p: device float [n/2+1] per stored bank column,
+ *     powers of two multiplying the template and the particle operands
+ *     (undone after accumulation), or NULL for 1;
+ *   wait_limit: bound (iterations) of every on-chip hand-off wait, 0 for
+ *     the default; on a timeout the kernel stops, waits for its own copies
+ *     and MMAs in flight with the default bound and returns;
+ *   status: device int; 1 if an on-chip barrier wait ran out (the outputs
+ *     are then incomplete), 2 if a scaled template value left the operand
+ *     type's range; the caller zeroes it.
  * Sizes: n in {32, 64, 96, 128, 192, 256}, crop even in 2..14 (10..14 at n = 256),
  * n_cand <= 128 per call (the
  * work list is planned for that n_cand: a tile holds 128 / ceil8(n_cand)
- * whole directions).
+ * whole directions). gisapr_correlate_tc_batch is the _ex call with
+ * split != 0 -> GISAPR_TC_FP16X3, else GISAPR_TC_FP16, no column scales and
+ * the default wait bound.
  */
+enum { GISAPR_TC_FP16 = 0, GISAPR_TC_FP16X3 = 1, GISAPR_TC_BF16 = 2, GISAPR_TC_BF16X3 = 3 };
 long long gisapr_tc_bank_bytes(int n_slot, int n);
 int gisapr_tc_plan_work(const int* local_ptr, const int* local_idx, int n_particles, int n_cand, int n_psi,
                         int crop, int* work, int max_work, int* n_work);
@@ -224,6 +238,11 @@ int gisapr_correlate_tc_batch(gisapr_ctx ctx, void* stream, const float* bank, l
                               int n_slot, void* tbank, const float* stack, const int* local_ptr,
                               const int* local_idx, const int* work, int n_work, int nnz, int n_psi, int n, int crop,
                               int split, float* out_score, int* out_y, int* out_x, int* status);
+int gisapr_correlate_tc_batch_ex(gisapr_ctx ctx, void* stream, const float* bank, long long bank_stride,
+                                 int n_cand, int n_slot, void* tbank, const float* stack, const int* local_ptr,
+                                 const int* local_idx, const int* work, int n_work, int nnz, int n_psi, int n,
+                                 int crop, int precision, const float* col_scale_t, const float* col_scale_p,
+                                 unsigned wait_limit, float* out_score, int* out_y, int* out_x, int* status);
 
 /*
  * Per particle: first maximum over (local entry, psi), its crop position and

@@ -200,3 +200,55 @@ def test_split_box256_crop14_matches_plain():
     plain, tc, want, got, err = _compare_to_plain(job, poses, "fp16x3", SPLIT_MAP_REL)
     np.testing.assert_allclose(got, want, rtol=1e-6)
     assert int(tc.tc_status.item()) == 0
+
+
+@pytest.mark.parametrize("precision,map_rel", [("bf16x3", 1e-4), ("bf16", 1e-2)])
+def test_bf16_forms_match_plain_golden32(golden32, precision, map_rel):
+    """The bf16 operand forms (8 significant bits per part): the split form
+    within 1e-4 of the plain maps' scale, the single form within 1e-2."""
+    g = golden32
+    job = _golden32_job(g)
+    poses = [g["pose"]] + list(syn.candidate_poses(3, 9, 5.0, 3.0))
+    plain = BatchScoringJob(job, len(poses), use_graph=False)
+    tc = BatchScoringJob(job, len(poses), use_graph=False, precision=precision)
+    want = plain.score_batch(poses)
+    got = tc.score_batch(poses)
+    ps, ts = plain.score_buf.cpu().numpy(), tc.score_buf.cpu().numpy()
+    err = float(np.max(np.abs(ts - ps))) / float(np.max(np.abs(ps)))
+    print(f"{precision}: map error {err:.2e} of the map scale")
+    assert err <= map_rel, err
+    np.testing.assert_allclose(got, want, rtol=1e-5 if precision == "bf16x3" else 1e-3)
+    assert int(tc.tc_status.item()) == 0
+
+
+def test_column_scales_are_powers_of_two_within_range(golden32):
+    g = golden32
+    job = _golden32_job(g)
+    ts, ps = BatchScoringJob.column_scales(job)
+    for s in (ts.cpu().numpy(), ps.cpu().numpy()):
+        e = np.log2(s)
+        assert np.all(e == np.round(e))
+    assert np.all(ts.cpu().numpy() >= 1.0) and np.all(ts.cpu().numpy() <= 256.0)
+    # particle columns scaled to at most 1/2 (times the global 2^13)
+    pmax = job.stack.abs().amax(dim=(0, 1, 2)).cpu().numpy()
+    assert np.all(pmax * ps.cpu().numpy() <= 0.5 + 1e-6)
+
+
+def test_wait_limit_runs_out_and_reports_status(golden32):
+    """With the on-chip hand-off waits bounded at one attempt the kernel
+    gives up at once: it reports status 1, waits for its own copies in
+    flight, frees its TMEM and returns, so the context stays usable and the
+    next call with the default bound gives the normal scores."""
+    g = golden32
+    job = _golden32_job(g)
+    poses = list(syn.candidate_poses(3, 13, 5.0, 3.0))
+    ref = BatchScoringJob(job, len(poses), use_graph=False, precision="fp16x3").score_active(poses)
+    b = BatchScoringJob(job, len(poses), use_graph=False, precision="fp16x3")
+    b.tc_wait_limit = 1
+    with pytest.raises(RuntimeError, match="ran out"):
+        b.score_active(poses)
+    assert int(b.tc_status.item()) == 1
+    b.tc_status.zero_()
+    b.tc_wait_limit = 0
+    np.testing.assert_array_equal(b.score_active(poses), ref)
+    assert int(b.tc_status.item()) == 0

@@ -15,8 +15,11 @@ tables and particle spectra resident in HBM, the 1.0 GB particle stack is
 read every step, so inputs exceed L2), then the same K poses through the
 public API with the pose copied host->device and the score plus the
 per-particle peaks copied back each step (``e2e``). The reference arm
-(``--impl reference``) times the CPU oracle, the numpy restatement of the
-reference's CPU path, on a bounded sample of the same workload per step.
+(``--impl reference``) runs GisAPR's own CPU torch path, installed
+unmodified in baseline/_ref by oracle/install_reference.py, on the same job
+and poses (each step one pose with a particle sample, the candidate rate
+extrapolated over particles); without baseline/_ref it falls back to the
+numpy restatement of that path and says so.
 """
 from __future__ import annotations
 
@@ -249,39 +252,93 @@ def profiled_traffic(kernel: str, workload: str):
 # arms
 # ---------------------------------------------------------------------------
 
-def run_reference(args):
+REF_PARTICLE_SAMPLE = 200  # particles the reference arm runs per step, evenly spaced over the job
+
+
+def gb300_config(spec) -> dict:
+    """The workload both arms run (the reference's published shapes)."""
+    return {"workload": f"{spec.name}: box {spec.box} at {spec.apix} A/px, {spec.n_particles} particles, "
+                        f"{spec.n_moving_atoms} moving + {spec.n_fixed_atoms} fixed atoms, HEALPix order "
+                        f"{spec.healpix_order} within +-{spec.local_range} deg, psi step {spec.psi_step} deg, "
+                        f"crop {spec.crop}; one candidate pose per step",
+            "box": spec.box, "apix": spec.apix, "particles": spec.n_particles, "moving_atoms": spec.n_moving_atoms,
+            "fixed_atoms": spec.n_fixed_atoms, "healpix_order": spec.healpix_order,
+            "local_range_deg": spec.local_range, "psi_step_deg": spec.psi_step, "crop": spec.crop,
+            "candidates_per_step": 1}
+
+
+def reference_job(args):
+    """The GPU arm's own rank-0 job (same seeds, same model, same particles)
+    and its poses, generated on the GPU when there is one (data generation
+    is not timed)."""
+    import torch
     from gisapr_gb300 import synthetic as syn
-    n_sample = max(8, args.cpu_sample)
-    spec = syn.WORKLOADS[args.workload]
-    # the sample needs only the particles it times; the model, box and
-    # direction set are the full workload's
-    spec_s, job = make_workload(args.workload, args.seed, "cpu", particles=max(n_sample, 64))
+    from gisapr_gb300.replicas import replica_seed
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    spec, data, _ = make_workload(args.workload, replica_seed(args.seed, 0), dev, args.particles, with_models=True)
     poses = syn.candidate_poses(args.steps + args.warmup, args.seed + 100, spec.pose_rotation_deg,
                                 spec.pose_translation, exact=True)
-    per = []
+    return spec, data, poses
+
+
+def run_reference(args):
+    """GisAPR's own CPU path (oracle/reference_cpu.py, from baseline/_ref) on
+    the GPU arm's job and poses. Each step scores one candidate pose:
+    density of every atom, every template of the angle table, and the
+    reference's per-particle loop over an evenly spaced sample of the
+    job's particles. ms_per_step is that measured work; the candidate rate
+    extrapolates the per-particle time to every particle of the job (the
+    loop is linear in particles). Without baseline/_ref the numpy port of
+    the same path (the oracle) stands in and the line says so."""
+    import numpy as np
+    from oracle import reference_cpu
+    spec, data, poses = reference_job(args)
+    n_p = len(data.records.rot)
+    sample = np.unique(np.linspace(0, n_p - 1, min(REF_PARTICLE_SAMPLE, n_p)).astype(int)).tolist()
+    if reference_cpu.available():
+        runner = reference_cpu.RefRunner(data)
+        kind, dtype = "reference", "f32"
+        step = lambda pose: runner.step(pose, sample)  # noqa: E731
+        threads = runner.threads
+        what = ("GisAPR's own CPU torch path (optimized-3 tree: pdb2mrc v3 generate_volume, v606 "
+                "IntegratedProjector.build_templates over all directions, PackedCTFTorch, per-particle "
+                "prepare / correlate_templates_and_particle / make_result_records)")
+    else:
+        kind, dtype = "port", "f64"
+        threads = os.cpu_count() or 1
+
+        def step(pose):
+            info = cpu_baseline(spec, data, pose, len(sample))
+            return {"density_s": info["density_s"] + info["volume_fft_s"],
+                    "templates_s": info["template_s"] * info["n_templates"],
+                    "particles_s": info["particle_s"] * len(sample), "n_templates": info["n_templates"]}
+        what = "numpy restatement of the reference's CPU path (oracle), baseline/_ref not installed"
+    per, meas = [], []
     info = None
     for k in range(args.warmup + args.steps):
-        info = cpu_baseline(spec, job, poses[k], n_sample)
-        # scale the per-particle cost to the full particle count of the workload
-        secs = (info["density_s"] + info["volume_fft_s"] + info["template_s"] * info["n_templates"]
-                + info["particle_s"] * spec.n_particles)
+        t0 = time.perf_counter()
+        info = step(poses[k])
+        dt = time.perf_counter() - t0
+        full = info["density_s"] + info["templates_s"] + info["particles_s"] * n_p / len(sample)
         if k >= args.warmup:
-            per.append(secs)
+            per.append(full)
+            meas.append(dt)
     sec = statistics.mean(per)
     value = 1.0 / sec
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"{args.workload}: box {spec.box}, {spec.n_particles} particles, "
-                               f"{spec.n_moving_atoms}+{spec.n_fixed_atoms} atoms, HEALPix order "
-                               f"{spec.healpix_order}, +-{spec.local_range} deg, crop {spec.crop}",
-                   "candidates_per_step": 1},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": int(info["threads"]), "kind": "port",
-                         "sample": f"per step: full moving-chain splat and 3-D FFT, {int(info['sample_templates'])}"
-                                   f" templates timed (extrapolated to the {int(info['n_templates'])} needed) and "
-                                   f"{int(info['sample_particles'])} of {spec.n_particles} particles (prepare + "
-                                   f"correlate), extrapolated"},
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(meas) * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic",
+        "config": gb300_config(spec),
+        "seconds_per_candidate": {"value": sec, "density_s": info["density_s"],
+                                  "templates_s": info["templates_s"],
+                                  "particles_s_per_particle": info["particles_s"] / len(sample),
+                                  "templates": int(info["n_templates"]), "particles": n_p,
+                                  "note": f"each step runs {len(sample)} of the {n_p} particles; the candidate "
+                                          f"rate extrapolates the per-particle time to all {n_p}"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": int(threads), "kind": kind,
+                         "sample": f"{what}; per step one pose: density, {int(info['n_templates'])} templates "
+                                   f"and {len(sample)} of {n_p} particles, particle time scaled to all {n_p}"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -571,13 +628,11 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": elapsed / K * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"{args.workload}: plain FP32, one candidate per step",
-                   "box": spec.box, "apix": spec.apix, "particles": len(job.records),
-                   "moving_atoms": job.density.n_moving, "fixed_atoms": job.density.fixed_atom_count,
-                   "directions": len(data.model_rot), "needed_directions": len(job.needed),
-                   "maps_per_candidate": maps, "local_range_deg": spec.local_range, "psi_step_deg": spec.psi_step,
-                   "crop": spec.crop, "candidates_per_step": 1, "parallelism": f"replicas x{world}",
-                   "l2": l2_note(job.stack.numel() * job.stack.element_size())},
+        "config": dict(gb300_config(spec), form="plain FP32", parallelism=f"replicas x{world}",
+                       l2=l2_note(job.stack.numel() * job.stack.element_size())),
+        "job": {"particles": len(job.records), "moving_atoms": job.density.n_moving,
+                "fixed_atoms": job.density.fixed_atom_count, "directions": len(data.model_rot),
+                "needed_directions": len(job.needed), "maps_per_candidate": maps},
         "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(math.ceil(0.99 * len(lat))) - 1)]},
         "roofline": roofline,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 12 * 8,
@@ -593,15 +648,89 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
         line["serving"] = run_serving(args, device)
     if world == 1 and args.precision_particles > 0:
         line["precision"] = run_precision(args, device)
+    if world == 1:
+        line["deposit_vs_reference"] = run_deposit_comparison(job, data, spec, poses[W], device)
     if world == 1 and not args.no_cpu_baseline:
-        cb = cpu_baseline(spec, data, poses[W], args.cpu_sample)
-        line["cpu_baseline"] = {
-            "value": 1.0 / cb["seconds_per_candidate"], "unit": UNIT, "cores": int(cb["threads"]), "kind": "port",
-            "sample": f"one pose: full moving-chain splat and 3-D FFT, {int(cb['sample_templates'])} templates "
-                      f"timed (extrapolated to the {int(cb['n_templates'])} needed), {int(cb['sample_particles'])} of "
-                      f"{len(job.records)} particles (prepare + correlate), extrapolated "
-                      f"({cb['sample_wall_s']:.1f} s of CPU work)"}
+        line["cpu_baseline"] = run_cpu_baseline(spec, data, poses[W], args.cpu_sample)
     print(json.dumps(line), flush=True)
+
+
+def run_cpu_baseline(spec, data, pose, sample: int) -> dict:
+    """The reference's own CPU path on this job (one pose, 100 particles;
+    about 10 s of CPU work), or the numpy port when baseline/_ref is absent."""
+    import numpy as np
+    from oracle import reference_cpu
+    n_p = len(data.records.rot)
+    if reference_cpu.available():
+        idx = np.unique(np.linspace(0, n_p - 1, min(100, n_p)).astype(int)).tolist()
+        runner = reference_cpu.RefRunner(data)
+        t0 = time.perf_counter()
+        r = runner.step(pose, idx)
+        wall = time.perf_counter() - t0
+        sec = r["density_s"] + r["templates_s"] + r["particles_s"] * n_p / len(idx)
+        return {"value": 1.0 / sec, "unit": UNIT, "cores": runner.threads, "kind": "reference",
+                "sample": f"GisAPR's own CPU torch path from baseline/_ref, one pose: density, "
+                          f"{int(r['n_templates'])} templates, {len(idx)} of {n_p} particles "
+                          f"(particle time scaled to all {n_p}; {wall:.1f} s of CPU work)"}
+    cb = cpu_baseline(spec, data, pose, sample)
+    return {"value": 1.0 / cb["seconds_per_candidate"], "unit": UNIT, "cores": int(cb["threads"]), "kind": "port",
+            "sample": f"numpy port of the reference's CPU path (baseline/_ref absent), one pose: full "
+                      f"moving-chain splat and 3-D FFT, {int(cb['sample_templates'])} templates timed "
+                      f"(extrapolated to the {int(cb['n_templates'])} needed), {int(cb['sample_particles'])} of "
+                      f"{n_p} particles (prepare + correlate), extrapolated ({cb['sample_wall_s']:.1f} s of CPU work)"}
+
+
+def run_deposit_comparison(job, data, spec, pose, device, reps: int = 20) -> dict:
+    """The moving chain onto the cached fixed context, as one candidate's
+    density step: the reference's GPU splat (pdb2mrc v4 with the NVRTC
+    deposit kernel: a clone of the fixed volume, one block per atom, global
+    float atomics) against gisapr_deposit_moved (pose, 8.3 round trip and
+    binned splat fused), device time per call with CUDA events. The
+    reference gets the moved coordinates the way its Lite path does (pose
+    and PDB 8.3 round trip on the host, not timed)."""
+    import numpy as np
+    import torch
+    from oracle import reference_cpu
+    if not reference_cpu.RefDeposit.available():
+        return {"unavailable": "baseline/_ref (the reference's Lite tree) is not installed"}
+    from gisapr_gb300.pdb_text import quantize_coordinates, transform_coordinates
+    dens = job.density
+    mv = dens.moving_xyz.cpu().numpy()
+    moved = quantize_coordinates(transform_coordinates(mv.astype(np.float64), pose,
+                                                        pivot=dens.pivot.cpu().numpy().astype(np.float64)))
+    xyz = torch.from_numpy(np.ascontiguousarray(moved, np.float32)).to(device)
+    z = dens.moving_z.to(device)
+    fixed = dens.fixed.to(device)
+    ref = reference_cpu.RefDeposit()
+    try:
+        ref.deposit(xyz, z, spec.box, spec.apix, spec.res, fixed)  # compiles the kernel (NVRTC)
+    except Exception as exc:  # noqa: BLE001 - reported, not hidden
+        return {"unavailable": f"reference deposit failed: {type(exc).__name__}: {exc}"[:300]}
+    out = torch.empty_like(fixed)
+    pose_dev = dens.pose_tensor(pose).to(device)
+
+    def timed(fn):
+        torch.cuda.synchronize(device)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        fn()
+        a.record()
+        for _ in range(reps):
+            fn()
+        b.record()
+        torch.cuda.synchronize(device)
+        return a.elapsed_time(b) / reps
+
+    ref_ms = timed(lambda: ref.deposit(xyz, z, spec.box, spec.apix, spec.res, fixed))
+    ours_ms = timed(lambda: dens.generate(None, out=out, pose_device=pose_dev))
+    got = ref.deposit(xyz, z, spec.box, spec.apix, spec.res, fixed).cpu().numpy().astype(np.float64)
+    dens.generate(None, out=out, pose_device=pose_dev)
+    mine = out.cpu().numpy().astype(np.float64)
+    rrms = float(np.sqrt(np.sum((mine - got) ** 2) / np.sum(got ** 2)))
+    return {"moving_atoms": int(dens.n_moving), "box": spec.box,
+            "reference_nvrtc_deposit_ms": ref_ms, "gb300_deposit_moved_ms": ours_ms, "speedup": ref_ms / ours_ms,
+            "density_rrms_vs_reference": rrms,
+            "note": "device time per call (CUDA events, mean of 20); the reference clones the fixed volume and "
+                    "adds the moved atoms with global atomics, gisapr_deposit_moved also applies the pose"}
 
 
 def main():

@@ -403,7 +403,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
   static_assert(C % 2 == 0 && C <= 14, "even crop up to 14");
   static_assert(kTcThreads == 32 * (kTcEpiWarp0 + kTcEpiWarps), "warp roles");
   static_assert(kTcEpiWarps == 4 * 3, "three psi angles of four TMEM lane quarters");
+  // TMEM: two accumulators of kN columns, then (C - RR) crop rows of C
+  // columns for each psi of the group (warps of a psi past the group never
+  // touch TMEM); a psi's accumulator columns lie inside the accumulator
   static_assert(2 * tc_n(C) + tc_psi_group(C) * (C - tc_reg_rows<C>()) * C <= kTcTmemCols, "TMEM columns");
+  static_assert(tc_psi_group(C) * tc_psi_stride(C) <= tc_n(C), "psi rows of the accumulator");
   constexpr int kN = tc_n(C);
   constexpr int kPS = tc_psi_stride(C);
   constexpr int S = tc_stages(N);
@@ -602,6 +606,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
     // ---------------- stage 2 and the first maximum per (row, psi)
     constexpr int RR = tc_reg_rows<C>();  // crop rows in registers; rows [RR, C) in TMEM
     const int q4 = warp & 3, my_psi = (warp - kTcEpiWarp0) >> 2;
+    // warps of a psi index past the tile's psi group (the third at crop 14)
+    // own no TMEM rows and never touch TMEM
+    const bool psi_ok = my_psi < tc_psi_group(C);
     const int my_row = 32 * q4 + lane;
     const uint32_t lane_off = (uint32_t)(32 * q4) << 16;
     const uint32_t ta_z = taddr + lane_off + (uint32_t)(my_psi * kPS);
@@ -616,12 +623,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
 #pragma unroll
         for (int j = 0; j < C; ++j) acc[y][j] = 0.f;
       if constexpr (RR < C) {
-        float z[C];
+        if (psi_ok) {
+          float z[C];
 #pragma unroll
-        for (int j = 0; j < C; ++j) z[j] = 0.f;
+          for (int j = 0; j < C; ++j) z[j] = 0.f;
 #pragma unroll
-        for (int y = RR; y < C; ++y) tmem_st_row<C>(z, ta_acc + (uint32_t)((y - RR) * C));
-        asm volatile("tcgen05.wait::st.sync.aligned;");
+          for (int y = RR; y < C; ++y) tmem_st_row<C>(z, ta_acc + (uint32_t)((y - RR) * C));
+          asm volatile("tcgen05.wait::st.sync.aligned;");
+        }
       }
       for (int col = 0; col < H && ok; ++col) {
         const int tb = col & 1;
@@ -674,16 +683,18 @@ __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
           }
         }
       }
+      if (psi_ok) {
 #pragma unroll
-      for (int y = RR; y < C; ++y) {
-        float a[C];
-        tmem_ld_row<C>(a, ta_acc + (uint32_t)((y - RR) * C));
+        for (int y = RR; y < C; ++y) {
+          float a[C];
+          tmem_ld_row<C>(a, ta_acc + (uint32_t)((y - RR) * C));
 #pragma unroll
-        for (int x = 0; x < C; ++x) {
-          const float v = raw_at<C>(a, x);
-          if (v > best) {
-            best = v;
-            bi = y * C + x;
+          for (int x = 0; x < C; ++x) {
+            const float v = raw_at<C>(a, x);
+            if (v > best) {
+              best = v;
+              bi = y * C + x;
+            }
           }
         }
       }

@@ -385,16 +385,46 @@ def run_precision(args, device):
     return out
 
 
-SERVE_JOBS = (("box96_serve", 2000), ("box128_5kp", 2500), ("box192_serve", 1000))  # (workload, particles)
+SERVE_BOXES = ("box96_serve", "box128_5kp", "box192_serve")  # boxes 96 / 128 / 192, 1k / 3k / 6k moving atoms
+SERVE_POOL = 600        # unique particle images per box; jobs draw their particles from these
+SERVE_JOBS = 5          # resident jobs, particles log-uniform over 1,000-20,000
+SERVE_MAX_BATCH = 64
+
+
+def _serve_stream(srv, jids, req_job, req_poses, arrive):
+    """Submit the requests at their arrival times (seconds after t0) from
+    four driver threads; wait for all; (wall seconds, results)."""
+    import threading
+    t0 = time.perf_counter()
+    futs = [None] * len(req_job)
+
+    def driver(d):
+        for i in range(d, len(req_job), 4):
+            wait = t0 + arrive[i] - time.perf_counter()
+            if wait > 0:
+                time.sleep(wait)
+            futs[i] = srv.submit(req_job[i], req_poses[i])
+
+    ts = [threading.Thread(target=driver, args=(d,)) for d in range(4)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    srv.drain()
+    return time.perf_counter() - t0, [f.result() for f in futs]
 
 
 def run_serving(args, device):
-    """A seeded Poisson stream of candidate-evaluation requests from four
-    driver threads over three resident jobs, through the continuous-batching
-    server (fp16 hi/lo tensor-core correlation), and the same stream
-    evaluated serially through the plain FP32 per-candidate path. Latency is
-    arrival to scores on the host."""
-    import threading
+    """Candidate-evaluation requests from concurrent drivers over resident
+    jobs at the serving configuration's shapes: jobs of box 96, 128 or 192
+    with 1,000-20,000 particles (log-uniform), requests of 1-64 candidates,
+    tensor-core split form, continuous batching. Three streams:
+    capacity (every request offered at once, load above capacity),
+    latency (Poisson arrivals at half the measured capacity, p50/p99 from
+    arrival to scores on the host, against serial plain FP32 evaluation of
+    the same stream) and admission (the HBM cap lowered to the largest
+    and smallest jobs' footprints, jobs retired once served, so admission
+    defers jobs)."""
     import numpy as np
     import torch
     from gisapr_gb300 import synthetic as syn
@@ -403,89 +433,117 @@ def run_serving(args, device):
     from gisapr_gb300.tables import model_angles_from_lists
 
     rng = np.random.default_rng(args.seed + 4242)
+    t_gen = time.perf_counter()
+    pools = {name: syn.make_job(syn.WORKLOADS[name], seed=args.seed + 50 + k, device=str(device),
+                                n_particles=SERVE_POOL) for k, name in enumerate(SERVE_BOXES)}
     jobs = {}
-    for k, (name, npart) in enumerate(SERVE_JOBS):
-        spec = syn.WORKLOADS[name]
-        data = syn.make_job(spec, seed=args.seed + 50 + k, device=str(device), n_particles=npart)
+    for k in range(SERVE_JOBS):
+        name = SERVE_BOXES[int(rng.integers(0, len(SERVE_BOXES)))]
+        npart = int(round(math.exp(rng.uniform(math.log(1000.0), math.log(20000.0)))))
+        data = syn.job_from_pool(pools[name], npart, args.seed + 60 + k)
+        spec = data.spec
         cfg = JobConfig(box=spec.box, apix=spec.apix, crop=spec.crop, psi_step=spec.psi_step,
                         local_range=spec.local_range, mask_edge=spec.mask_edge, kk=spec.kk)
-        jobs[f"job{k}"] = (cfg, data, spec)
+        fp = job_footprint_bytes(cfg.box, cfg.new_box, npart, 3, len(data.model_rot), SERVE_MAX_BATCH, "fp16x3")
+        jobs[f"job{k}"] = (cfg, data, spec, fp)
+    t_gen = time.perf_counter() - t_gen
+    jids = sorted(jobs)
 
     def factory(jid):
-        cfg, data, _ = jobs[jid]
+        cfg, data, _, _ = jobs[jid]
         return lambda: ScoringJob(cfg, data.model.pdb_text, model_angles_from_lists(data.model_rot, data.model_tilt),
                                   job_records(data), data.images, fsc_values=data.fsc, device=device)
 
+    def requests(n_req, seed):
+        r = np.random.default_rng(seed)
+        rj = [jids[int(i)] for i in r.integers(0, len(jids), size=n_req)]
+        rn = [int(x) for x in r.integers(1, 65, size=n_req)]
+        rp = [syn.candidate_poses(k, seed + 9000 + i, 5.0, 3.0) for i, k in enumerate(rn)]
+        return rj, rn, rp
+
     n_req = args.serve_requests
-    jids = sorted(jobs)
-    req_job = [jids[int(i)] for i in rng.integers(0, len(jids), size=n_req)]
-    req_n = [int(x) for x in rng.integers(1, 65, size=n_req)]
-    req_poses = [syn.candidate_poses(k, args.seed + 9000 + i, 5.0, 3.0) for i, k in enumerate(req_n)]
-    gaps = rng.exponential(0.100, size=n_req)  # mean 100 ms between arrivals (about 0.3k candidates/s offered)
-    arrive = np.cumsum(gaps)
-    max_batch = 64
-    with ScoringServer(device, hbm_cap_bytes=150e9, max_batch=max_batch, n_workers=3, precision="fp16x3") as srv:
+    out = {"jobs": [f"{jid}: box {jobs[jid][0].box}, {len(jobs[jid][1].records.rot)} particles, "
+                    f"{jobs[jid][3] / 1e9:.1f} GB footprint" for jid in jids],
+           "precision": "fp16x3", "max_batch": SERVE_MAX_BATCH, "workers": 3, "drivers": 4,
+           "synthetic_data_s": t_gen}
+    with ScoringServer(device, hbm_cap_bytes=150e9, max_batch=SERVE_MAX_BATCH, n_workers=3,
+                       precision="fp16x3") as srv:
         for jid in jids:
-            cfg, data, spec = jobs[jid]
-            fp = job_footprint_bytes(cfg.box, cfg.new_box, len(data.records.rot), 3,
-                                     len(data.model_rot), max_batch, "fp16x3")
-            srv.register(jid, factory(jid), fp)
-        # warm-up: build every job and its batch buffers, compile plans
-        for jid in jids:
-            srv.submit(jid, req_poses[0][:1]).result()
+            srv.register(jid, factory(jid), jobs[jid][3])
+        t_build = time.perf_counter()
+        for jid in jids:  # build every job and its batch buffers
+            srv.submit(jid, syn.candidate_poses(1, 7, 5.0, 3.0)).result()
+        out["job_build_s"] = time.perf_counter() - t_build
+        # (A) capacity: every request offered at once
+        rj, rn, rp = requests(n_req, args.seed + 11)
         srv.reset_stats()
         torch.cuda.synchronize(device)
-        t0 = time.perf_counter()
-        futs = [None] * n_req
-
-        def driver(d):
-            for i in range(d, n_req, 4):
-                wait = t0 + arrive[i] - time.perf_counter()
-                if wait > 0:
-                    time.sleep(wait)
-                futs[i] = srv.submit(req_job[i], req_poses[i])
-
-        ts = [threading.Thread(target=driver, args=(d,)) for d in range(4)]
-        for t in ts:
-            t.start()
-        for t in ts:
-            t.join()
-        srv.drain()
-        wall = time.perf_counter() - t0
+        wall, _ = _serve_stream(srv, jids, rj, rp, np.zeros(n_req))
         st = srv.stats()
-        served = [f.result() for f in futs]
-    # serial plain FP32, one candidate at a time, requests in arrival order
+        capacity = sum(rn) / wall
+        out["capacity"] = {"value": capacity, "unit": UNIT, "requests": n_req, "candidates": int(sum(rn)),
+                           "offered": "all requests at t = 0", "wall_s": wall, "batches": st.batches,
+                           "mean_batch": st.mean_batch}
+        # (B) latency at half the measured capacity
+        rj, rn, rp = requests(n_req, args.seed + 12)
+        mean_req = float(np.mean(rn))
+        rate = 0.5 * capacity / mean_req  # requests per second
+        arrive = np.cumsum(np.random.default_rng(args.seed + 13).exponential(1.0 / rate, size=n_req))
+        srv.reset_stats()
+        torch.cuda.synchronize(device)
+        wall, served = _serve_stream(srv, jids, rj, rp, arrive)
+        st = srv.stats()
+        out["latency"] = {"value": sum(rn) / wall, "unit": UNIT, "offered": f"Poisson, {rate:.2f} requests/s "
+                          f"(half the capacity, mean {mean_req:.1f} candidates per request)",
+                          "latency_ms": {"p50": st.latency_ms_p50, "p99": st.latency_ms_p99},
+                          "batches": st.batches, "mean_batch": st.mean_batch}
+    # serial plain FP32 of stream B, one candidate at a time, in arrival order
     sjobs = {jid: factory(jid)() for jid in jids}
     for jid in jids:
-        sjobs[jid].score(req_poses[0][0])
+        sjobs[jid].score(rp[0][0])
     torch.cuda.synchronize(device)
-    lat = []
-    t_free = 0.0
-    serial_scores = []
-    t_busy = 0.0
+    lat, serial_scores = [], []
+    t_free = t_busy = 0.0
     for i in range(n_req):
         t1 = time.perf_counter()
-        serial_scores.append(np.asarray([sjobs[req_job[i]].score(p) for p in req_poses[i]]))
+        serial_scores.append(np.asarray([sjobs[rj[i]].score(p) for p in rp[i]]))
         dt = time.perf_counter() - t1
         t_busy += dt
         start = max(arrive[i], t_free)
         t_free = start + dt
         lat.append(t_free - arrive[i])
-    rel = max(float(np.max(np.abs(a / b - 1.0))) for a, b in zip(served, serial_scores))
+    del sjobs
     lat_ms = np.asarray(lat) * 1e3
-    total = int(sum(req_n))
-    return {
-        "requests": n_req, "candidates": total, "jobs": [f"{n}: {p} particles" for n, p in SERVE_JOBS],
-        "drivers": 4, "workers": 3, "max_batch": max_batch, "precision": "fp16x3",
-        "arrivals": "Poisson, mean gap 100 ms, 1-64 candidates per request",
-        "value": total / wall, "unit": UNIT, "wall_s": wall,
-        "latency_ms": {"p50": st.latency_ms_p50, "p99": st.latency_ms_p99},
-        "batches": st.batches, "mean_batch": st.mean_batch,
-        "serial_plain_fp32": {"value": total / t_busy, "unit": UNIT,
-                              "latency_ms": {"p50": float(np.percentile(lat_ms, 50)),
-                                             "p99": float(np.percentile(lat_ms, 99))}},
-        "max_score_rel_diff_vs_serial_fp32": rel,
-    }
+    out["latency"]["serial_plain_fp32"] = {"value": sum(rn) / t_busy, "unit": UNIT,
+                                           "latency_ms": {"p50": float(np.percentile(lat_ms, 50)),
+                                                          "p99": float(np.percentile(lat_ms, 99))}}
+    out["latency"]["max_score_rel_diff_vs_serial_fp32"] = max(
+        float(np.max(np.abs(a / b - 1.0))) for a, b in zip(served, serial_scores))
+    torch.cuda.empty_cache()
+    # (C) admission under a lowered cap: the largest plus the smallest
+    # footprint, so every job fits alone but not all at once
+    fps = sorted((jobs[j][3] for j in jids), reverse=True)
+    cap = fps[0] + fps[-1]
+    with ScoringServer(device, hbm_cap_bytes=cap, max_batch=SERVE_MAX_BATCH, n_workers=3,
+                       precision="fp16x3") as srv:
+        t0 = time.perf_counter()
+        futs = []
+        for k, jid in enumerate(jids):
+            srv.register(jid, factory(jid), jobs[jid][3])
+        for k, jid in enumerate(jids):
+            futs.append((jid, [srv.submit(jid, syn.candidate_poses(16, args.seed + 300 + 8 * k + i, 5.0, 3.0))
+                               for i in range(4)]))
+        for jid, fl in futs:  # serve each job's requests, then retire it
+            for f in fl:
+                f.result()
+            srv.retire(jid)
+        srv.drain()
+        st = srv.stats()
+        out["admission"] = {"hbm_cap_gb": cap / 1e9, "jobs": len(jids), "deferred_admissions": st.deferred_admissions,
+                            "peak_admitted_gb": st.peak_in_use / 1e9, "candidates": st.candidates,
+                            "wall_s": time.perf_counter() - t0, "out_of_memory": st.out_of_memory}
+    torch.cuda.empty_cache()
+    return out
 
 
 def run_gb300(args, rank: int, world: int, local_rank: int):

@@ -17,7 +17,12 @@ continuously:
 * several workers, each with its own CUDA stream and native context (FFT
   plans and scratch are per context), run different jobs at the same time,
   so their kernels overlap on the GPU; a job runs on one worker at a time;
-* each request's latency (submission to scores on the host) is recorded.
+* each request's latency (submission to scores on the host) is recorded;
+* a batch that runs out of device memory fails its requests with a
+  RuntimeError and releases the job's resident data (rebuilt by its next
+  request), and the server keeps serving, as the Lite tree's worker turns
+  a CUDA out-of-memory error into a recoverable request error
+  (ZL/gisapr_worker_v2.py:131-139).
 
 A candidate's score does not depend on which other candidates share its
 batch (every kernel computes a slot from that slot's inputs only, with a
@@ -121,6 +126,9 @@ class ServerStats:
     latency_ms_p99: float
     batches: int
     mean_batch: float
+    deferred_admissions: int = 0   # registrations that waited for memory to be freed
+    peak_in_use: int = 0           # largest sum of admitted footprints (bytes)
+    out_of_memory: int = 0         # batches that ran out of device memory (requests failed, job released)
 
     @property
     def candidates_per_s(self) -> float:
@@ -156,6 +164,9 @@ class ScoringServer:
         self._t0: Optional[float] = None
         self._t_last = 0.0
         self._errors: List[BaseException] = []
+        self._deferred = 0
+        self._peak_in_use = 0
+        self._oom = 0
         self._workers = [threading.Thread(target=self._work, name=f"gisapr-serve-{i}", daemon=True)
                          for i in range(int(n_workers))]
         for w in self._workers:
@@ -172,6 +183,8 @@ class ScoringServer:
             self._jobs[job_id] = _Job(job_id, factory, int(footprint_bytes), self.precision)
             self._order.append(job_id)
             self._admit_locked()
+            if not self._jobs[job_id].admitted:
+                self._deferred += 1
             self._lock.notify_all()
 
     def retire(self, job_id: str) -> None:
@@ -236,7 +249,9 @@ class ScoringServer:
                                latency_ms_p50=float(np.percentile(lat, 50)) if len(lat) else 0.0,
                                latency_ms_p99=float(np.percentile(lat, 99)) if len(lat) else 0.0,
                                batches=self._batches,
-                               mean_batch=self._candidates / self._batches if self._batches else 0.0)
+                               mean_batch=self._candidates / self._batches if self._batches else 0.0,
+                               deferred_admissions=self._deferred, peak_in_use=self._peak_in_use,
+                               out_of_memory=self._oom)
 
     def reset_stats(self) -> None:
         with self._lock:
@@ -268,6 +283,7 @@ class ScoringServer:
                 break  # admission in registration order
             j.admitted = True
             self._in_use += j.footprint
+            self._peak_in_use = max(self._peak_in_use, self._in_use)
 
     def _maybe_free_locked(self, j: _Job) -> None:
         if j.retiring and j.admitted and not j.pending and not j.busy:
@@ -325,16 +341,37 @@ class ScoringServer:
                     self._batches += 1
                     self._t_last = max(self._t_last, done)
             except BaseException as e:  # noqa: BLE001 - reported through the futures
-                for r in reqs:
-                    if not r.future.done():
-                        r.future.set_exception(e)
-                with self._lock:
-                    self._errors.append(e)
+                if _is_out_of_memory(e):
+                    # recoverable: release what the job holds on the device and
+                    # fail only this batch; the job is rebuilt by its next request
+                    err = RuntimeError(f"job {j.job_id!r}: the batch ran out of device memory; its requests "
+                                       f"failed and the job's device data was released (it is rebuilt on the "
+                                       f"next request). Lower max_batch or the HBM cap.")
+                    err.__cause__ = e
+                    j.job = None
+                    j.batch = None
+                    self._release_device_memory()
+                    for r in reqs:
+                        if not r.future.done():
+                            r.future.set_exception(err)
+                    with self._lock:
+                        self._oom += 1
+                else:
+                    for r in reqs:
+                        if not r.future.done():
+                            r.future.set_exception(e)
+                    with self._lock:
+                        self._errors.append(e)
             finally:
                 with self._lock:
                     j.busy = False
                     self._maybe_free_locked(j)
                     self._lock.notify_all()
+
+    def _release_device_memory(self) -> None:
+        import torch
+        if torch.cuda.is_available():
+            torch.cuda.empty_cache()
 
     def _run(self, j: _Job, poses: np.ndarray, stream) -> np.ndarray:
         import torch
@@ -344,6 +381,18 @@ class ScoringServer:
                 j.job = j.factory()
                 j.batch = BatchScoringJob(j.job, self.max_batch, use_graph=False, precision=j.precision)
         return j.batch.score_active(list(poses), stream=stream)
+
+
+def _is_out_of_memory(e: BaseException) -> bool:
+    """A CUDA out-of-memory error from torch's allocator or from the
+    library's own cudaMalloc (reported as RuntimeError naming it)."""
+    try:
+        import torch
+        if isinstance(e, torch.cuda.OutOfMemoryError):
+            return True
+    except ImportError:  # pragma: no cover - torch is always present
+        pass
+    return isinstance(e, RuntimeError) and "out of memory" in str(e).lower()
 
 
 def _join_futures(parts: List[Future], out: Future) -> None:

@@ -529,6 +529,25 @@ def make_job(spec: WorkloadSpec, seed: int = 1, device: str = "cpu",
                      np.stack([rot, tilt, psi], 1), shifts)
 
 
+def job_from_pool(pool: SearchJob, n_particles: int, seed: int) -> SearchJob:
+    """A job of ``n_particles`` particles drawn (with repeats) from a pool
+    job of the same model and box: each drawn particle keeps its image, its
+    STAR angles and defocus, and gets its own STAR line. Large serving jobs
+    (up to 20,000 particles) are built this way in seconds; the search work
+    per particle has the pool's distribution."""
+    rng = np.random.default_rng(seed)
+    n_pool = len(pool.records.rot)
+    pick = np.arange(int(n_particles)) % n_pool if n_particles <= n_pool else \
+        np.concatenate([np.arange(n_pool), rng.integers(0, n_pool, size=int(n_particles) - n_pool)])
+    r = pool.records
+    rec = ParticleRecords(line_index=np.arange(len(pick), dtype=np.int64) + 20, rot=r.rot[pick],
+                          tilt=r.tilt[pick], psi=r.psi[pick], defocus_u=r.defocus_u[pick],
+                          defocus_v=r.defocus_v[pick], defocus_angle=r.defocus_angle[pick])
+    return SearchJob(pool.spec, pool.model, pool.model_rot, pool.model_tilt, pool.images[pick], rec, pool.fsc,
+                     None if pool.true_angles is None else pool.true_angles[pick],
+                     None if pool.true_shifts is None else pool.true_shifts[pick])
+
+
 def reference_density(coords, elements, box, apix, res) -> np.ndarray:
     """Plain float64 Gaussian splat used only to make particles."""
     z = np.asarray([{"H": 1, "C": 6, "N": 7, "O": 8, "P": 15, "S": 16}.get(e.upper(), 0)

@@ -16,6 +16,13 @@ from gisapr_gb300.tables import ParticleRecord
 DENSITY_RRMS = 1e-5
 SPECTRUM_RRMS = 1e-5
 TEMPLATE_RRMS = 1e-4
+# Templates of a smooth model density (the box-128 fixture's chains with the
+# logistic FSC): its outer shells sit near float32 rounding, which the
+# whitening rescales to unit amplitude. The reference's float32 templates are
+# 6.7e-4 from the FP64 oracle there and the GPU's 1.7e-4, so the GPU bar for
+# that density is 2.5e-4 (1e-4 holds for densities whose shells stay above
+# rounding, the blob-and-noise densities of the other template tests).
+TEMPLATE_RRMS_SMOOTH = 2.5e-4
 # the reference's own distance from the oracle (measured maxima, rounded up)
 TEMPLATE_REF_FLOOR = {32: 1e-4, 64: 1e-4, 96: 1e-4, 128: 7e-4, 192: 1e-4, 256: 1.5e-4}
 

@@ -130,3 +130,61 @@ def test_footprint_counts_projector_scratch():
     assert projector_scratch_bytes(96, 96, 10) == G * 10 * (96 * 97 + 96 * 49) * 8
     assert projector_scratch_bytes(192, 192, 10000) == G * 456 * (192 * 193 + 192 * 97) * 8
     assert job_footprint_bytes(256, 256, 4000, 3, 3072, 8) - small > 0
+
+
+def test_out_of_memory_fails_the_batch_and_releases_the_job():
+    """A batch that runs out of device memory fails its own requests with a
+    recoverable error, the job's device data is dropped and rebuilt by the
+    next request, and the server keeps serving (the Lite worker's OOM path)."""
+    import torch
+
+    class OomOnce(FakeServer):
+        def __init__(self, *a, **k):
+            self.boom = True
+            self.released = 0
+            super().__init__(*a, **k)
+
+        def _release_device_memory(self):
+            self.released += 1
+
+        def _run(self, j, poses, stream):
+            if j.job is None:
+                j.job = j.factory()
+                with self.lock2:
+                    self.built.append(j.job_id)
+            if self.boom:
+                self.boom = False
+                raise torch.cuda.OutOfMemoryError("CUDA out of memory. Tried to allocate 2.00 GiB")
+            return poses.sum(axis=1) * j.job
+
+    with OomOnce(max_batch=8, n_workers=1) as srv:
+        srv.register("a", lambda: 2.0, 10)
+        f1 = srv.submit("a", poses_of(1, 3))
+        with pytest.raises(RuntimeError, match="ran out of device memory"):
+            f1.result(timeout=30)
+        p = poses_of(2, 4)
+        np.testing.assert_array_equal(srv.submit("a", p).result(timeout=30), p.sum(axis=1) * 2.0)
+        srv.drain(timeout=30)  # no unrecoverable error recorded
+        st = srv.stats()
+        assert st.out_of_memory == 1 and srv.released == 1
+        assert srv.built == ["a", "a"]  # the job was rebuilt after the failure
+
+
+def test_library_allocation_failure_counts_as_out_of_memory():
+    from gisapr_gb300.serving import _is_out_of_memory
+    assert _is_out_of_memory(RuntimeError("cudaMalloc(planes): out of memory"))
+    assert not _is_out_of_memory(RuntimeError("tensor-core correlation: an on-chip barrier wait ran out"))
+    assert not _is_out_of_memory(ValueError("out of memory"))
+
+
+def test_deferred_admissions_and_peak_memory_are_counted():
+    with FakeServer(hbm_cap_bytes=100, max_batch=8, n_workers=1) as srv:
+        srv.register("a", lambda: 1.0, 70)
+        srv.register("b", lambda: 2.0, 50)   # deferred
+        srv.register("c", lambda: 3.0, 20)   # deferred behind b (registration order)
+        st = srv.stats()
+        assert st.deferred_admissions == 2 and st.peak_in_use == 70
+        srv.submit("a", poses_of(1, 2)).result(timeout=30)
+        srv.retire("a")
+        srv.submit("b", poses_of(2, 2)).result(timeout=30)
+        assert srv.stats().peak_in_use == 70

@@ -26,6 +26,7 @@ SIGNATURES = {
     "gisapr_deposit_noalloc": [_p, _p, _p, _i, _p, _i, _i, _d, _d, _d],
     "gisapr_deposit_moved": [_p, _p, _p, _p, _i, _p, _p, _p, _p, _p, _i, _i, _i, _d, _d, _d],
     "gisapr_volume_spectrum": [_p, _p, _p, _i, _p],
+    "gisapr_volume_spectrum_blocked": [_p, _p, _p, _i],
     "gisapr_project_templates": [_p, _p, _p, _i, _p, _p, _i, _p, _p, _p, _i, _p],
     "gisapr_packed_ctf": [_p, _p, _p, _p, _i, _p, _p, _p, _p, _i, _f, _f, _f, _f, _f, _p],
     "gisapr_prepare_particles": [_p, _p, _p, _i, _i, _p, _p, _p, _p, _i, _i, _p],

@@ -23,7 +23,8 @@ SRC = PKG / "csrc"
 OUT = PKG / "_native"
 LIB = OUT / "libgisapr_gb300.so"
 INCLUDE = PKG.parent / "include"
-SOURCES = ["splat.cu", "project.cu", "particles.cu", "correlate.cu", "correlate_tc.cu", "restraint.cu", "ingest.cu", "abi.cu"]
+SOURCES = ["splat.cu", "project.cu", "volfft.cu", "particles.cu", "correlate.cu", "correlate_tc.cu", "restraint.cu",
+           "ingest.cu", "abi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -47,6 +47,8 @@ cudaError_t launch_project_templates_planes(cudaStream_t, const float2*, const f
                                             const float*, int, const float2*, const float2*, float2*, float2*,
                                             int, int, int, float2*, float2*, int);
 size_t project_flat_plane_elems(int N, int n);
+size_t vfft_scratch_elems(int N);
+cudaError_t launch_volume_spectrum_blocked(cudaStream_t, const float*, int, float2*, float2*, const float2*);
 cudaError_t launch_packed_ctf(cudaStream_t, const float*, const float*, const float*, int,
                               const float*, const float*, const float*, const float*, int, float,
                               float, float, float, float, float*);
@@ -138,7 +140,8 @@ struct gisapr_context {
   std::map<int, std::pair<cufftHandle, float*>> fft;  // box -> (R2C plan, padded input)
   std::map<int, BinTable> bins;                        // N -> radial bins
   std::map<std::pair<int, int>, CorrTables> corr;      // (n, crop) -> twiddles
-  DeviceBuffer atoms, bin_counts, bin_lists, proj_scratch, prep_scratch, proj_slices, proj_blocked;
+  DeviceBuffer atoms, bin_counts, bin_lists, proj_scratch, prep_scratch, proj_slices, proj_blocked, vfft_scratch;
+  int blocked_box = 0;  // box of the blocked spectrum gisapr_volume_spectrum_blocked last wrote (0: none)
   // Buffers replaced by larger ones. They are freed only with the context:
   // a CUDA graph captured before a buffer grew still names the old one, and
   // that buffer stays valid (and large enough for the graph's own sizes).
@@ -368,6 +371,7 @@ int gisapr_context_destroy(gisapr_ctx ctx) {
   cudaFree(ctx->proj_slices.ptr);
   cudaFree(ctx->proj_blocked.ptr);
   cudaFree(ctx->prep_scratch.ptr);
+  cudaFree(ctx->vfft_scratch.ptr);
   cudaFree(ctx->tw);
   for (void* p : ctx->retired) cudaFree(p);
   cudaFree(ctx->tw3);
@@ -461,13 +465,33 @@ int gisapr_project_launches(int box, int n_build) {
   return 1;
 }
 
+int gisapr_volume_spectrum_blocked(gisapr_ctx ctx, void* stream, const float* volume, int box) {
+  if (!ctx || !volume) return fail(GISAPR_ERR_ARGUMENT, "context or volume is NULL");
+  if (!(is_pow2(box) && box >= 32 && box <= 256))
+    return fail(GISAPR_ERR_UNSUPPORTED, "the blocked volume transform takes a power-of-two box in [32, 256]");
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  rc = ensure(ctx, ctx->vfft_scratch, vfft_scratch_elems(box) * sizeof(float2), "cudaMalloc(volume transform)");
+  if (rc) return rc;
+  rc = ensure(ctx, ctx->proj_blocked, project_blocked_elems(box) * sizeof(float2), "cudaMalloc(blocked spectrum)");
+  if (rc) return rc;
+  GISAPR_CHECK_CUDA(launch_volume_spectrum_blocked((cudaStream_t)stream, volume, box, (float2*)ctx->vfft_scratch.ptr,
+                                                   (float2*)ctx->proj_blocked.ptr, ctx->tw),
+                    "volume_spectrum_blocked");
+  ctx->blocked_box = box;
+  return GISAPR_OK;
+}
+
 int gisapr_project_templates(gisapr_ctx ctx, void* stream, const float* spectrum, int box,
                              const float* rot, const int* dirs, int n_build, const int* out_slot,
                              const float* mask, const float* fsc, int newbox, float* bank) {
-  if (!ctx || !spectrum || !rot || !dirs || !fsc || !bank)
+  if (!ctx || !rot || !dirs || !fsc || !bank)
     return fail(GISAPR_ERR_ARGUMENT, "a required pointer is NULL");
   int rc = check_box(box);
   if (rc) return rc;
+  if (!spectrum && ctx->blocked_box != box)
+    return fail(GISAPR_ERR_ARGUMENT, "spectrum is NULL and no blocked spectrum of this box was written "
+                                     "(gisapr_volume_spectrum_blocked) on this context");
   rc = check_newbox(box, newbox);
   if (rc) return rc;
   if (n_build < 0) return fail(GISAPR_ERR_ARGUMENT, "n_build < 0");
@@ -490,6 +514,7 @@ int gisapr_project_templates(gisapr_ctx ctx, void* stream, const float* spectrum
                                                     bt.n_bins, ctx->tw, (float2*)bank, grid, box, newbox,
                                                     (float2*)ctx->proj_slices.ptr, (float2*)ctx->proj_blocked.ptr),
                       "project_templates");
+    ctx->blocked_box = box;
     return GISAPR_OK;
   }
   // CTAs per SM of the general path (measured on GB300): smaller boxes fill
@@ -513,6 +538,7 @@ int gisapr_project_templates(gisapr_ctx ctx, void* stream, const float* spectrum
                                                       (float2*)ctx->proj_slices.ptr, (float2*)ctx->proj_blocked.ptr,
                                                       chunk),
                       "project_templates");
+    ctx->blocked_box = box;
     return GISAPR_OK;
   }
   GISAPR_CHECK_CUDA(launch_project_templates((cudaStream_t)stream, (const float2*)spectrum, rot, dirs, n_build,

@@ -335,3 +335,27 @@ GISAPR_DEV float2 tw_full(const float2* __restrict__ tw, int t, int L) {
   float2 w = u < kMaxFftLen / 2 ? tw[u] : make_float2(-tw[u - kMaxFftLen / 2].x, -tw[u - kMaxFftLen / 2].y);
   return DIR < 0 ? w : make_float2(w.x, -w.y);
 }
+
+// ---------------------------------------------------------------------------
+// The reference's real-space gridding correction (v606:837-853): the padded
+// volume is multiplied by sinc(|f|)^2, f the fftshifted fftfreq of the 2N grid.
+// ---------------------------------------------------------------------------
+GISAPR_DEV float fftfreq_shifted_f32(int i, int m) {
+  // fftshift(fftfreq(m))[i] = (i - m/2) * float(1/m)
+  return __fmul_rn((float)(i - m / 2), (float)(1.0 / (double)m));
+}
+
+// float32 sinc(r)^2 in the operation order of the reference filter
+// (v606:841-853 with torch.sinc: sin(pi*r)/(pi*r), 1 at r == 0).
+GISAPR_DEV float sinc2_f32(float fz2, float fy2, float fx2) {
+  float r = sqrtf(__fadd_rn(__fadd_rn(fz2, fy2), fx2));
+  float s;
+  if (r == 0.0f) {
+    s = 1.0f;
+  } else {
+    float prod = __fmul_rn(3.14159274101257324219f, r);
+    s = __fdiv_rn(sinf(prod), prod);
+  }
+  return __fmul_rn(s, s);
+}
+

@@ -34,6 +34,7 @@
 // sum cancels sit on the conjugation boundary (v606:881-885), and any other
 // rounding there picks the mirrored sample.
 #include "common.cuh"
+#include "warpfft.cuh"
 
 namespace {
 
@@ -157,72 +158,6 @@ __device__ __forceinline__ float block_sum_f(float v, float* scratch) {
 #pragma unroll
   for (int w = 1; w < NW; ++w) t += scratch[w];
   return t;
-}
-
-// Row stride (complex elements) of the padded shared-memory plane: holds the
-// N + 1 columns plus one spare slot per 8, chosen by a bank-conflict search.
-// Box 256 has no shared-memory plane; its value there is the stride of
-// rows_inverse's staging lines (256 elements plus one spare slot per 8).
-__host__ __device__ constexpr int plane_ld(int N) {
-  return N == 256 ? 290 : (N == 128 ? 150 : (N == 64 ? 74 : 38));
-}
-__host__ __device__ constexpr int plane_rows(int N) { return N + N / 8; }
-
-// Lines of length N with one spare slot per 8 elements, line stride
-// plane_ld(N): element k of line g.
-template <int N>
-struct StageLines {
-  float2* p;
-  __device__ __forceinline__ float2& at(int g, int k) const { return p[g * plane_ld(N) + k + (k >> 3)]; }
-};
-
-// In-place four-step FFT of ``nlines`` (<= 32 / (N/16)) lines, natural order
-// in and out: a 16-point register codelet over n1, twiddles, then N/16-point
-// codelets over n2 (N = 16 * (N/16)). One warp, warp barriers only. With
-// ``cj`` the input is conjugated on load and the output on store, which
-// turns the transform into the one of the opposite direction.
-template <int N, int DIR, class Lines>
-__device__ __forceinline__ void warp_fft(const Lines& L, int nlines, const float2* tw, bool cj = false) {
-  constexpr int L2 = N / 16, G = 32 / L2, T = (G * 16) / 32;
-  const int lane = threadIdx.x & 31;
-  {
-    const int g = lane / L2, n2 = lane % L2;
-    if (g < nlines) {
-      float2 x[16];
-#pragma unroll
-      for (int n1 = 0; n1 < 16; ++n1) {
-        x[n1] = L.at(g, L2 * n1 + n2);
-        if (cj) x[n1].y = -x[n1].y;
-      }
-      dft<16, DIR>(x);
-#pragma unroll
-      for (int k1 = 1; k1 < 16; ++k1)
-        if (n2) x[k1] = cmul(x[k1], tw_full<DIR>(tw, n2 * k1, N));
-#pragma unroll
-      for (int k1 = 0; k1 < 16; ++k1) L.at(g, L2 * k1 + n2) = x[k1];
-    }
-  }
-  __syncwarp();
-  float2 y[T][L2];
-#pragma unroll
-  for (int t = 0; t < T; ++t) {
-    const int task = lane + 32 * t, g = task / 16, k1 = task % 16;
-    if (g < nlines) {
-#pragma unroll
-      for (int n2 = 0; n2 < L2; ++n2) y[t][n2] = L.at(g, L2 * k1 + n2);
-      dft<L2, DIR>(y[t]);
-    }
-  }
-  __syncwarp();
-#pragma unroll
-  for (int t = 0; t < T; ++t) {
-    const int task = lane + 32 * t, g = task / 16, k1 = task % 16;
-    if (g < nlines) {
-#pragma unroll
-      for (int k2 = 0; k2 < L2; ++k2) L.at(g, k1 + 16 * k2) = cj ? cconj(y[t][k2]) : y[t][k2];
-    }
-  }
-  __syncwarp();
 }
 
 // Line batches of the general kernel in shared memory. Box 256 runs its
@@ -1126,14 +1061,18 @@ __global__ void __launch_bounds__(kRiWarps * 32) rows_inverse(const float2* __re
   for (int t = threadIdx.x; t < kMaxFftLen / 2; t += blockDim.x) s_tw[t] = tw_g[t];
   const float* R = rot + (size_t)dirs[b] * 9;
   float2(*L)[LINE] = s_line[warp];
-  // lanes take nc columns x 32/nc rows per step: samples of neighbouring
-  // columns share trilinear corners, and this patch shape cut the gather's
-  // time by 40% against 32 rows of one column on GB300
+  // The CTA gathers its columns together: a warp load takes all ncta
+  // (usually 8) columns x 32/ncta rows, a compact patch of the slice whose
+  // trilinear corners share the blocked copy's 128-byte lines (2 columns x
+  // 16 rows per load had cut the gather's time by 40% against 32 rows of
+  // one column); each sample lands in the staged line of the warp that
+  // transforms its column.
+  const int ncta = max(0, min(CC, W - c_cta));
 #pragma unroll 4
-  for (int idx = lane; idx < nc * m; idx += 32) {
-    const int cl = idx % nc, r = idx / nc;
+  for (int idx = threadIdx.x; idx < ncta * m; idx += blockDim.x) {
+    const int cc = idx % ncta, r = idx / ncta;
     const int k = r >> 1;
-    L[2 * cl + (r & 1)][k + (k >> 3)] = slice_value<N>(spectrum, R, r, cw + cl);
+    s_line[cc / CPR][2 * (cc % CPR) + (r & 1)][k + (k >> 3)] = slice_value<N>(spectrum, R, r, c_cta + cc);
   }
   __syncthreads();
   if (nc > 0) {
@@ -1148,7 +1087,6 @@ __global__ void __launch_bounds__(kRiWarps * 32) rows_inverse(const float2* __re
   __syncthreads();
   constexpr int OUT = plane_out_ld<N>();
   float2* dst = planes + (size_t)b * N * OUT;
-  const int ncta = min(CC, W - c_cta);
   for (int e = threadIdx.x; e < N * CC; e += blockDim.x) {
     const int y = e / CC, cl = e - y * CC, c = c_cta + cl;
     if (cl < ncta) dst[(size_t)y * OUT + (flat_plane<N>() ? c : c + (c >> 3))] = s_out[y][cl];
@@ -1223,9 +1161,12 @@ size_t project_smem_bytes_fast(int N, int n_bins, int nb) {
 template <int N>
 static cudaError_t launch_fast(ProjParams P, int grid, float2* planes, float2* blocked, cudaStream_t st) {
   constexpr int CC = ri_cols<N>();
-  spectrum_blocked<N><<<8 * 152, 256, 0, st>>>(P.spectrum, blocked);
-  cudaError_t e0 = cudaGetLastError();
-  if (e0 != cudaSuccess) return e0;
+  cudaError_t e0 = cudaSuccess;
+  if (P.spectrum != nullptr) {  // else the blocked copy was written by the volume transform
+    spectrum_blocked<N><<<8 * 152, 256, 0, st>>>(P.spectrum, blocked);
+    e0 = cudaGetLastError();
+    if (e0 != cudaSuccess) return e0;
+  }
   rows_inverse<N><<<dim3((N + 1 + CC - 1) / CC, P.n_build), kRiWarps * 32, 0, st>>>(blocked, P.rot, P.dirs, P.tw,
                                                                                       planes);
   e0 = cudaGetLastError();
@@ -1276,9 +1217,12 @@ cudaError_t launch_project_templates_planes(cudaStream_t st, const float2* spect
   constexpr int kN = 256, CC = ri_cols<kN>();
   if (n_build <= 0) return cudaSuccess;
   if (N != kN || chunk <= 0 || chunk > 65535 || grid <= 0) return cudaErrorInvalidValue;
-  spectrum_blocked<kN><<<8 * 152, 256, 0, st>>>(spectrum, blocked);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
+  cudaError_t e = cudaSuccess;
+  if (spectrum != nullptr) {  // else the blocked copy was written by the volume transform
+    spectrum_blocked<kN><<<8 * 152, 256, 0, st>>>(spectrum, blocked);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
   ProjParams P;
   P.spectrum = spectrum; P.rot = rot; P.mask = mask; P.fsc = fsc; P.bin_list = bin_list; P.bin_ptr = bin_ptr;
   P.bin_count = bin_count; P.n_bins = n_bins; P.tw = tw; P.tw3 = tw3; P.bank = bank; P.scratch = scratch;

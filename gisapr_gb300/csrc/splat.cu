@@ -120,24 +120,7 @@ __global__ void atoms_prepare(const float* __restrict__ xyz, const float* __rest
   out[i] = r;
 }
 
-// float32 sinc(r)^2 in the operation order of the reference filter
-// (v606:841-853 with torch.sinc: sin(pi*r)/(pi*r), 1 at r == 0).
-__device__ __forceinline__ float sinc2_f32(float fz2, float fy2, float fx2) {
-  float r = sqrtf(__fadd_rn(__fadd_rn(fz2, fy2), fx2));
-  float s;
-  if (r == 0.0f) {
-    s = 1.0f;
-  } else {
-    float prod = __fmul_rn(3.14159274101257324219f, r);
-    s = __fdiv_rn(sinf(prod), prod);
-  }
-  return __fmul_rn(s, s);
-}
 
-__device__ __forceinline__ float fftfreq_shifted_f32(int i, int m) {
-  // fftshift(fftfreq(m))[i] = (i - m/2) * float(1/m)
-  return __fmul_rn((float)(i - m / 2), (float)(1.0 / (double)m));
-}
 
 __global__ void __launch_bounds__(256)
 splat_bricks(const AtomRec* __restrict__ atoms, int n_atoms, const float* initial,
@@ -549,7 +532,9 @@ cudaError_t launch_splat_binned(cudaStream_t st, const float* xyz, const float* 
   cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(int) * nbricks, st);
   if (e != cudaSuccess) return e;
   if (n > 0) {
-    atoms_prepare_binned<<<(n + 255) / 256, 256, 0, st>>>(xyz, numbers, n, transform, pivot, rot, shift, box,
+    // 64 threads a block: a few thousand atoms spread over many SMs (the
+    // FP64 pose and 8.3 rounding are long dependent chains per atom)
+    atoms_prepare_binned<<<(n + 63) / 64, 64, 0, st>>>(xyz, numbers, n, transform, pivot, rot, shift, box,
                                                            width, apix, kn, (AtomRec*)atom_recs, counts, lists,
                                                            cap);
     e = cudaGetLastError();

@@ -124,6 +124,11 @@ class ScoringJob:
             pdb_text, cfg.chain_id, n, cfg.apix, cfg.resolution, dev, include_hetatm=cfg.include_hetatm,
             from_text=True)
         self.projector = IntegratedProjector(dev, n, nb, self.layout, self.mask, self.packed_fsc)
+        # power-of-two boxes: the splat writes the density and the blocked
+        # volume transform reads it; other boxes: the splat writes the padded
+        # FFT input of the cuFFT transform
+        self.vol_buf = torch.empty((n, n, n), dtype=torch.float32, device=dev) \
+            if self.projector.blocked_fft else None
         self._alloc_search_buffers()
         np_ = len(self.records)
         self.best_entry = torch.empty(np_, dtype=torch.int32, device=dev)
@@ -184,10 +189,11 @@ class ScoringJob:
         self._warm.clear()
 
     # ------------------------------------------------------------------
-    # launches of this engine per scored candidate at box <= 128 (cuFFT's own
-    # kernels not counted): atoms + splat, blocked spectrum copy + slice rows +
-    # template tail, correlation, records, score sum
-    KERNELS_PER_CANDIDATE = 8
+    # launches of this engine per scored candidate at a power-of-two box up
+    # to 128: atoms + splat, the three passes of the volume transform, slice
+    # rows + template tail, correlation, records, score sum (at boxes 96 and
+    # 192 the volume transform is cuFFT's, whose kernels are not counted)
+    KERNELS_PER_CANDIDATE = 10
 
     @staticmethod
     def projector_launches(box: int, n_build: int = 1) -> int:
@@ -201,8 +207,18 @@ class ScoringJob:
             raise ValueError(f"unsupported box {box}")
         return n
 
+    def template_launches(self) -> int:
+        """Kernels of this library that one candidate's density, volume
+        transform and templates enqueue: the splat (2), the blocked volume
+        transform (3) and the projector without its blocked copy at
+        power-of-two boxes; elsewhere the splat and the projector."""
+        proj = self.projector_launches(self.cfg.box, len(self.needed))
+        if self.projector.blocked_fft:
+            return 2 + 3 + max(0, proj - 1)
+        return 2 + proj
+
     def launches_per_candidate(self) -> int:
-        return 5 + self.projector_launches(self.cfg.box, len(self.needed))
+        return self.template_launches() + 3
     STAGES = ("density", "volume_fft", "templates", "correlate", "records")
 
     def enqueue(self, pose_device: torch.Tensor, write_volume: Optional[torch.Tensor] = None,
@@ -215,9 +231,30 @@ class ScoringJob:
             raise ValueError("this job has no model; score densities with score_volume")
         mark = self._marker(stage_events)
         mark("density", False)
-        self.density.generate(None, out=write_volume, write_padded=True, pose_device=pose_device)
+        vol = self.model_density(self.density, pose_device, write_volume)
         mark("density", True)
-        self._enqueue_search(None, mark)
+        self._enqueue_search(vol, mark)
+
+    def model_density(self, model, pose_device: torch.Tensor, out: Optional[torch.Tensor] = None):
+        """Enqueue one moved-chain density for the projector: into ``out``
+        (or the job's buffer) for the blocked transform of power-of-two
+        boxes, else into the padded FFT input (returns None)."""
+        if self.projector.blocked_fft:
+            vol = out if out is not None else self.vol_buf
+            model.generate(None, out=vol, write_padded=False, pose_device=pose_device)
+            return vol
+        model.generate(None, out=out, write_padded=True, pose_device=pose_device)
+        return None
+
+    def enqueue_templates(self, volume: Optional[torch.Tensor], bank: torch.Tensor) -> None:
+        """Volume spectrum and the needed templates into ``bank`` (``volume``
+        None: the padded FFT input the splat wrote)."""
+        if self.projector.blocked_fft:
+            self.projector.volume_spectrum_blocked(volume)
+        else:
+            self.projector.volume_spectrum(volume)
+        if self.needed:
+            self.projector.project(self.angles, self.needed_dirs, bank, self.needed_slots)
 
     def enqueue_volume(self, volume: torch.Tensor, stage_events: Optional[Dict[str, list]] = None) -> None:
         """Enqueue the search of one given density ([box]^3 float32 on the
@@ -246,7 +283,10 @@ class ScoringJob:
         ctx = nat.Context.for_device(self.device).handle
         st = nat.stream_of(self.device)
         mark("volume_fft", False)
-        self.projector.volume_spectrum(volume)
+        if self.projector.blocked_fft:
+            self.projector.volume_spectrum_blocked(volume)
+        else:
+            self.projector.volume_spectrum(volume)
         mark("volume_fft", True)
         mark("templates", False)
         if self.needed:
@@ -516,7 +556,7 @@ class BatchScoringJob:
     def launches_per_batch(self) -> int:
         # per slot: splat (2 launches) and the projector; fp16 hi/lo bank copy
         # and tensor-core kernel per chunk instead of one plain kernel
-        per_slot = 2 + ScoringJob.projector_launches(self.job.cfg.box, len(self.job.needed))
+        per_slot = self.job.template_launches()
         extra = 2 * len(self.tc_chunks) - 1 if self.precision != "fp32" else 0
         return self.n_cand * per_slot + self.KERNELS_PER_BATCH + extra
 
@@ -542,10 +582,8 @@ class BatchScoringJob:
 
         mark("start")
         for c in range(n_act):
-            self.models[self.model_of[c]].generate(None, write_padded=True, pose_device=self.poses_dev[c])
-            job.projector.volume_spectrum(None)
-            if job.needed:
-                job.projector.project(job.angles, job.needed_dirs, self.banks[c], job.needed_slots)
+            vol = job.model_density(self.models[self.model_of[c]], self.poses_dev[c])
+            job.enqueue_templates(vol, self.banks[c])
         mark("templates")
         np_ = len(job.records)
         if self.precision == "fp32":

@@ -174,6 +174,12 @@ class IntegratedProjector:
         self.batch_size = max(1, int(projection_batch_size))
         self._rot_cache = None
         self.spectrum = None
+        # power-of-two boxes transform the density straight into the blocked
+        # copy the slice gather reads (gisapr_volume_spectrum_blocked);
+        # False keeps the cuFFT spectrum + blocked copy of volume_spectrum
+        n = self.original_box
+        self.blocked_fft = n & (n - 1) == 0 and 32 <= n <= 256
+        self._from_blocked = False
 
     def _rot(self, angles: ModelAngles) -> torch.Tensor:
         key = id(angles.rotation_matrices_t)
@@ -188,13 +194,30 @@ class IntegratedProjector:
             self.spectrum = torch.empty((2 * n, 2 * n, n + 1), dtype=torch.complex64, device=self.device)
         nat.call("gisapr_volume_spectrum", nat.Context.for_device(self.device).handle,
                  nat.stream_of(self.device), nat.ptr(volume), n, nat.ptr(self.spectrum))
+        self._from_blocked = False
         return self.spectrum
+
+    def volume_spectrum_blocked(self, volume: torch.Tensor) -> None:
+        """The density's half-volume spectrum, straight into the context's
+        blocked copy (power-of-two boxes); the next project() reads it."""
+        nat.call("gisapr_volume_spectrum_blocked", nat.Context.for_device(self.device).handle,
+                 nat.stream_of(self.device), nat.ptr(volume), self.original_box)
+        self._from_blocked = True
+
+    def prepare(self, volume: torch.Tensor) -> None:
+        """The spectrum the projector samples, by the transform of this box."""
+        if self.blocked_fft:
+            self.volume_spectrum_blocked(volume)
+        else:
+            self.volume_spectrum(volume)
 
     def project(self, angles: ModelAngles, dirs: torch.Tensor, out: torch.Tensor,
                 out_slot: Optional[torch.Tensor] = None) -> torch.Tensor:
-        """Templates of ``dirs`` from the last volume_spectrum into ``out``."""
+        """Templates of ``dirs`` from the last volume_spectrum (or
+        volume_spectrum_blocked) into ``out``."""
         nat.call("gisapr_project_templates", nat.Context.for_device(self.device).handle,
-                 nat.stream_of(self.device), nat.ptr(self.spectrum), self.original_box,
+                 nat.stream_of(self.device), nat.ptr(None if self._from_blocked else self.spectrum),
+                 self.original_box,
                  nat.ptr(self._rot(angles)), nat.ptr(dirs), int(dirs.numel()), nat.ptr(out_slot),
                  nat.ptr(self.real_space_mask), nat.ptr(self.packed_fsc), self.new_box, nat.ptr(out))
         return out
@@ -219,7 +242,7 @@ class IntegratedProjector:
                           device=self.device)
         if not selected:
             return out
-        self.volume_spectrum(volume.contiguous())
+        self.prepare(volume.contiguous())
         dirs = torch.tensor(selected, dtype=torch.int32, device=self.device)
         slots = torch.arange(len(selected), dtype=torch.int32, device=self.device)
         return self.project(angles, dirs, out, slots)

@@ -110,6 +110,17 @@ int gisapr_volume_spectrum(gisapr_ctx ctx, void* stream, const float* volume, in
                            float* spectrum);
 
 /*
+ * The half-volume spectrum of gisapr_volume_spectrum for a power-of-two box
+ * (32..256), computed from the box^3 density without the (2*box)^3 padded
+ * volume (each 2N-point transform of N nonzero samples as two N-point ones)
+ * and kept in the context in the blocked layout the slice gather reads, for
+ * gisapr_project_templates with spectrum == NULL. Replaces the same
+ * reference steps as gisapr_volume_spectrum (v606:1063-1073). volume:
+ * [box][box][box] float32.
+ */
+int gisapr_volume_spectrum_blocked(gisapr_ctx ctx, void* stream, const float* volume, int box);
+
+/*
  * Templates of ``n_build`` directions. Replaces the slice gather and the
  * per-orientation tail of IntegratedProjector.build_templates
  * (v606:1075-1147) with ProjectionWhitening (v606:899-992).
@@ -118,7 +129,9 @@ int gisapr_volume_spectrum(gisapr_ctx ctx, void* stream, const float* volume, in
  * row = dirs[i]), mask [box][box] float32 or NULL, fsc [newbox][newbox/2+1]
  * float32 packed FSC, bank [..][newbox][newbox/2+1] complex pre-shifted
  * packed templates. box: power of two, 32..256, or 96 or 192; newbox:
- * even, <= box, multiple of 16.
+ * even, <= box, multiple of 16. spectrum NULL (power-of-two boxes): the
+ * context's blocked spectrum of this box, as gisapr_volume_spectrum_blocked
+ * or the last projector call with a spectrum left it.
  */
 int gisapr_project_templates(gisapr_ctx ctx, void* stream, const float* spectrum, int box,
                              const float* rot, const int* dirs, int n_build, const int* out_slot,

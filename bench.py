@@ -638,6 +638,8 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
         else:
             tuned = Autotuner(trials=1).tune(job, n_cand=args.batch, precision="fp16x3")
             autotune = {"corr_cluster": tuned.corr_cluster, "tc_chunk": tuned.tc_chunk,
+                        "tc_dirs_per_tile": tuned.dirs_per_tile,
+                        "tc_rings": [tuned.tc_a_stages, tuned.tc_b_stages],
                         "correlate_ms": tuned.times_ms, "tune_s": time.perf_counter() - t_tune}
         for precision in args.precisions.split(","):
             batched[precision] = run_batched(job, dens, gen, precision, args.batch, K, W, device, barrier,

@@ -6,6 +6,7 @@ RuntimeError naming the missing file.
 """
 from __future__ import annotations
 
+import contextlib
 import ctypes as C
 import os
 import threading
@@ -36,6 +37,10 @@ SIGNATURES = {
     "gisapr_correlate_batch": [_p, _p, _p, C.c_longlong, _i, _p, _p, _p, _i, _i, _i, _i, _i, _p, _p, _p],
     "gisapr_particle_results_batch": [_p, _p, _p, _p, _p, _i, _i, _i, _p, _p, _p, _p, _p, _p],
     "gisapr_score_sum_batch": [_p, _p, _p, _i, _i, _p],
+    "gisapr_correlate_batch_subset": [_p, _p, _p, C.c_longlong, _i, _p, _p, _p, _i, _i, _i, _i, _i, _p, _p, _p,
+                                      _p],
+    "gisapr_particle_results_subset": [_p, _p, _p, _p, _p, _i, _i, _i, _p, _p, _p, _p, _p, _p, _p],
+    "gisapr_score_sum_subset": [_p, _p, _p, _i, _i, _p, _p],
     "gisapr_tc_bank_bytes": [_i, _i],
     "gisapr_project_launches": [_i, _i],
     "gisapr_set_tuning": [_p, _i, _i, _i],
@@ -107,6 +112,8 @@ def stream_of(device) -> C.c_void_p:
 
 
 TUNE_CORR_CLUSTER = 1  # gisapr_set_tuning keys (include/gisapr_gb300.h)
+TUNE_TC_A_STAGES = 2
+TUNE_TC_B_STAGES = 3
 
 # Process-wide launch-shape settings, (key, size) -> value, applied to every
 # native context at creation (and to this thread's contexts when changed);
@@ -152,6 +159,21 @@ class Context:
             except Exception:
                 pass
             self.handle = None
+
+    @classmethod
+    @contextlib.contextmanager
+    def using(cls, ctx: "Context"):
+        """Make ``ctx`` this thread's context for its device inside the block
+        (a batch runs independent candidates on several contexts, each with
+        its own scratch, on several streams)."""
+        cls.for_device(f"cuda:{ctx.device_index}")  # the thread's own context exists
+        cache = cls._per_thread.ctx
+        prev = cache[ctx.device_index]
+        cache[ctx.device_index] = ctx
+        try:
+            yield ctx
+        finally:
+            cache[ctx.device_index] = prev
 
     @classmethod
     def for_device(cls, device) -> "Context":

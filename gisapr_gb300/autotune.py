@@ -8,7 +8,11 @@ and particle set, and the best value depends on the GPU:
   spectrum in shared memory), 1..8;
 * the candidates per tensor-core launch: a 128-row MMA tile holds
   128 // ceil8(candidates) whole directions, so the chunk size sets how many
-  directions share a tile and how many tiles a particle needs.
+  directions share a tile (the tile shape) and how many tiles a particle
+  needs;
+* the tensor-core kernel's shared-memory ring depths (A: bulk-copied
+  template rows, B: built particle rows): deeper rings hide more copy
+  latency but leave less of the SM's shared memory to its L1 cache.
 
 ``Autotuner.tune`` times the batched correlation stage (CUDA events, best of
 a few runs on the job's own data) for every valid value, keeps the fastest,
@@ -32,6 +36,7 @@ __all__ = ["Autotuner", "TuneResult", "default_cache_path"]
 
 CLUSTER_CHOICES = (1, 2, 3, 4, 5, 6, 8)
 CHUNK_CHOICES = (16, 32, 64, 128)
+RING_CHOICES = ((4, 2), (3, 2), (6, 2), (4, 3))  # (A, B) ring depths; the first is the kernel's default
 SMEM_LIMIT = 227 * 1024
 
 
@@ -58,10 +63,16 @@ class TuneResult:
     corr_cluster: int
     tc_chunk: int
     times_ms: Dict[str, float] = field(default_factory=dict)
+    tc_a_stages: int = 0  # 0: the kernel's default
+    tc_b_stages: int = 0
+    dirs_per_tile: int = 0
 
     def apply(self) -> None:
-        """Make the cluster size the default of every native context at this size."""
+        """Make the cluster size and the ring depths the defaults of every
+        native context at this size."""
         nat.set_default_tuning(nat.TUNE_CORR_CLUSTER, self.size, self.corr_cluster)
+        nat.set_default_tuning(nat.TUNE_TC_A_STAGES, self.size, self.tc_a_stages)
+        nat.set_default_tuning(nat.TUNE_TC_B_STAGES, self.size, self.tc_b_stages)
 
 
 class Autotuner:
@@ -101,9 +112,11 @@ class Autotuner:
         return best
 
     def tune(self, job, n_cand: int = 64, precision: str = "fp16x3", force: bool = False,
-             clusters: Sequence[int] = CLUSTER_CHOICES, chunks: Sequence[int] = CHUNK_CHOICES) -> TuneResult:
+             clusters: Sequence[int] = CLUSTER_CHOICES, chunks: Sequence[int] = CHUNK_CHOICES,
+             rings: Sequence = RING_CHOICES) -> TuneResult:
         """Pick the cluster size (plain path) and, unless precision is
-        "fp32", the tensor-core chunk size for batches of n_cand candidates."""
+        "fp32", the tensor-core chunk size (hence directions per tile) and ring
+        depths for batches of n_cand candidates."""
         from . import synthetic as syn
         key = self.key(job, n_cand) + f"|{precision}"
         cache = self._load()
@@ -133,7 +146,21 @@ class Autotuner:
                 times[f"tc_chunk_{c}"] = t
                 if t < best_ct:
                     best_c, best_ct = c, t
-        r = TuneResult(key=key, size=nb, corr_cluster=best_k, tc_chunk=best_c, times_ms=times)
+        best_ring = (0, 0)
+        if precision != "fp32":
+            best_rt = math.inf
+            for sa, sb in rings:
+                nat.call("gisapr_set_tuning", ctx.handle, nat.TUNE_TC_A_STAGES, nb, sa)
+                nat.call("gisapr_set_tuning", ctx.handle, nat.TUNE_TC_B_STAGES, nb, sb)
+                t = self._time_correlate(job, n_cand, precision, poses, tc_chunk=best_c)
+                times[f"tc_rings_{sa}_{sb}"] = t
+                if t < best_rt:
+                    best_ring, best_rt = (sa, sb), t
+            nat.call("gisapr_set_tuning", ctx.handle, nat.TUNE_TC_A_STAGES, nb, best_ring[0])
+            nat.call("gisapr_set_tuning", ctx.handle, nat.TUNE_TC_B_STAGES, nb, best_ring[1])
+        dpt = 128 // ((min(best_c, 128) + 7) // 8 * 8)
+        r = TuneResult(key=key, size=nb, corr_cluster=best_k, tc_chunk=best_c, times_ms=times,
+                       tc_a_stages=best_ring[0], tc_b_stages=best_ring[1], dirs_per_tile=dpt)
         cache[key] = asdict(r)
         self._save(cache)
         r.apply()

@@ -60,10 +60,10 @@ int correlate_cluster_size(int n);
 size_t correlate_smem_bytes(int n, int n_psi, int crop, int cluster);
 cudaError_t launch_correlate_plain(cudaStream_t, const float2*, const float2*, const int*,
                                    const int*, int, int, int, int, const float2*, const float2*,
-                                   float*, int*, int*, int, long long, int, int);
+                                   float*, int*, int*, int, long long, int, int, const unsigned char*);
 cudaError_t launch_particle_results(cudaStream_t, const int*, const float*, const int*, const int*,
-                                    int, int, int*, int*, float*, int*, int*, float*, int);
-cudaError_t launch_score_sum(cudaStream_t, const int*, const float*, int, double*, int);
+                                    int, int, int*, int*, float*, int*, int*, float*, int, const unsigned char*);
+cudaError_t launch_score_sum(cudaStream_t, const int*, const float*, int, double*, int, const unsigned char*);
 size_t edt_smem_bytes(int box);
 cudaError_t launch_restraint_edt(cudaStream_t, const float*, float, unsigned char*, int*, int*, int);
 cudaError_t launch_restraint_init(cudaStream_t, int*, int);
@@ -77,7 +77,8 @@ cudaError_t launch_ingest_scale_mask(cudaStream_t, double2*, int, int, const dou
 cudaError_t launch_ingest_store(cudaStream_t, const double2*, int, int, double, float*, int);
 int correlate_tc_max_psi();
 int correlate_tc_max_n();
-size_t correlate_tc_smem_bytes(int n, int crop);
+size_t correlate_tc_smem_bytes(int n, int crop, int split, int sa, int sb);
+bool correlate_tc_rings(int n, int crop, int split, int want_sa, int want_sb, int* sa, int* sb);
 long long correlate_tc_bank_halves(int n_slot, int n);
 int correlate_tc_plan(const int*, const int*, int, int, int, int, int*, int);
 cudaError_t launch_bank_to_operands(cudaStream_t, const float2*, long long, int, int, int, int, const float*, void*,
@@ -85,7 +86,7 @@ cudaError_t launch_bank_to_operands(cudaStream_t, const float2*, long long, int,
 int correlate_tc_max_cand();
 cudaError_t launch_correlate_tc(cudaStream_t, const void*, int, const float2*, const int*, const int*, const int*,
                                 int, int, int, int, int, int, int, const float*, const float*, unsigned,
-                                const float2*, const float2*, float*, int*, int*, int*, int);
+                                const float2*, const float2*, float*, int*, int*, int*, int, int, int);
 
 namespace {
 
@@ -150,6 +151,7 @@ struct gisapr_context {
   std::vector<void*> retired;
   int sm_count = 152;
   std::map<int, int> tune_corr_cluster;  // n -> CTAs per particle in the plain correlation
+  std::map<int, int> tune_tc_a, tune_tc_b;  // n -> A / B ring depth of the tensor-core correlation
 };
 
 namespace {
@@ -587,9 +589,10 @@ int gisapr_prepare_particles(gisapr_ctx ctx, void* stream, const float* images, 
   return GISAPR_OK;
 }
 
-int gisapr_correlate_batch(gisapr_ctx ctx, void* stream, const float* bank, long long bank_stride, int n_cand,
-                           const float* stack, const int* local_ptr, const int* local_idx, int n_particles,
-                           int nnz, int n_psi, int n, int crop, float* out_score, int* out_y, int* out_x) {
+int gisapr_correlate_batch_subset(gisapr_ctx ctx, void* stream, const float* bank, long long bank_stride,
+                                  int n_cand, const float* stack, const int* local_ptr, const int* local_idx,
+                                  int n_particles, int nnz, int n_psi, int n, int crop, const unsigned char* subset,
+                                  float* out_score, int* out_y, int* out_x) {
   if (!ctx) return fail(GISAPR_ERR_ARGUMENT, "context is NULL");
   if (n_particles < 0 || n_psi <= 0 || n_cand < 0)
     return fail(GISAPR_ERR_ARGUMENT, "n_particles < 0, n_psi <= 0 or n_cand < 0");
@@ -613,9 +616,16 @@ int gisapr_correlate_batch(gisapr_ctx ctx, void* stream, const float* bank, long
   if (nnz < 0) return fail(GISAPR_ERR_ARGUMENT, "nnz < 0");
   GISAPR_CHECK_CUDA(launch_correlate_plain((cudaStream_t)stream, (const float2*)bank, (const float2*)stack,
                                            local_ptr, local_idx, n_particles, n_psi, n, crop, t.outer, t.col,
-                                           out_score, out_y, out_x, n_cand, bank_stride, nnz, cluster),
+                                           out_score, out_y, out_x, n_cand, bank_stride, nnz, cluster, subset),
                     "correlate");
   return GISAPR_OK;
+}
+
+int gisapr_correlate_batch(gisapr_ctx ctx, void* stream, const float* bank, long long bank_stride, int n_cand,
+                           const float* stack, const int* local_ptr, const int* local_idx, int n_particles,
+                           int nnz, int n_psi, int n, int crop, float* out_score, int* out_y, int* out_x) {
+  return gisapr_correlate_batch_subset(ctx, stream, bank, bank_stride, n_cand, stack, local_ptr, local_idx,
+                                       n_particles, nnz, n_psi, n, crop, nullptr, out_score, out_y, out_x);
 }
 
 int gisapr_correlate(gisapr_ctx ctx, void* stream, const float* bank, const float* stack,
@@ -641,14 +651,31 @@ int gisapr_correlate(gisapr_ctx ctx, void* stream, const float* bank, const floa
   if (rc) return rc;
   GISAPR_CHECK_CUDA(launch_correlate_plain((cudaStream_t)stream, (const float2*)bank, (const float2*)stack,
                                            local_ptr, local_idx, n_particles, n_psi, n, crop, t.outer, t.col,
-                                           out_score, out_y, out_x, 1, 0, 0, cluster),
+                                           out_score, out_y, out_x, 1, 0, 0, cluster, nullptr),
                     "correlate");
   return GISAPR_OK;
+}
+
+static int tuned(const std::map<int, int>& m, int n) {
+  auto it = m.find(n);
+  return it == m.end() ? 0 : it->second;
 }
 
 int gisapr_set_tuning(gisapr_ctx ctx, int key, int size, int value) {
   if (!ctx) return fail(GISAPR_ERR_ARGUMENT, "context is NULL");
   switch (key) {
+    case GISAPR_TUNE_TC_A_STAGES:
+    case GISAPR_TUNE_TC_B_STAGES: {
+      const int hi = key == GISAPR_TUNE_TC_A_STAGES ? 8 : 3;
+      if (value != 0 && (value < 2 || value > hi))
+        return fail(GISAPR_ERR_ARGUMENT, "ring depth must be 0 (default) or 2.." + std::to_string(hi));
+      if (size != 32 && size != 64 && size != 96 && size != 128 && size != 192 && size != 256)
+        return fail(GISAPR_ERR_ARGUMENT, "tensor-core correlation size must be one of 32, 64, 96, 128, 192, 256");
+      auto& m = key == GISAPR_TUNE_TC_A_STAGES ? ctx->tune_tc_a : ctx->tune_tc_b;
+      if (value == 0) m.erase(size);
+      else m[size] = value;
+      return GISAPR_OK;
+    }
     case GISAPR_TUNE_CORR_CLUSTER:
       if (value < 0 || value > 8) return fail(GISAPR_ERR_ARGUMENT, "correlation cluster size must be 0..8");
       if (size < 32 || size > 256 || size % 16 != 0)
@@ -664,11 +691,15 @@ int gisapr_set_tuning(gisapr_ctx ctx, int key, int size, int value) {
 int gisapr_get_tuning(gisapr_ctx ctx, int key, int size, int* value) {
   if (!ctx || !value) return fail(GISAPR_ERR_ARGUMENT, "context or value is NULL");
   switch (key) {
-    case GISAPR_TUNE_CORR_CLUSTER: {
-      auto it = ctx->tune_corr_cluster.find(size);
-      *value = it == ctx->tune_corr_cluster.end() ? 0 : it->second;
+    case GISAPR_TUNE_CORR_CLUSTER:
+      *value = tuned(ctx->tune_corr_cluster, size);
       return GISAPR_OK;
-    }
+    case GISAPR_TUNE_TC_A_STAGES:
+      *value = tuned(ctx->tune_tc_a, size);
+      return GISAPR_OK;
+    case GISAPR_TUNE_TC_B_STAGES:
+      *value = tuned(ctx->tune_tc_b, size);
+      return GISAPR_OK;
     default:
       return fail(GISAPR_ERR_ARGUMENT, "unknown tuning key " + std::to_string(key));
   }
@@ -740,7 +771,8 @@ int gisapr_correlate_tc_batch_ex(gisapr_ctx ctx, void* stream, const float* bank
   const int grid = std::min(n_work, ctx->sm_count);
   GISAPR_CHECK_CUDA(launch_correlate_tc(st, tbank, n_cand, (const float2*)stack, local_ptr, local_idx, work, n_work,
                                         n_psi, n, crop, nnz, split, bf16, col_scale_t, col_scale_p, wait_limit,
-                                        t.row, t.col, out_score, out_y, out_x, status, grid),
+                                        t.row, t.col, out_score, out_y, out_x, status, grid,
+                                        tuned(ctx->tune_tc_a, n), tuned(ctx->tune_tc_b, n)),
                     "correlate_tc");
   return GISAPR_OK;
 }
@@ -755,9 +787,10 @@ int gisapr_correlate_tc_batch(gisapr_ctx ctx, void* stream, const float* bank, l
                                       out_x, status);
 }
 
-int gisapr_particle_results_batch(void* stream, const int* local_ptr, const float* score, const int* ys,
-                                  const int* xs, int n_particles, int n_psi, int n_cand, int* best_entry,
-                                  int* best_psi, float* peak, int* peak_y, int* peak_x, float* zscore) {
+int gisapr_particle_results_subset(void* stream, const int* local_ptr, const float* score, const int* ys,
+                                   const int* xs, int n_particles, int n_psi, int n_cand,
+                                   const unsigned char* subset, int* best_entry, int* best_psi, float* peak,
+                                   int* peak_y, int* peak_x, float* zscore) {
   if (n_particles < 0 || n_psi <= 0 || n_cand < 0)
     return fail(GISAPR_ERR_ARGUMENT, "n_particles < 0, n_psi <= 0 or n_cand < 0");
   if (n_particles == 0 || n_cand == 0) return GISAPR_OK;
@@ -766,9 +799,16 @@ int gisapr_particle_results_batch(void* stream, const int* local_ptr, const floa
     return fail(GISAPR_ERR_ARGUMENT, "a required pointer is NULL");
   if (n_cand > 65535) return fail(GISAPR_ERR_ARGUMENT, "at most 65535 candidates per call");
   GISAPR_CHECK_CUDA(launch_particle_results((cudaStream_t)stream, local_ptr, score, ys, xs, n_particles, n_psi,
-                                            best_entry, best_psi, peak, peak_y, peak_x, zscore, n_cand),
+                                            best_entry, best_psi, peak, peak_y, peak_x, zscore, n_cand, subset),
                     "particle_results");
   return GISAPR_OK;
+}
+
+int gisapr_particle_results_batch(void* stream, const int* local_ptr, const float* score, const int* ys,
+                                  const int* xs, int n_particles, int n_psi, int n_cand, int* best_entry,
+                                  int* best_psi, float* peak, int* peak_y, int* peak_x, float* zscore) {
+  return gisapr_particle_results_subset(stream, local_ptr, score, ys, xs, n_particles, n_psi, n_cand, nullptr,
+                                        best_entry, best_psi, peak, peak_y, peak_x, zscore);
 }
 
 int gisapr_particle_results(void* stream, const int* local_ptr, const float* score, const int* ys,
@@ -778,13 +818,18 @@ int gisapr_particle_results(void* stream, const int* local_ptr, const float* sco
                                        best_psi, peak, peak_y, peak_x, zscore);
 }
 
-int gisapr_score_sum_batch(void* stream, const int* local_ptr, const float* peak, int n_particles, int n_cand,
-                           double* out) {
+int gisapr_score_sum_subset(void* stream, const int* local_ptr, const float* peak, int n_particles, int n_cand,
+                            const unsigned char* subset, double* out) {
   if (n_particles < 0 || n_cand < 0 || !out) return fail(GISAPR_ERR_ARGUMENT, "bad arguments");
   if (n_particles > 0 && (!local_ptr || !peak)) return fail(GISAPR_ERR_ARGUMENT, "a required pointer is NULL");
-  GISAPR_CHECK_CUDA(launch_score_sum((cudaStream_t)stream, local_ptr, peak, n_particles, out, n_cand),
+  GISAPR_CHECK_CUDA(launch_score_sum((cudaStream_t)stream, local_ptr, peak, n_particles, out, n_cand, subset),
                     "score_sum");
   return GISAPR_OK;
+}
+
+int gisapr_score_sum_batch(void* stream, const int* local_ptr, const float* peak, int n_particles, int n_cand,
+                           double* out) {
+  return gisapr_score_sum_subset(stream, local_ptr, peak, n_particles, n_cand, nullptr, out);
 }
 
 int gisapr_score_sum(void* stream, const int* local_ptr, const float* peak, int n_particles, double* out) {

@@ -43,6 +43,7 @@ struct CorrParams {
   int n_cand;              // candidates sharing the particle spectra
   long long bank_stride;   // complex elements between candidates' banks
   int nnz;                 // entries of the CSR (output stride per candidate)
+  const unsigned char* subset;  // [n_cand][n_particles] nonzero: the candidate scores the particle (null: all)
 };
 
 // 8-byte asynchronous global-to-shared copy with an L2 evict-first hint:
@@ -81,6 +82,11 @@ __global__ void __launch_bounds__(kThreads) correlate_plain(CorrParams P) {
 
   const int e0 = P.local_ptr[b], d = P.local_ptr[b + 1] - e0;
   if (d <= 0) return;  // whole cluster returns together (same b)
+  if (P.subset != nullptr) {  // a particle no candidate scores: nothing to do (same b for the cluster)
+    bool any = false;
+    for (int c = 0; c < P.n_cand && !any; ++c) any = P.subset[(size_t)c * P.n_particles + b] != 0;
+    if (!any) return;
+  }
 
   for (int t = threadIdx.x; t < M * C; t += blockDim.x) s_two[t] = P.tw_outer[t];
   for (int t = threadIdx.x; t < cw * C; t += blockDim.x) s_twc[t] = P.tw_col[(size_t)clo * C + t];
@@ -98,6 +104,7 @@ __global__ void __launch_bounds__(kThreads) correlate_plain(CorrParams P) {
   __syncthreads();
 
   for (int cand = 0; cand < P.n_cand; ++cand) {
+  if (P.subset != nullptr && P.subset[(size_t)cand * P.n_particles + b] == 0) continue;  // cluster-uniform
   const float2* bank = P.bank + (size_t)cand * (size_t)P.bank_stride;
   const size_t out_base = (size_t)cand * P.nnz * n_psi;
   for (int sg = 0; sg < d; sg += kMaxLocal) {
@@ -193,10 +200,12 @@ __global__ void __launch_bounds__(kThreads) correlate_plain(CorrParams P) {
 
 // One warp per particle: first maximum over (local direction, psi), the
 // population mean and sigma of all its scores (FP64 sums), and the z-score.
+// A particle the candidate does not score (subset) gets the record of a
+// particle without directions.
 __global__ void particle_results(const int* __restrict__ local_ptr, const float* __restrict__ score,
                                  const int* __restrict__ ys, const int* __restrict__ xs, int n_particles,
-                                 int n_psi, int* __restrict__ best_entry, int* __restrict__ best_psi,
-                                 float* __restrict__ peak, int* __restrict__ peak_y,
+                                 int n_psi, const unsigned char* __restrict__ subset, int* __restrict__ best_entry,
+                                 int* __restrict__ best_psi, float* __restrict__ peak, int* __restrict__ peak_y,
                                  int* __restrict__ peak_x, float* __restrict__ zscore) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= n_particles) return;
@@ -206,7 +215,8 @@ __global__ void particle_results(const int* __restrict__ local_ptr, const float*
     score += so; ys += so; xs += so;
     best_entry += po; best_psi += po; peak += po; peak_y += po; peak_x += po; zscore += po;
   }
-  const int e0 = local_ptr[warp], cnt = (local_ptr[warp + 1] - e0) * n_psi;
+  const bool scored = subset == nullptr || subset[(size_t)blockIdx.y * n_particles + warp] != 0;
+  const int e0 = local_ptr[warp], cnt = scored ? (local_ptr[warp + 1] - e0) * n_psi : 0;
   if (cnt <= 0) {
     if (lane == 0) {
       best_entry[warp] = -1; best_psi[warp] = -1; peak[warp] = 0.f;
@@ -255,17 +265,20 @@ __global__ void particle_results(const int* __restrict__ local_ptr, const float*
 constexpr int kScoreCtas = 8;
 
 __global__ void __launch_bounds__(256) score_sum(const int* __restrict__ local_ptr, const float* __restrict__ peak,
-                                                 int n_particles, double* __restrict__ out) {
+                                                 int n_particles, const unsigned char* __restrict__ subset,
+                                                 double* __restrict__ out) {
   __shared__ double red[32];
   __shared__ double part;
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank(), cand = blockIdx.x / kScoreCtas;
   peak += (size_t)cand * n_particles;
+  if (subset != nullptr) subset += (size_t)cand * n_particles;
   const int per = (n_particles + kScoreCtas - 1) / kScoreCtas;
   const int p0 = rank * per, p1 = min(n_particles, p0 + per);
   double acc = 0.0;
   for (int p = p0 + threadIdx.x; p < p1; p += blockDim.x)
-    if (local_ptr[p + 1] > local_ptr[p]) acc += exp((double)peak[p] / 1024.0);
+    if (local_ptr[p + 1] > local_ptr[p] && (subset == nullptr || subset[p] != 0))
+      acc += exp((double)peak[p] / 1024.0);
   acc = block_sum_d(acc, red);
   if (threadIdx.x == 0) part = acc;
   cluster.sync();
@@ -324,10 +337,11 @@ cudaError_t launch_correlate_plain(cudaStream_t st, const float2* bank, const fl
                                    const int* local_ptr, const int* local_idx, int n_particles,
                                    int n_psi, int n, int crop, const float2* tw_outer,
                                    const float2* tw_col, float* out_score, int* out_y, int* out_x,
-                                   int n_cand, long long bank_stride, int nnz, int cluster) {
+                                   int n_cand, long long bank_stride, int nnz, int cluster,
+                                   const unsigned char* subset) {
   if (n_particles <= 0 || n_cand <= 0) return cudaSuccess;
   CorrParams P;
-  P.n_cand = n_cand; P.bank_stride = bank_stride; P.nnz = nnz;
+  P.n_cand = n_cand; P.bank_stride = bank_stride; P.nnz = nnz; P.subset = subset;
   P.bank = bank; P.stack = stack; P.local_ptr = local_ptr; P.local_idx = local_idx;
   P.tw_outer = tw_outer; P.tw_col = tw_col; P.out_score = out_score; P.out_y = out_y;
   P.out_x = out_x; P.n_particles = n_particles; P.n_psi = n_psi; P.n = n;
@@ -349,16 +363,16 @@ cudaError_t launch_correlate_plain(cudaStream_t st, const float2* bank, const fl
 cudaError_t launch_particle_results(cudaStream_t st, const int* local_ptr, const float* score,
                                     const int* ys, const int* xs, int n_particles, int n_psi,
                                     int* best_entry, int* best_psi, float* peak, int* peak_y,
-                                    int* peak_x, float* zscore, int n_cand) {
+                                    int* peak_x, float* zscore, int n_cand, const unsigned char* subset) {
   if (n_particles <= 0 || n_cand <= 0) return cudaSuccess;
   const int threads = 256, warps = threads / 32;
   particle_results<<<dim3((n_particles + warps - 1) / warps, n_cand), threads, 0, st>>>(
-      local_ptr, score, ys, xs, n_particles, n_psi, best_entry, best_psi, peak, peak_y, peak_x, zscore);
+      local_ptr, score, ys, xs, n_particles, n_psi, subset, best_entry, best_psi, peak, peak_y, peak_x, zscore);
   return cudaGetLastError();
 }
 
 cudaError_t launch_score_sum(cudaStream_t st, const int* local_ptr, const float* peak, int n_particles,
-                             double* out, int n_cand) {
+                             double* out, int n_cand, const unsigned char* subset) {
   if (n_cand <= 0) return cudaSuccess;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(n_cand * kScoreCtas));
@@ -371,5 +385,5 @@ cudaError_t launch_score_sum(cudaStream_t st, const int* local_ptr, const float*
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, score_sum, local_ptr, peak, n_particles, out);
+  return cudaLaunchKernelEx(&cfg, score_sum, local_ptr, peak, n_particles, subset, out);
 }

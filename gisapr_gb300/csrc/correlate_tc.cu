@@ -29,11 +29,12 @@
 //
 // Warp roles (640 threads, 20 warps): warp 0 issues the MMAs (one lane),
 // warp 1 the bulk async copies (cp.async.bulk, mbarrier complete_tx) of the
-// rows' template chunks two steps ahead into a ring of shared-memory stages
-// (the operand bank is laid out [slot][col][step][part][cand][128 B], so
-// each direction's rows of a step are one contiguous copy), warps 2-7 build
-// B for each K step from the particle column (prefetched with cp.async two
-// columns ahead) and a twiddle recurrence, and warps 8-19 run stage 2: each
+// rows' template chunks into the A ring of shared-memory stages (the operand
+// bank is laid out [slot][col][step][part][cand][128 B], so each
+// direction's rows of a step are one contiguous copy; the rows of the column
+// two ahead are prefetched into L2), warps 2-7 build B for each K step into
+// the B ring from the particle column (prefetched with cp.async two columns
+// ahead) and a twiddle recurrence, and warps 8-19 run stage 2: each
 // thread owns one (row, psi) map, reads the finished column accumulator from
 // TMEM (tcgen05.ld) and accumulates its crop rows, some in registers and the
 // rest in free TMEM columns. Two TMEM accumulators let the MMAs of a column
@@ -65,8 +66,11 @@ constexpr int kTcMaxN = 256;      // K = 2n <= 512, in steps of 64 (32 rows r)
 // psi angles per tile: three up to crop 12; at crop 14 two, so that the MMA
 // accumulators and the stage-2 rows kept in TMEM fit its 512 columns.
 __host__ __device__ constexpr int tc_psi_group(int C) { return C <= 12 ? 3 : 2; }
-// shared-memory stages: four, three above n = 128 (larger particle columns and tables)
-__host__ __device__ constexpr int tc_stages(int N) { return N > 128 ? 3 : 4; }
+// Shared-memory rings: A stages (the bulk-copied template rows of a K step)
+// and B stages (the built particle rows) are separate, so the copies can run
+// further ahead than the B build; their depths are launch parameters.
+constexpr int kTcMaxSA = 8, kTcMaxSB = 3;
+constexpr size_t kTcSmemMax = 232448;  // dynamic shared memory of one CTA (227 KB)
 constexpr int kTcMaxCand = 128;   // candidates per launch
 constexpr int kTcTmemCols = 512;
 constexpr float kTcScale = 8192.0f;       // 2^13 on each operand (times the column scale)
@@ -94,6 +98,7 @@ struct TcParams {
   const float* t_scale;   // [H] per-column template scale (power of two) or null
   const float* p_scale;   // [H] per-column particle scale (power of two) or null
   unsigned wait_limit;    // bound of a hand-off wait (iterations)
+  int sa, sb;             // A and B ring depths
   float* out_score;       // [n_cand][nnz][n_psi]
   int* out_y;
   int* out_x;
@@ -410,28 +415,31 @@ __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
   static_assert(tc_psi_group(C) * tc_psi_stride(C) <= tc_n(C), "psi rows of the accumulator");
   constexpr int kN = tc_n(C);
   constexpr int kPS = tc_psi_stride(C);
-  constexpr int S = tc_stages(N);
   constexpr int NQ = N / 32;               // K steps per column: 32 rows r (64 K) each
   constexpr int n = N, H = N / 2 + 1;
   constexpr int TWE = tc_tw_entries(C);
-  constexpr uint32_t a_part = kTcM * 128;  // bytes of A (hi or lo) per stage: 128 rows x 128 B
-  constexpr uint32_t b_part = kN * 128;
-  constexpr uint32_t stage_bytes = 2 * a_part + 2 * b_part;
-  static_assert(stage_bytes % 1024 == 0, "stages keep the 1024-byte swizzle alignment");
+  constexpr uint32_t a_part = kTcM * 128;  // bytes of A (hi or lo) per step: 128 rows x 128 B
+  constexpr uint32_t b_part = kN * 128;    // bytes of B (hi or lo) per step
+  static_assert(a_part % 1024 == 0 && b_part % 1024 == 0, "stages keep the 1024-byte swizzle alignment");
+  const int parts = P.split ? 2 : 1;
+  const int SA = P.sa, SB = P.sb;
+  const uint32_t a_bytes = parts * a_part, b_bytes = parts * b_part;
   const int n_cand = P.n_cand;
   const int nc8 = (n_cand + 7) & ~7;       // rows per direction in a tile
-  unsigned char* stages = smem_raw;        // [S][A hi, A lo, B hi, B lo]
-  float2* s_p = reinterpret_cast<float2*>(smem_raw + S * stage_bytes);  // [3][kTcPsi][n] particle columns
+  unsigned char* ring_a = smem_raw;                  // [SA][part][128 rows][128 B]
+  unsigned char* ring_b = smem_raw + SA * a_bytes;   // [SB][part][kN rows][128 B]
+  float2* s_p = reinterpret_cast<float2*>(ring_b + SB * b_bytes);  // [3][kTcPsi][n] particle columns
   float2* s_twr = s_p + 3 * kTcPsi * n;                        // [n]
   float* s_twall = reinterpret_cast<float*>(s_twr + n);      // [H][TWE] column tables
   float* s_psc = s_twall + H * TWE;                           // [H] particle-side scale per column
   uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_psc + ((H + 1) & ~1));
-  uint64_t* bar_afull = s_bar;           // [S] A bytes landed (copy warp's expect_tx)
-  uint64_t* bar_bfull = s_bar + S;       // [S] every builder warp wrote B
-  uint64_t* bar_empty = s_bar + 2 * S;   // [S] the MMAs reading the stage are done
-  uint64_t* bar_tfull = s_bar + 3 * S;   // [2] a column's accumulator is final
-  uint64_t* bar_tempty = s_bar + 3 * S + 2;  // [2] every stage-2 warp read its accumulator
-  uint32_t* s_taddr = reinterpret_cast<uint32_t*>(s_bar + 3 * S + 4);
+  uint64_t* bar_afull = s_bar;                    // [SA] A bytes landed (copy warp's expect_tx)
+  uint64_t* bar_aempty = s_bar + kTcMaxSA;        // [SA] the MMAs reading the A stage are done
+  uint64_t* bar_bfull = s_bar + 2 * kTcMaxSA;     // [SB] every builder warp wrote B
+  uint64_t* bar_bempty = bar_bfull + kTcMaxSB;    // [SB] the MMAs reading the B stage are done
+  uint64_t* bar_tfull = bar_bempty + kTcMaxSB;    // [2] a column's accumulator is final
+  uint64_t* bar_tempty = bar_tfull + 2;           // [2] every stage-2 warp read its accumulator
+  uint32_t* s_taddr = reinterpret_cast<uint32_t*>(bar_tempty + 2);
   int* s_fail = reinterpret_cast<int*>(s_taddr + 1);
   uint32_t* s_mma_steps = reinterpret_cast<uint32_t*>(s_fail + 1);   // K steps whose MMAs were committed
   uint32_t* s_copy_steps = s_mma_steps + 1;                           // K steps whose A copies were issued
@@ -444,13 +452,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
     s_twall[t] = tw_entry<C>(P.tw_col, c, t % TWE, 1.0f / (kTcScale * kTcScale * ts * ps));
   }
   for (int t = tid; t < H; t += blockDim.x) s_psc[t] = kTcScale * (P.p_scale ? P.p_scale[t] : 1.0f);
-  for (uint32_t t = tid; t < S * stage_bytes / 16; t += blockDim.x)
-    reinterpret_cast<uint4*>(stages)[t] = make_uint4(0, 0, 0, 0);
+  for (uint32_t t = tid; t < (SA * a_bytes + SB * b_bytes) / 16; t += blockDim.x)
+    reinterpret_cast<uint4*>(smem_raw)[t] = make_uint4(0, 0, 0, 0);
   if (tid == 0) {
-    for (int i = 0; i < S; ++i) {
+    for (int i = 0; i < SA; ++i) {
       mbar_init(bar_afull + i, 1);
+      mbar_init(bar_aempty + i, 1);
+    }
+    for (int i = 0; i < SB; ++i) {
       mbar_init(bar_bfull + i, kTcBuildWarps);
-      mbar_init(bar_empty + i, 1);
+      mbar_init(bar_bempty + i, 1);
     }
     for (int i = 0; i < 2; ++i) {
       mbar_init(bar_tfull + i, 1);
@@ -481,81 +492,98 @@ __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
     return r;
   };
 
+  // Ring positions: every role walks the same K steps g = 0, 1, ...; step g
+  // uses A stage g % SA and B stage g % SB, in use number g / SA (g / SB).
+  // Consumers wait for the full barrier's phase (use & 1); producers of a
+  // stage's next use wait for the empty barrier's previous phase.
   if (warp == 0) {
     // ---------------- MMA issue (one lane)
     if (lane == 0) {
-      uint32_t g = 0, tuse[2] = {0, 0};
+      uint32_t g = 0, tuse[2] = {0, 0}, pa = 0, pb = 0;
+      int ia = 0, ib = 0;
       const uint32_t idesc = make_idesc(kTcM, kN, BF ? 1 : 0);
       bool ok = true;
       for (int wi = blockIdx.x; wi < P.n_work && ok; wi += gridDim.x) {
         for (int col = 0; col < H && ok; ++col) {
           const int tb = col & 1;
           for (int qq = 0; qq < NQ && ok; ++qq, ++g) {
-            const uint32_t st = g % S;
             if (qq == 0 && tuse[tb] > 0) ok = wait(bar_tempty + tb, (tuse[tb] - 1) & 1u);
-            ok = ok && wait(bar_bfull + st, (g / S) & 1u) && wait(bar_afull + st, (g / S) & 1u);
+            ok = ok && wait(bar_bfull + ib, pb) && wait(bar_afull + ia, pa);
             if (!ok) break;
             asm volatile("tcgen05.fence::after_thread_sync;");
-            const uint32_t a0s = smem_u32(stages + st * stage_bytes);
-            issue_mma_step(taddr + (uint32_t)(tb * kN), a0s, a0s + 2 * a_part, a_part, b_part, idesc,
-                           P.split ? 3 : 1, qq > 0);
-            mma_commit(bar_empty + st);
+            const uint32_t a0s = smem_u32(ring_a + ia * a_bytes), b0s = smem_u32(ring_b + ib * b_bytes);
+            issue_mma_step(taddr + (uint32_t)(tb * kN), a0s, b0s, a_part, b_part, idesc, P.split ? 3 : 1, qq > 0);
+            mma_commit(bar_aempty + ia);
+            mma_commit(bar_bempty + ib);
             *s_mma_steps = g + 1;
             if (qq == NQ - 1) {
               mma_commit(bar_tfull + tb);
               ++tuse[tb];
             }
+            if (++ia == SA) { ia = 0; pa ^= 1u; }
+            if (++ib == SB) { ib = 0; pb ^= 1u; }
           }
         }
       }
     }
   } else if (warp == 1) {
-    // ---------------- A: one bulk copy of n_cand 128-byte rows per (part, direction) and step
-    const int parts = P.split ? 2 : 1;
+    // ---------------- A: one bulk copy of n_cand 128-byte rows per (part, direction) and step,
+    // and an L2 prefetch of each direction's rows two columns ahead
     const uint32_t bytes = (uint32_t)n_cand * 128;
-    uint32_t g = 0;
-    int zeroed[S];  // rows [zeroed[s], 128) of stage s read as zero
+    uint32_t g = 0, pa = 0;
+    int ia = 0;
+    int zeroed[kTcMaxSA];  // rows [zeroed[s], 128) of A stage s read as zero
 #pragma unroll
-    for (int s = 0; s < S; ++s) zeroed[s] = 0;
+    for (int s = 0; s < kTcMaxSA; ++s) zeroed[s] = 0;
     bool ok = true;
     for (int wi = blockIdx.x; wi < P.n_work && ok; wi += gridDim.x) {
       const TcItem it = tc_item(P, wi, n, H, tc_psi_group(C));
       const int used = it.nd * nc8;
       int slot = 0;
       if (lane < parts * it.nd) slot = P.local_idx[it.e0 + it.a0 + lane % it.nd];
+      const unsigned char* bank = static_cast<const unsigned char*>(P.tbank);
       for (int col = 0; col < H && ok; ++col) {
+        if (col + 2 < H) {
+          // the parts of every (direction, K step) of column col + 2
+          for (int t = lane; t < it.nd * NQ; t += 32) {
+            const int d = t / NQ, q = t - d * NQ;
+            const int sl = P.local_idx[it.e0 + it.a0 + d];
+            const unsigned char* src = bank + ((((size_t)sl * H + col + 2) * NQ + q) * 2) * (size_t)bytes;
+            asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(parts * bytes) : "memory");
+          }
+        }
         for (int qq = 0; qq < NQ && ok; ++qq, ++g) {
-          const uint32_t st = g % S;
-          unsigned char* stA = stages + st * stage_bytes;
-          if (g >= (uint32_t)S) {
+          unsigned char* stA = ring_a + ia * a_bytes;
+          if (g >= (uint32_t)SA) {
             bool w = true;
-            if (lane == 0) w = wait(bar_empty + st, (g / S - 1) & 1u);
+            if (lane == 0) w = wait(bar_aempty + ia, pa ^ 1u);
             ok = __shfl_sync(0xffffffffu, w ? 1 : 0, 0) != 0;
             if (!ok) break;
           }
 #pragma unroll
-          for (int s = 0; s < S; ++s) {
-            if (s == (int)st && used < zeroed[s]) {
+          for (int s = 0; s < kTcMaxSA; ++s) {
+            if (s == ia && used < zeroed[s]) {
               // rows this tile leaves empty must read as zero
-              for (int t = lane; t < 2 * (zeroed[s] - used) * 8; t += 32) {
-                const int row = used + (t >> 3) % (zeroed[s] - used), part = (t >> 3) / (zeroed[s] - used);
+              const int span = zeroed[s] - used;
+              for (int t = lane; t < parts * span * 8; t += 32) {
+                const int row = used + (t >> 3) % span, part = (t >> 3) / span;
                 *reinterpret_cast<uint4*>(stA + part * a_part + row * 128 + (t & 7) * 16) =
                     make_uint4(0, 0, 0, 0);
               }
               asm volatile("fence.proxy.async.shared::cta;");
               __syncwarp();
             }
-            if (s == (int)st) zeroed[s] = used;
+            if (s == ia) zeroed[s] = used;
           }
-          if (lane == 0) mbar_expect_tx(bar_afull + st, (uint32_t)(parts * it.nd) * bytes);
+          if (lane == 0) mbar_expect_tx(bar_afull + ia, (uint32_t)(parts * it.nd) * bytes);
           __syncwarp();
           if (lane < parts * it.nd) {
             const int part = lane / it.nd, dl = lane - part * it.nd;
-            const unsigned char* src = static_cast<const unsigned char*>(P.tbank) +
-                                       ((((size_t)slot * H + col) * NQ + qq) * 2 + part) * (size_t)n_cand * 128;
-            bulk_copy(stA + part * a_part + (uint32_t)dl * nc8 * 128, src, bytes, bar_afull + st);
+            const unsigned char* src = bank + ((((size_t)slot * H + col) * NQ + qq) * 2 + part) * (size_t)bytes;
+            bulk_copy(stA + part * a_part + (uint32_t)dl * nc8 * 128, src, bytes, bar_afull + ia);
           }
           if (lane == 0) *s_copy_steps = g + 1;
+          if (++ia == SA) { ia = 0; pa ^= 1u; }
         }
       }
     }
@@ -564,7 +592,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
     // The builder warps always run the same sequence of named barriers (no
     // early exit): after a failure they only skip the work.
     const int bt = tid - 32 * kTcBuildWarp0;
-    uint32_t g = 0;
+    uint32_t g = 0, pb = 0;
+    int ib = 0;
     bool ok = true;
     for (int wi = blockIdx.x; wi < P.n_work; wi += gridDim.x) {
       const TcItem it = tc_item(P, wi, n, H, tc_psi_group(C));
@@ -591,13 +620,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
         const float2* sp = s_p + (col % 3) * kTcPsi * n;
         const float scale = s_psc[col];
         for (int qq = 0; qq < NQ; ++qq, ++g) {
-          const uint32_t st = g % S;
-          unsigned char* stB = stages + st * stage_bytes + 2 * a_part;
-          if (g >= (uint32_t)S) ok = wait(bar_empty + st, (g / S - 1) & 1u) && ok;
+          unsigned char* stB = ring_b + ib * b_bytes;
+          if (g >= (uint32_t)SB) ok = wait(bar_bempty + ib, pb ^ 1u) && ok;
           if (ok) build_b_step<C, N, BF>(stB, b_part, sp, s_twr, scale, qq, g_psi, P.split != 0, bt);
           asm volatile("fence.proxy.async.shared::cta;");
           __syncwarp();
-          if (lane == 0) mbar_arrive(bar_bfull + st);
+          if (lane == 0) mbar_arrive(bar_bfull + ib);
+          if (++ib == SB) { ib = 0; pb ^= 1u; }
         }
       }
       asm volatile("cp.async.wait_all;" ::: "memory");
@@ -711,16 +740,17 @@ __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
   // Every role has left its loop. After a failure, the bulk copies and the
   // MMAs this CTA issued get a last bounded chance (the default bound) to
   // finish before the CTA frees its TMEM and exits: the latest use of each
-  // stage is among the last S steps issued.
+  // A stage is among the last SA steps issued (every MMA commit also covers
+  // the MMAs before it, so the A ring's barriers cover the B ring's readers).
   __syncthreads();
   if (*reinterpret_cast<volatile int*>(s_fail) != 0) {
     if (tid == 0) {
       if (P.status != nullptr) atomicExch(P.status, 1);
-      const uint32_t gm = *s_mma_steps, ga = *s_copy_steps;
-      for (uint32_t g = gm > (uint32_t)S ? gm - S : 0; g < gm; ++g)
-        mbar_wait(bar_empty + g % S, (g / S) & 1u, kWaitLimit);
-      for (uint32_t g = ga > (uint32_t)S ? ga - S : 0; g < ga; ++g)
-        mbar_wait(bar_afull + g % S, (g / S) & 1u, kWaitLimit);
+      const uint32_t gm = *s_mma_steps, ga = *s_copy_steps, sa = (uint32_t)SA;
+      for (uint32_t g = gm > sa ? gm - sa : 0; g < gm; ++g)
+        mbar_wait(bar_aempty + g % sa, (g / sa) & 1u, kWaitLimit);
+      for (uint32_t g = ga > sa ? ga - sa : 0; g < ga; ++g)
+        mbar_wait(bar_afull + g % sa, (g / sa) & 1u, kWaitLimit);
     }
     __syncthreads();
   }
@@ -826,12 +856,36 @@ int correlate_tc_max_n() { return kTcMaxN; }
 int correlate_tc_max_cand() { return kTcMaxCand; }
 unsigned correlate_tc_default_wait() { return kWaitLimit; }
 
-size_t correlate_tc_smem_bytes(int n, int crop) {
-  const size_t stage = 2 * (size_t)kTcM * 128 + 2 * (size_t)tc_n(crop) * 128;
+// Shared memory after the rings: particle columns, tables, barriers, TMEM
+// address and status words.
+static size_t tc_tail_bytes(int n, int crop) {
   const int H = n / 2 + 1;
-  return tc_stages(n) * stage + 3 * (size_t)kTcPsi * n * sizeof(float2) + (size_t)n * sizeof(float2) +
+  return 3 * (size_t)kTcPsi * n * sizeof(float2) + (size_t)n * sizeof(float2) +
          (size_t)H * tc_tw_entries(crop) * sizeof(float) + (size_t)((H + 1) & ~1) * sizeof(float) +
-         (3 * tc_stages(n) + 4) * 8 + 16;
+         (2 * kTcMaxSA + 2 * kTcMaxSB + 4) * 8 + 16;
+}
+static size_t tc_a_bytes(int split) { return (split ? 2 : 1) * (size_t)kTcM * 128; }
+static size_t tc_b_bytes(int crop, int split) { return (split ? 2 : 1) * (size_t)tc_n(crop) * 128; }
+
+// Ring depths of a launch: the requested ones (0: the default, A four deep
+// and B two deep) within their limits, A reduced to what the shared memory
+// holds. Deeper A rings did not help on GB300: the shared memory they take
+// comes out of the L1 cache that holds the particle rows the B build
+// gathers (at box 128 a particle's three psi rows are 48 KB of lines).
+// Returns false when not even two A stages fit.
+bool correlate_tc_rings(int n, int crop, int split, int want_sa, int want_sb, int* sa, int* sb) {
+  const long long avail = (long long)kTcSmemMax - (long long)tc_tail_bytes(n, crop);
+  const long long a = (long long)tc_a_bytes(split), b = (long long)tc_b_bytes(crop, split);
+  const int B = want_sb > 0 ? std::min(want_sb, kTcMaxSB) : 2;
+  const int A = (int)std::min<long long>(want_sa > 0 ? std::min(want_sa, kTcMaxSA) : 4, (avail - B * b) / a);
+  if (A < 2) return false;
+  *sa = A;
+  *sb = B;
+  return true;
+}
+
+size_t correlate_tc_smem_bytes(int n, int crop, int split, int sa, int sb) {
+  return sa * tc_a_bytes(split) + sb * tc_b_bytes(crop, split) + tc_tail_bytes(n, crop);
 }
 
 // bytes of the operand copy of one candidate's bank: hi and lo halves
@@ -903,9 +957,11 @@ cudaError_t launch_correlate_tc(cudaStream_t st, const void* tbank, int n_cand, 
                                 int n, int crop, int nnz, int split, int bf16, const float* t_scale,
                                 const float* p_scale, unsigned wait_limit, const float2* tw_row,
                                 const float2* tw_col, float* out_score, int* out_y, int* out_x, int* status,
-                                int grid) {
+                                int grid, int want_sa, int want_sb) {
   if (n_work <= 0 || n_cand <= 0) return cudaSuccess;
   if (n_cand > kTcMaxCand) return cudaErrorInvalidValue;
+  int sa = 0, sb = 0;
+  if (!correlate_tc_rings(n, crop, split, want_sa, want_sb, &sa, &sb)) return cudaErrorInvalidValue;
   TcParams P;
   P.tbank = tbank;
   P.stack = stack;
@@ -929,7 +985,9 @@ cudaError_t launch_correlate_tc(cudaStream_t st, const void* tbank, int n_cand, 
   P.out_y = out_y;
   P.out_x = out_x;
   P.status = status;
-  const size_t smem = correlate_tc_smem_bytes(n, crop);
+  P.sa = sa;
+  P.sb = sb;
+  const size_t smem = correlate_tc_smem_bytes(n, crop, split, sa, sb);
   switch (crop) {
     case 2: return launch_tc_c<2>(P, smem, grid, st);
     case 4: return launch_tc_c<4>(P, smem, grid, st);

@@ -372,11 +372,13 @@ class ScoringJob:
 
     def format_results(self, r: Dict[str, np.ndarray]) -> List[List[object]]:
         """Text records from per-particle arrays (best_entry, best_psi, peak,
-        peak_y, peak_x, zscore), in particle order."""
+        peak_y, peak_x, zscore), in particle order; particles without
+        directions, or left out of a batch slot's subset (best_entry -1),
+        have no record."""
         rows = []
         ptr = self.local_ptr.cpu().numpy()
         for i, rec in enumerate(self.records):
-            if ptr[i + 1] <= ptr[i]:
+            if ptr[i + 1] <= ptr[i] or r["best_entry"][i] < 0:
                 continue
             fake, _ = self.psi_meta[i]
             local_index = int(r["best_entry"][i] - ptr[i])
@@ -395,6 +397,39 @@ def idx_ptr(a: np.ndarray) -> C.c_void_p:
     return C.c_void_p(a.ctypes.data)
 
 
+def subset_mask(subsets, n_cand: int, n_particles: int) -> np.ndarray:
+    """The [n_cand][n_particles] uint8 mask of per-slot particle subsets.
+
+    ``subsets``: None (every slot scores every particle) or one entry per
+    slot (at most n_cand; missing slots score every particle), each None
+    (all particles), a sequence of particle indices, or a boolean mask of
+    length n_particles. Raises ValueError for an index out of range, a
+    repeated index, or a mask of the wrong length."""
+    mask = np.ones((n_cand, n_particles), dtype=np.uint8)
+    if subsets is None:
+        return mask
+    subsets = list(subsets)
+    if len(subsets) > n_cand:
+        raise ValueError(f"{len(subsets)} subsets for {n_cand} slots")
+    for c, sub in enumerate(subsets):
+        if sub is None:
+            continue
+        a = np.asarray(sub)
+        if a.dtype == np.bool_:
+            if a.shape != (n_particles,):
+                raise ValueError(f"slot {c}: a boolean subset needs {n_particles} entries, got {a.shape}")
+            mask[c] = a
+            continue
+        a = a.astype(np.int64, copy=False).reshape(-1)
+        if a.size and (a.min() < 0 or a.max() >= n_particles):
+            raise ValueError(f"slot {c}: particle index out of range 0..{n_particles - 1}")
+        if np.unique(a).size != a.size:
+            raise ValueError(f"slot {c}: repeated particle index")
+        mask[c] = 0
+        mask[c, a] = 1
+    return mask
+
+
 class BatchScoringJob:
     """Many candidates per launch sequence, replayed as one CUDA graph.
 
@@ -408,6 +443,14 @@ class BatchScoringJob:
     new generation copies the poses in and replays the graph. This is the
     GPU form of the Lite tree's round-batched evaluation
     (ZL gisapr_batch_search.py:251-364).
+
+    Slots may score different particle subsets (``set_subsets``): a slot's
+    score, records and search text are those of a job that holds only its
+    particles. The subset mask lives on the device and is read when the
+    kernels run, so subsets may change between graph replays. The plain
+    correlation skips the (slot, particle) pairs left out; the tensor-core
+    correlation computes every slot's rows of a particle tile and the
+    records and score leave the pairs out.
     """
 
     PRECISIONS = ("fp32", "fp16x3", "fp16", "bf16x3", "bf16")
@@ -416,7 +459,7 @@ class BatchScoringJob:
 
     def __init__(self, job: ScoringJob, n_cand: int, models: Optional[Sequence] = None,
                  model_of: Optional[Sequence[int]] = None, use_graph: bool = True, precision: str = "fp32",
-                 tc_chunk: int = 128):
+                 tc_chunk: int = 128, lanes: int = 2):
         if precision not in self.PRECISIONS:
             raise ValueError(f"precision must be one of {self.PRECISIONS}, got {precision!r}")
         self.precision = precision
@@ -449,14 +492,33 @@ class BatchScoringJob:
         self.peak_x = torch.empty(shape, dtype=torch.int32, device=dev)
         self.zscore = torch.empty(shape, dtype=torch.float32, device=dev)
         self.totals = torch.zeros(self.n_cand, dtype=torch.float64, device=dev)
+        self.subset = torch.ones(shape, dtype=torch.uint8, device=dev)
         self.poses_dev = torch.zeros((self.n_cand, 12), dtype=torch.float64, device=dev)
         self.poses_host = torch.zeros((self.n_cand, 12), dtype=torch.float64).pin_memory()
         self.totals_host = torch.zeros(self.n_cand, dtype=torch.float64).pin_memory()
         self.use_graph = bool(use_graph)
         self.graph = None
         self.stream = torch.cuda.Stream(dev)
+        self._setup_lanes(int(lanes))
         if precision != "fp32":
             self._setup_tensor_path(n_needed)
+
+    def _setup_lanes(self, lanes: int) -> None:
+        """Template lanes: slot c's density, volume transform and projector run
+        on lane c % lanes. Lane 0 is the caller's stream and native context;
+        each further lane has its own stream, native context (its own
+        splat, transform and projector scratch) and density buffer, so the
+        slots' template stages overlap on the GPU (one slot's short splat
+        and transform launches fill the tail of another's projector)."""
+        if lanes < 1:
+            raise ValueError("lanes must be at least 1")
+        job = self.job
+        dev = torch.device(job.device)
+        idx = dev.index if dev.index is not None else torch.cuda.current_device()
+        self.lanes = [(None, None, None)]
+        for _ in range(1, min(lanes, self.n_cand)):
+            vol = torch.empty_like(job.vol_buf) if job.vol_buf is not None else None
+            self.lanes.append((nat.Context(idx), torch.cuda.Stream(dev), vol))
 
     TC_MAX_CAND = 128  # candidates per tensor-core launch
 
@@ -581,16 +643,33 @@ class BatchScoringJob:
                 marks.append((name, ev))
 
         mark("start")
+        n_lanes = min(len(self.lanes), n_act)
+        main = torch.cuda.current_stream(dev)
+        if n_lanes > 1:
+            fork = torch.cuda.Event()
+            fork.record(main)
+            for _, lane_stream, _ in self.lanes[1:n_lanes]:
+                lane_stream.wait_event(fork)
         for c in range(n_act):
-            vol = job.model_density(self.models[self.model_of[c]], self.poses_dev[c])
-            job.enqueue_templates(vol, self.banks[c])
+            lane_ctx, lane_stream, lane_vol = self.lanes[c % n_lanes]
+            model = self.models[self.model_of[c]]
+            if lane_ctx is None:
+                job.enqueue_templates(job.model_density(model, self.poses_dev[c]), self.banks[c])
+            else:
+                with torch.cuda.stream(lane_stream), nat.Context.using(lane_ctx):
+                    job.enqueue_templates(job.model_density(model, self.poses_dev[c], out=lane_vol),
+                                          self.banks[c])
+        for _, lane_stream, _ in self.lanes[1:n_lanes]:
+            join = torch.cuda.Event()
+            join.record(lane_stream)
+            main.wait_event(join)
         mark("templates")
         np_ = len(job.records)
         if self.precision == "fp32":
-            nat.call("gisapr_correlate_batch", ctx, st, nat.ptr(self.banks), self.bank_stride, n_act,
+            nat.call("gisapr_correlate_batch_subset", ctx, st, nat.ptr(self.banks), self.bank_stride, n_act,
                      nat.ptr(job.stack), nat.ptr(job.local_ptr), nat.ptr(job.local_idx), np_, job.nnz, job.n_psi,
-                     job.cfg.new_box, job.cfg.crop, nat.ptr(self.score_buf), nat.ptr(self.y_buf),
-                     nat.ptr(self.x_buf))
+                     job.cfg.new_box, job.cfg.crop, nat.ptr(self.subset), nat.ptr(self.score_buf),
+                     nat.ptr(self.y_buf), nat.ptr(self.x_buf))
         else:
             m = max(1, job.nnz) * job.n_psi
             for c0, cc in self._chunks(n_act):
@@ -604,12 +683,13 @@ class BatchScoringJob:
                          nat.c_ptr_offset(self.y_buf, c0 * m * 4), nat.c_ptr_offset(self.x_buf, c0 * m * 4),
                          nat.ptr(self.tc_status))
         mark("correlate")
-        nat.call("gisapr_particle_results_batch", st, nat.ptr(job.local_ptr), nat.ptr(self.score_buf),
-                 nat.ptr(self.y_buf), nat.ptr(self.x_buf), np_, job.n_psi, n_act, nat.ptr(self.best_entry),
+        nat.call("gisapr_particle_results_subset", st, nat.ptr(job.local_ptr), nat.ptr(self.score_buf),
+                 nat.ptr(self.y_buf), nat.ptr(self.x_buf), np_, job.n_psi, n_act, nat.ptr(self.subset),
+                 nat.ptr(self.best_entry),
                  nat.ptr(self.best_psi), nat.ptr(self.peak), nat.ptr(self.peak_y), nat.ptr(self.peak_x),
                  nat.ptr(self.zscore))
-        nat.call("gisapr_score_sum_batch", st, nat.ptr(job.local_ptr), nat.ptr(self.peak), np_, n_act,
-                 nat.ptr(self.totals))
+        nat.call("gisapr_score_sum_subset", st, nat.ptr(job.local_ptr), nat.ptr(self.peak), np_, n_act,
+                 nat.ptr(self.subset), nat.ptr(self.totals))
         mark("records")
 
     def stage_ms(self, poses) -> Dict[str, float]:
@@ -642,18 +722,29 @@ class BatchScoringJob:
         else:
             self.enqueue()
 
+    def set_subsets(self, subsets) -> None:
+        """Particle subsets per slot (see ``subset_mask`` for the forms;
+        None: every slot scores every particle). They stay until changed.
+        The mask is copied synchronously, so it is in place for the next
+        run or graph replay on any stream."""
+        mask = subset_mask(subsets, self.n_cand, len(self.job.records))
+        self.subset.copy_(torch.from_numpy(mask))
+
     def set_poses(self, poses) -> None:
         for c, p in enumerate(poses):
             self.poses_host[c].copy_(self.models[self.model_of[c]].pose_tensor(p))
         self.poses_dev.copy_(self.poses_host, non_blocking=True)
 
-    def score_active(self, poses, stream=None) -> np.ndarray:
+    def score_active(self, poses, stream=None, subsets=None) -> np.ndarray:
         """Scores of up to n_cand poses in one eager launch sequence on
         ``stream`` (default: the batch stream); slots past len(poses) are not
-        computed. Blocks until the scores are on the host."""
+        computed. ``subsets``: set_subsets first when given. Blocks until the
+        scores are on the host."""
         k = len(poses)
         if not 0 < k <= self.n_cand:
             raise ValueError(f"expected 1..{self.n_cand} poses, got {k}")
+        if subsets is not None:
+            self.set_subsets(subsets)
         st = stream if stream is not None else self.stream
         for c, p in enumerate(poses):
             self.poses_host[c].copy_(self.models[self.model_of[c]].pose_tensor(p))
@@ -678,10 +769,13 @@ class BatchScoringJob:
         return ["".join(str(row) + "\n" for row in self.job.format_results(r))
                 for r in self.slot_results(n_slots)]
 
-    def score_batch(self, poses) -> np.ndarray:
-        """Scores of len(poses) == n_cand poses, in slot order."""
+    def score_batch(self, poses, subsets=None) -> np.ndarray:
+        """Scores of len(poses) == n_cand poses, in slot order
+        (``subsets``: set_subsets first when given)."""
         if len(poses) != self.n_cand:
             raise ValueError(f"expected {self.n_cand} poses, got {len(poses)}")
+        if subsets is not None:
+            self.set_subsets(subsets)
         self._ensure_graph()
         self.set_poses(poses)
         self.run()

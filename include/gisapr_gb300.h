@@ -196,14 +196,46 @@ int gisapr_correlate_batch(gisapr_ctx ctx, void* stream, const float* bank, long
                            int nnz, int n_psi, int n, int crop, float* out_score, int* out_y, int* out_x);
 
 /*
+ * Particle subsets per candidate. subset [n_cand][n_particles] (bytes,
+ * device memory; NULL = every candidate scores every particle): candidate c
+ * scores particle b when subset[c][b] != 0. The reference's round-batched
+ * search scores every candidate on the job's whole particle set
+ * (ZL/gisapr_batch_search.py:314-349, 361); a candidate with a subset gets
+ * what that search gives on a job holding only those particles.
+ *   gisapr_correlate_batch_subset: gisapr_correlate_batch that skips the
+ *     (candidate, particle) pairs left out (their map entries are left
+ *     as they were; a particle no candidate scores is not read).
+ *   gisapr_particle_results_subset: a pair left out gets the record of a
+ *     particle without directions (best_entry -1).
+ *   gisapr_score_sum_subset: the sum over the candidate's particles only.
+ * The mask is read when the kernels run, so a captured CUDA graph that names
+ * it takes new subsets written between replays.
+ */
+int gisapr_correlate_batch_subset(gisapr_ctx ctx, void* stream, const float* bank, long long bank_stride,
+                                  int n_cand, const float* stack, const int* local_ptr, const int* local_idx,
+                                  int n_particles, int nnz, int n_psi, int n, int crop, const unsigned char* subset,
+                                  float* out_score, int* out_y, int* out_x);
+int gisapr_particle_results_subset(void* stream, const int* local_ptr, const float* score, const int* ys,
+                                   const int* xs, int n_particles, int n_psi, int n_cand,
+                                   const unsigned char* subset, int* best_entry, int* best_psi, float* peak,
+                                   int* peak_y, int* peak_x, float* zscore);
+int gisapr_score_sum_subset(void* stream, const int* local_ptr, const float* peak, int n_particles, int n_cand,
+                            const unsigned char* subset, double* out);
+
+/*
  * Launch-shape knobs of a context per transform size, chosen by the
  * autotuner (gisapr_gb300/autotune.py); no counterpart in the reference.
  *   GISAPR_TUNE_CORR_CLUSTER: CTAs per particle (thread-block cluster size,
  *     1..8; 0 = the default) of gisapr_correlate and gisapr_correlate_batch
  *     at correlation size ``size``. Results do not depend on it beyond
  *     float32 summation order of the cluster's partial maps.
+ *   GISAPR_TUNE_TC_A_STAGES / GISAPR_TUNE_TC_B_STAGES: shared-memory ring
+ *     depths of the tensor-core correlation at particle size ``size`` (A:
+ *     bulk-copied template rows, 2..8; B: built particle rows, 2..3; 0 =
+ *     the default: B two deep, A as deep as the shared memory allows).
+ *     Depths that do not fit are reduced. Results do not depend on them.
  */
-enum { GISAPR_TUNE_CORR_CLUSTER = 1 };
+enum { GISAPR_TUNE_CORR_CLUSTER = 1, GISAPR_TUNE_TC_A_STAGES = 2, GISAPR_TUNE_TC_B_STAGES = 3 };
 int gisapr_set_tuning(gisapr_ctx ctx, int key, int size, int value);
 int gisapr_get_tuning(gisapr_ctx ctx, int key, int size, int* value);
 

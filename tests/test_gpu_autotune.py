@@ -42,6 +42,9 @@ def test_tune_caches_and_keeps_scores(golden32, tmp_path):
         assert r.tc_chunk in (8,) or r.tc_chunk <= 8
         assert any(k.startswith("plain_cluster_") for k in r.times_ms)
         assert any(k.startswith("tc_chunk_") for k in r.times_ms)
+        assert any(k.startswith("tc_rings_") for k in r.times_ms)
+        assert (r.tc_a_stages, r.tc_b_stages) in ((4, 2), (3, 2), (6, 2), (4, 3))
+        assert r.dirs_per_tile == 128 // 8
         assert (tmp_path / "tuning.json").exists()
         r2 = Autotuner(tmp_path / "tuning.json").tune(job, n_cand=8, precision="fp16x3")
         assert (r2.corr_cluster, r2.tc_chunk, r2.times_ms) == (r.corr_cluster, r.tc_chunk, r.times_ms)
@@ -58,5 +61,21 @@ def test_tune_caches_and_keeps_scores(golden32, tmp_path):
             nat.call("gisapr_set_tuning", ctx.handle, nat.TUNE_CORR_CLUSTER, 32, 9)
         with pytest.raises(ValueError):
             nat.call("gisapr_set_tuning", ctx.handle, 77, 32, 1)
+        # every ring depth gives bitwise the same tensor-core maps
+        tc_ref = BatchScoringJob(job, 8, use_graph=False, precision="fp16x3", tc_chunk=r.tc_chunk)
+        tc_ref.score_active(poses)
+        maps = tc_ref.score_buf.cpu().numpy()
+        for sa, sb in ((2, 2), (3, 3), (8, 2)):
+            nat.call("gisapr_set_tuning", ctx.handle, nat.TUNE_TC_A_STAGES, 32, sa)
+            nat.call("gisapr_set_tuning", ctx.handle, nat.TUNE_TC_B_STAGES, 32, sb)
+            b = BatchScoringJob(job, 8, use_graph=False, precision="fp16x3", tc_chunk=r.tc_chunk)
+            b.score_active(poses)
+            np.testing.assert_array_equal(b.score_buf.cpu().numpy(), maps)
+        with pytest.raises(ValueError):
+            nat.call("gisapr_set_tuning", ctx.handle, nat.TUNE_TC_A_STAGES, 32, 9)
+        with pytest.raises(ValueError):
+            nat.call("gisapr_set_tuning", ctx.handle, nat.TUNE_TC_B_STAGES, 48, 2)
     finally:
         nat.set_default_tuning(nat.TUNE_CORR_CLUSTER, 32, 0)
+        nat.set_default_tuning(nat.TUNE_TC_A_STAGES, 32, 0)
+        nat.set_default_tuning(nat.TUNE_TC_B_STAGES, 32, 0)

@@ -201,7 +201,21 @@ def run_batched(job, dens, gen, precision, n_batch, K, W, device, barrier, tc_ch
     torch.cuda.synchronize(device)
     b_e2e = e2.elapsed_time(e3) / 1e3
     stages = bj.stage_ms(gen[W])
-    return {"candidates_per_step": n_batch, "precision": precision,
+    extra = {}
+    if precision != "fp32":
+        # tensor pipe: MMA flops the generation issues over the correlation
+        # stage's device time (the stage also holds the operand copy of the banks)
+        _, bf16_peak, peak_kind = load_peaks()
+        flops = bj.tc_mma_flops()
+        ach = flops / (stages["correlate"] / 1e3) / 1e12
+        extra["roofline"] = {
+            "kernel": "correlate_tc", "bound": "tensor", "achieved": ach, "peak": bf16_peak, "unit": "TFLOP/s",
+            "frac": ach / bf16_peak, "traffic": None,
+            "peak_source": f"{peak_kind} bf16 dense (MEASURED_PEAKS.json)" if peak_kind == "measured" else "fallback",
+            "algorithmic": f"{flops:.4g} MMA flop issued per generation (M=128, K=16 MMAs of every work item, "
+                           f"padding rows included) over the correlation stage",
+            "stage_ms": stages["correlate"]}
+    return {"candidates_per_step": n_batch, "precision": precision, **extra,
             "moving_chain_atoms": [m.n_moving for m in dens],
             "graph": bj.graph is not None, "ms_per_step": b_elapsed / K * 1e3,
             "latency_ms": {"p50": b_lat[len(b_lat) // 2],

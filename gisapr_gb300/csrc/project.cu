@@ -1061,18 +1061,17 @@ __global__ void __launch_bounds__(kRiWarps * 32) rows_inverse(const float2* __re
   for (int t = threadIdx.x; t < kMaxFftLen / 2; t += blockDim.x) s_tw[t] = tw_g[t];
   const float* R = rot + (size_t)dirs[b] * 9;
   float2(*L)[LINE] = s_line[warp];
-  // The CTA gathers its columns together: a warp load takes all ncta
-  // (usually 8) columns x 32/ncta rows, a compact patch of the slice whose
-  // trilinear corners share the blocked copy's 128-byte lines (2 columns x
-  // 16 rows per load had cut the gather's time by 40% against 32 rows of
-  // one column); each sample lands in the staged line of the warp that
-  // transforms its column.
+  // Lanes take the warp's nc columns x 32/nc rows per load: samples of
+  // neighbouring columns share trilinear corners. Against 32 rows of one
+  // column this patch shape cut the gather's time by 40% on GB300; a
+  // CTA-wide patch (8 columns x 4 rows per warp load) was slower again
+  // (templates of a 64-candidate batch at box 128: 48.7 ms against 45.1).
   const int ncta = max(0, min(CC, W - c_cta));
 #pragma unroll 4
-  for (int idx = threadIdx.x; idx < ncta * m; idx += blockDim.x) {
-    const int cc = idx % ncta, r = idx / ncta;
+  for (int idx = lane; idx < nc * m; idx += 32) {
+    const int cl = idx % nc, r = idx / nc;
     const int k = r >> 1;
-    s_line[cc / CPR][2 * (cc % CPR) + (r & 1)][k + (k >> 3)] = slice_value<N>(spectrum, R, r, c_cta + cc);
+    L[2 * cl + (r & 1)][k + (k >> 3)] = slice_value<N>(spectrum, R, r, cw + cl);
   }
   __syncthreads();
   if (nc > 0) {

@@ -592,6 +592,21 @@ class BatchScoringJob:
             self.tc_plans[cc] = (torch.from_numpy(work).to(job.device), count.value)
         return self.tc_plans[cc]
 
+    def tc_mma_flops(self) -> float:
+        """Tensor-core flops one generation issues: per work item and K step
+        (32 rows of a packed column, 64 K elements) four MMAs of
+        M = 128 x N x K = 16 per pass (three passes for the split forms),
+        N = psi angles per tile x 2 crop (rounded up to 8 per psi, then to 16)."""
+        if self.precision == "fp32":
+            return 0.0
+        nb, crop = self.job.cfg.new_box, self.job.cfg.crop
+        psi_group = 3 if crop <= 12 else 2
+        kn = -(-psi_group * (-(-2 * crop // 8) * 8) // 16) * 16
+        passes = 3 if self.precision in ("fp16x3", "bf16x3") else 1
+        steps = (nb // 2 + 1) * (nb // 32)
+        items = sum(self._tc_plan(cc)[1] for _, cc in self.tc_chunks)
+        return float(items) * steps * passes * 4 * 2.0 * 128 * kn * 16
+
     def _chunks(self, n_active: int):
         if n_active == self.n_cand:
             return self.tc_chunks

@@ -1,7 +1,7 @@
 """Install GisAPR's own code into baseline/_ref for the reference arm of
 bench.py -- BENCH INFRASTRUCTURE, never imported by the package.
 
-    python oracle/install_reference.py --reference <GisAPR source root>
+    python baseline/install_reference.py --reference <GisAPR source root>
 
 GisAPR is a flat directory of scripts plus two source zips, not a Python
 package. The recipe first tries the offline pip install of the reference

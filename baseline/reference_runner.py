@@ -1,19 +1,22 @@
-"""GisAPR's own CPU path, timed -- BENCH INFRASTRUCTURE ONLY.
+"""GisAPR's own code, timed -- BENCH INFRASTRUCTURE ONLY.
 
 The reference arm of bench.py runs the reference's code itself, unmodified,
-from baseline/_ref (unpacked there by oracle/install_reference.py; nothing
-reads the original source tree at run time): the optimized-3 tree's
-pdb2mrc v3 ``generate_volume`` (every atom re-splatted per candidate, torch
-CPU), v606's ``IntegratedProjector.build_templates`` over every direction of
-the angle table, ``PackedCTFTorch.batch``, and per particle
+from baseline/_ref (unpacked there by baseline/install_reference.py;
+nothing reads the original source tree at run time): the optimized-3
+tree's pdb2mrc v3 ``generate_volume`` (every atom re-splatted per
+candidate), v606's ``IntegratedProjector.build_templates`` over every
+direction of the angle table, ``PackedCTFTorch.batch``, and per particle
 ``ParticleFourierPreparer.prepare``, ``correlate_templates_and_particle``
 and ``make_result_records``, in the order of its ``run_search`` loop
-(v606:1594-1825), with torch using every host thread.
+(v606:1594-1825). On the CPU torch uses every host thread; with a CUDA
+device the same functions run on the GPU (the reference's own torch CUDA
+path), with a synchronize at each stage boundary.
 
-``RefRunner(job, root).step(pose, particle_index)`` scores one candidate
-pose on the given particles of the job and returns the seconds of each
-stage. The package never imports this module; bench.py's reference arm and
-its CPU baseline are its only users.
+``RefRunner(job, device=...).step(pose, particle_index)`` scores one
+candidate pose on the given particles of the job and returns the seconds of
+each stage. ``RefDeposit`` is the Lite tree's NVRTC splat. The package never
+imports this module; bench.py's reference arm, its CPU baseline and its
+comparisons with the reference's GPU code are its only users.
 """
 from __future__ import annotations
 
@@ -86,10 +89,11 @@ class RefRunner:
     """One job's tables built once (as the reference's worker caches them),
     then candidate evaluations through the reference's functions."""
 
-    def __init__(self, job, threads: int = 0):
+    def __init__(self, job, threads: int = 0, device: str = "cpu"):
         import torch
         self.threads = threads or (os.cpu_count() or 1)
         torch.set_num_threads(self.threads)
+        self.device = torch.device(device)
         self.v606, self.pdb2mrc, self.pdb_text = import_reference()
         v = self.v606
         spec = job.spec
@@ -103,21 +107,22 @@ class RefRunner:
         table = v.read_particle_table(str(self.tmp / "particles.star"))
         self.table = table
         self.records = table.records
-        dev = torch.device("cpu")
+        dev = self.device
         n, nb = spec.box, spec.new_box
         self.layout = v.PackedFourierLayout(nb, spec.crop, dev)
         self.new_apix = n / nb * spec.apix
         self.trans_scale = spec.apix / self.new_apix
         self.local = {e[0]: e[1:] for e in v.build_local_orientation_entries(
             self.records, self.angles.rot, self.angles.tilt, spec.local_range)}
-        mask = torch.from_numpy(v.generate_soft_mask((n, n), spec.mask_radius, spec.mask_edge))
+        mask = torch.from_numpy(v.generate_soft_mask((n, n), spec.mask_radius, spec.mask_edge)).to(dev)
         fsc_path = ""
         if spec.fsc_half_res is not None:
             fsc_path = str(self.tmp / "fsc.txt")
             with open(fsc_path, "w") as f:
                 for k, val in enumerate(job.fsc):
                     f.write(f"{k} {float(val)!r}\n")
-        packed_fsc = self.layout.centered_full_to_packed(torch.from_numpy(v.read_fsc_map(fsc_path, n, nb, False)))
+        packed_fsc = self.layout.centered_full_to_packed(
+            torch.from_numpy(v.read_fsc_map(fsc_path, n, nb, False)).to(dev))
         self.projector = v.IntegratedProjector(dev, n, nb, self.layout, mask, packed_fsc, 8)
         self.psi_meta = {}
         uniq = {}
@@ -136,31 +141,40 @@ class RefRunner:
         """One candidate on the given particles: stage seconds, the number of
         templates built and the partial score sum_i exp(rawCC_i / 1024)."""
         import torch
-        v, spec = self.v606, self.spec
+        v, spec, dev = self.v606, self.spec, self.device
         out: Dict[str, float] = {}
+
+        def now():
+            if dev.type == "cuda":
+                torch.cuda.synchronize(dev)
+            return time.perf_counter()
+
         with torch.no_grad():
-            t0 = time.perf_counter()
+            t0 = now()
             density = self.pdb2mrc.generate_volume(str(self.pdb_path), spec.box, spec.apix, spec.res,
-                                                   device="cpu", source_pdb=str(self.pdb_path), chain_id="A",
+                                                   device=str(dev), source_pdb=str(self.pdb_path), chain_id="A",
                                                    pose=list(map(float, pose)))
-            t1 = time.perf_counter()
+            t1 = now()
             templates = self.projector.build_templates(density, self.angles)
-            t2 = time.perf_counter()
+            t2 = now()
             recs = [self.records[i] for i in particle_index]
             ctf = self.ctfgen.batch(recs, self.table.has_ctf)
+            if isinstance(ctf, np.ndarray):
+                ctf = torch.from_numpy(ctf)
+            ctf = ctf.to(dev)
             raw = []
             for k, (i, rec) in enumerate(zip(particle_index, recs)):
                 idx = self.local.get(rec.line_index, [])
                 if not idx:
                     continue
                 fake, eff = self.psi_meta[rec.line_index]
-                p = self.prep.prepare(torch.from_numpy(self.images[i]), eff, ctf[k])
-                lt = templates.index_select(0, torch.tensor(idx, dtype=torch.long))
+                p = self.prep.prepare(torch.from_numpy(self.images[i]).to(dev), eff, ctf[k])
+                lt = templates.index_select(0, torch.tensor(idx, dtype=torch.long, device=dev))
                 s, y, x = v.correlate_templates_and_particle(lt, p, self.layout, self.ws)
                 rr = v.make_result_records(rec, fake, self.angles.rot, self.angles.tilt, idx, s, y, x,
                                            self.layout.crop_size, self.trans_scale)
                 raw.append(rr[2][2])
-            t3 = time.perf_counter()
+            t3 = now()
         out["density_s"] = t1 - t0
         out["templates_s"] = t2 - t1
         out["particles_s"] = t3 - t2

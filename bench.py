@@ -16,7 +16,7 @@ read every step, so inputs exceed L2), then the same K poses through the
 public API with the pose copied host->device and the score plus the
 per-particle peaks copied back each step (``e2e``). The reference arm
 (``--impl reference``) runs GisAPR's own CPU torch path, installed
-unmodified in baseline/_ref by oracle/install_reference.py, on the same job
+unmodified in baseline/_ref by baseline/install_reference.py, on the same job
 and poses (each step one pose with a particle sample, the candidate rate
 extrapolated over particles); without baseline/_ref it falls back to the
 numpy restatement of that path and says so.
@@ -68,6 +68,8 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=400, help="particles and templates in the CPU sample")
     ap.add_argument("--batch", type=int, default=64, help="candidates per batched generation (0: skip)")
+    ap.add_argument("--reference-cuda-sample", type=int, default=500,
+                    help="particles of the reference's own torch CUDA path timed beside this one (0: skip)")
     ap.add_argument("--no-autotune", action="store_true", help="default launch shapes (no tuning runs)")
     ap.add_argument("--precision-particles", type=int, default=4000,
                     help="particles of the box-256 precision comparison (0: skip it; 20000 is the full "
@@ -296,7 +298,7 @@ def reference_job(args):
 
 
 def run_reference(args):
-    """GisAPR's own CPU path (oracle/reference_cpu.py, from baseline/_ref) on
+    """GisAPR's own CPU path (baseline/reference_runner.py, from baseline/_ref) on
     the GPU arm's job and poses. Each step scores one candidate pose:
     density of every atom, every template of the angle table, and the
     reference's per-particle loop over an evenly spaced sample of the
@@ -305,12 +307,12 @@ def run_reference(args):
     loop is linear in particles). Without baseline/_ref the numpy port of
     the same path (the oracle) stands in and the line says so."""
     import numpy as np
-    from oracle import reference_cpu
+    from baseline import reference_runner as ref_runner
     spec, data, poses = reference_job(args)
     n_p = len(data.records.rot)
     sample = np.unique(np.linspace(0, n_p - 1, min(REF_PARTICLE_SAMPLE, n_p)).astype(int)).tolist()
-    if reference_cpu.available():
-        runner = reference_cpu.RefRunner(data)
+    if ref_runner.available():
+        runner = ref_runner.RefRunner(data)
         kind, dtype = "reference", "f32"
         step = lambda pose: runner.step(pose, sample)  # noqa: E731
         threads = runner.threads
@@ -724,6 +726,22 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
         line["precision"] = run_precision(args, device)
     if world == 1:
         line["deposit_vs_reference"] = run_deposit_comparison(job, data, spec, poses[W], device)
+    if world == 1 and args.reference_cuda_sample > 0:
+        rc = run_reference_cuda(data, poses[W], device, args.reference_cuda_sample)
+        if "value" in rc:
+            # the reference's partial score over its particle sample against the
+            # same particles' peaks from this path (one candidate, same pose)
+            import numpy as np
+            job.score(poses[W])
+            pk = job.peak.cpu().numpy().astype(np.float64)
+            has = (job.local_ptr[1:] > job.local_ptr[:-1]).cpu().numpy()
+            sel = [i for i in rc.pop("particles") if has[i]]
+            ours = float(np.sum(np.exp(pk[sel] / 1024.0)))
+            rc["partial_score_rel_diff"] = abs(ours / rc.pop("partial_score") - 1.0)
+            rc["gb300_plain_vs_reference_cuda"] = value / rc["value"]
+            for name, b in batched.items():
+                rc[f"gb300_batched_{name}_vs_reference_cuda"] = b["value"] / rc["value"]
+        line["reference_torch_cuda"] = rc
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = run_cpu_baseline(spec, data, poses[W], args.cpu_sample)
     print(json.dumps(line), flush=True)
@@ -733,11 +751,11 @@ def run_cpu_baseline(spec, data, pose, sample: int) -> dict:
     """The reference's own CPU path on this job (one pose, 100 particles;
     about 10 s of CPU work), or the numpy port when baseline/_ref is absent."""
     import numpy as np
-    from oracle import reference_cpu
+    from baseline import reference_runner as ref_runner
     n_p = len(data.records.rot)
-    if reference_cpu.available():
+    if ref_runner.available():
         idx = np.unique(np.linspace(0, n_p - 1, min(100, n_p)).astype(int)).tolist()
-        runner = reference_cpu.RefRunner(data)
+        runner = ref_runner.RefRunner(data)
         t0 = time.perf_counter()
         r = runner.step(pose, idx)
         wall = time.perf_counter() - t0
@@ -754,6 +772,36 @@ def run_cpu_baseline(spec, data, pose, sample: int) -> dict:
                       f"{n_p} particles (prepare + correlate), extrapolated ({cb['sample_wall_s']:.1f} s of CPU work)"}
 
 
+def run_reference_cuda(data, pose, device, sample: int = 500) -> dict:
+    """GisAPR's own torch path on this GPU (the same functions the CPU
+    baseline runs, device cuda): one pose, density, every template, and an
+    evenly spaced sample of the job's particles, the particle time scaled to
+    the whole job; the score of the sample is checked against the GB300
+    path's per-particle peaks by the caller."""
+    import numpy as np
+    from baseline import reference_runner as ref_runner
+    if not ref_runner.available():
+        return {"unavailable": "baseline/_ref (the reference's optimized-3 tree) is not installed"}
+    n_p = len(data.records.rot)
+    idx = np.unique(np.linspace(0, n_p - 1, min(sample, n_p)).astype(int)).tolist()
+    try:
+        runner = ref_runner.RefRunner(data, device=str(device))
+        runner.step(pose, idx[:4])  # warm-up: cuFFT plans, kernel loads, caching allocator
+        t0 = time.perf_counter()
+        r = runner.step(pose, idx)
+        wall = time.perf_counter() - t0
+    except Exception as exc:  # noqa: BLE001 - reported, not hidden
+        return {"unavailable": f"reference torch CUDA path failed: {type(exc).__name__}: {exc}"[:300]}
+    sec = r["density_s"] + r["templates_s"] + r["particles_s"] * n_p / len(idx)
+    return {"value": 1.0 / sec, "unit": UNIT,
+            "stage_s": {"density": r["density_s"], "templates": r["templates_s"],
+                        "particles_scaled": r["particles_s"] * n_p / len(idx)},
+            "sample": f"GisAPR's own torch path from baseline/_ref on {device}, one pose: density, "
+                      f"{int(r['n_templates'])} templates, {len(idx)} of {n_p} particles (particle time "
+                      f"scaled to all {n_p}; {wall:.1f} s wall)",
+            "partial_score": r["partial_score"], "particles": idx}
+
+
 def run_deposit_comparison(job, data, spec, pose, device, reps: int = 20) -> dict:
     """The moving chain onto the cached fixed context, as one candidate's
     density step: the reference's GPU splat (pdb2mrc v4 with the NVRTC
@@ -764,8 +812,8 @@ def run_deposit_comparison(job, data, spec, pose, device, reps: int = 20) -> dic
     and PDB 8.3 round trip on the host, not timed)."""
     import numpy as np
     import torch
-    from oracle import reference_cpu
-    if not reference_cpu.RefDeposit.available():
+    from baseline import reference_runner as ref_runner
+    if not ref_runner.RefDeposit.available():
         return {"unavailable": "baseline/_ref (the reference's Lite tree) is not installed"}
     from gisapr_gb300.pdb_text import quantize_coordinates, transform_coordinates
     dens = job.density
@@ -775,7 +823,7 @@ def run_deposit_comparison(job, data, spec, pose, device, reps: int = 20) -> dic
     xyz = torch.from_numpy(np.ascontiguousarray(moved, np.float32)).to(device)
     z = dens.moving_z.to(device)
     fixed = dens.fixed.to(device)
-    ref = reference_cpu.RefDeposit()
+    ref = ref_runner.RefDeposit()
     try:
         ref.deposit(xyz, z, spec.box, spec.apix, spec.res, fixed)  # compiles the kernel (NVRTC)
     except Exception as exc:  # noqa: BLE001 - reported, not hidden

@@ -76,7 +76,7 @@ def parse_args():
                          "configuration, about three minutes of synthetic-data generation)")
     ap.add_argument("--serve-requests", type=int, default=40,
                     help="requests in the serving stream (0: skip the serving measurement)")
-    ap.add_argument("--precisions", default="fp32,fp16x3",
+    ap.add_argument("--precisions", default="fp32,fp16x3,fp16",
                     help="batched correlation forms to time: fp32 (plain), fp16x3 (tensor-core split), fp16")
     return ap.parse_args()
 

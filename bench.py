@@ -161,7 +161,7 @@ def job_records(job):
                            float(r.defocus_angle[i])) for i in range(len(r.rot))]
 
 
-def run_batched(job, dens, gen, precision, n_batch, K, W, device, barrier, tc_chunk=128):
+def run_batched(job, dens, gen, precision, n_batch, K, W, device, barrier, tc_chunk=128, lanes=2):
     """Time K graph-replayed generations of n_batch candidates (device events on
     the batch stream), then K end-to-end generations (poses from the host,
     scores and per-particle peaks back)."""
@@ -169,7 +169,7 @@ def run_batched(job, dens, gen, precision, n_batch, K, W, device, barrier, tc_ch
     from gisapr_gb300.engine import BatchScoringJob
     model_of = [i % len(dens) for i in range(n_batch)]
     bj = BatchScoringJob(job, n_batch, models=dens, model_of=model_of, precision=precision,
-                         tc_chunk=min(tc_chunk, 128))
+                         tc_chunk=min(tc_chunk, 128), lanes=lanes)
     for k in range(W):
         bj.score_batch(gen[k])
     barrier()
@@ -656,10 +656,12 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
             autotune = {"corr_cluster": tuned.corr_cluster, "tc_chunk": tuned.tc_chunk,
                         "tc_dirs_per_tile": tuned.dirs_per_tile,
                         "tc_rings": [tuned.tc_a_stages, tuned.tc_b_stages],
+                        "template_lanes": tuned.template_lanes,
                         "correlate_ms": tuned.times_ms, "tune_s": time.perf_counter() - t_tune}
         for precision in args.precisions.split(","):
             batched[precision] = run_batched(job, dens, gen, precision, args.batch, K, W, device, barrier,
-                                             tc_chunk=tuned.tc_chunk if tuned else 128)
+                                             tc_chunk=tuned.tc_chunk if tuned else 128,
+                                             lanes=tuned.template_lanes if tuned else 2)
             batched[precision]["autotune"] = autotune
     tl = [elapsed, e2e_elapsed]
     for b in batched.values():

@@ -12,7 +12,11 @@ and particle set, and the best value depends on the GPU:
   needs;
 * the tensor-core kernel's shared-memory ring depths (A: bulk-copied
   template rows, B: built particle rows): deeper rings hide more copy
-  latency but leave less of the SM's shared memory to its L1 cache.
+  latency but leave less of the SM's shared memory to its L1 cache;
+* the template lanes of a batch (streams, each with its own native
+  context, over which the slots' density, volume transform and projector
+  launches are spread): one slot's short launches fill the tail of
+  another's projector.
 
 ``Autotuner.tune`` times the batched correlation stage (CUDA events, best of
 a few runs on the job's own data) for every valid value, keeps the fastest,
@@ -37,6 +41,7 @@ __all__ = ["Autotuner", "TuneResult", "default_cache_path"]
 CLUSTER_CHOICES = (1, 2, 3, 4, 5, 6, 8)
 CHUNK_CHOICES = (16, 32, 64, 128)
 RING_CHOICES = ((4, 2), (3, 2), (6, 2), (4, 3))  # (A, B) ring depths; the first is the kernel's default
+LANE_CHOICES = (1, 2, 3)
 SMEM_LIMIT = 227 * 1024
 
 
@@ -66,6 +71,7 @@ class TuneResult:
     tc_a_stages: int = 0  # 0: the kernel's default
     tc_b_stages: int = 0
     dirs_per_tile: int = 0
+    template_lanes: int = 2
 
     def apply(self) -> None:
         """Make the cluster size and the ring depths the defaults of every
@@ -111,9 +117,17 @@ class Autotuner:
         del bj
         return best
 
+    def _time_templates(self, job, n_cand: int, poses, lanes: int) -> float:
+        from .engine import BatchScoringJob
+        bj = BatchScoringJob(job, n_cand, use_graph=False, lanes=lanes)
+        bj.stage_ms(poses)  # warm-up: the lanes' contexts grow their scratch
+        best = min(bj.stage_ms(poses)["templates"] for _ in range(self.trials))
+        del bj
+        return best
+
     def tune(self, job, n_cand: int = 64, precision: str = "fp16x3", force: bool = False,
              clusters: Sequence[int] = CLUSTER_CHOICES, chunks: Sequence[int] = CHUNK_CHOICES,
-             rings: Sequence = RING_CHOICES) -> TuneResult:
+             rings: Sequence = RING_CHOICES, lanes: Sequence[int] = LANE_CHOICES) -> TuneResult:
         """Pick the cluster size (plain path) and, unless precision is
         "fp32", the tensor-core chunk size (hence directions per tile) and ring
         depths for batches of n_cand candidates."""
@@ -159,8 +173,17 @@ class Autotuner:
             nat.call("gisapr_set_tuning", ctx.handle, nat.TUNE_TC_A_STAGES, nb, best_ring[0])
             nat.call("gisapr_set_tuning", ctx.handle, nat.TUNE_TC_B_STAGES, nb, best_ring[1])
         dpt = 128 // ((min(best_c, 128) + 7) // 8 * 8)
+        best_l, best_lt = 1, math.inf
+        for n_l in lanes:
+            if n_l > n_cand:
+                continue
+            t = self._time_templates(job, n_cand, poses, n_l)
+            times[f"template_lanes_{n_l}"] = t
+            if t < best_lt:
+                best_l, best_lt = n_l, t
         r = TuneResult(key=key, size=nb, corr_cluster=best_k, tc_chunk=best_c, times_ms=times,
-                       tc_a_stages=best_ring[0], tc_b_stages=best_ring[1], dirs_per_tile=dpt)
+                       tc_a_stages=best_ring[0], tc_b_stages=best_ring[1], dirs_per_tile=dpt,
+                       template_lanes=best_l)
         cache[key] = asdict(r)
         self._save(cache)
         r.apply()

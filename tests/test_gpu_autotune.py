@@ -45,6 +45,8 @@ def test_tune_caches_and_keeps_scores(golden32, tmp_path):
         assert any(k.startswith("tc_rings_") for k in r.times_ms)
         assert (r.tc_a_stages, r.tc_b_stages) in ((4, 2), (3, 2), (6, 2), (4, 3))
         assert r.dirs_per_tile == 128 // 8
+        assert r.template_lanes in (1, 2, 3)
+        assert any(k.startswith("template_lanes_") for k in r.times_ms)
         assert (tmp_path / "tuning.json").exists()
         r2 = Autotuner(tmp_path / "tuning.json").tune(job, n_cand=8, precision="fp16x3")
         assert (r2.corr_cluster, r2.tc_chunk, r2.times_ms) == (r.corr_cluster, r.tc_chunk, r.times_ms)

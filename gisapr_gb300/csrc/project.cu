@@ -588,8 +588,9 @@ cudaError_t launch_project_templates(cudaStream_t st, const float2* spectrum, co
 // ===========================================================================
 namespace {
 
-constexpr int kSmemThreads = 384;
-constexpr int kSmemWarps = kSmemThreads / 32;
+// Warps of the template-tail CTA (a template parameter of the kernel; the
+// shared-memory scratch of the block sums is sized for the largest count)
+constexpr int kSmemMaxWarps = 20;
 
 // Columns a warp transforms per pass-A round: G = 32 / (N/16) lines, two
 // per column (even and odd rows of the 2N grid). The even line of column c
@@ -673,6 +674,7 @@ __device__ __forceinline__ float2 sample_slice(const float2* __restrict__ vol, f
 // and columns, row stride plane_ld(N). With it the four-step loads and stores
 // of row and column passes touch each 8-byte bank at most twice (three times
 // for two of the six patterns) per warp access.
+
 template <int N>
 struct Plane {
   float2* p;
@@ -778,11 +780,12 @@ __device__ __forceinline__ bool plane_wait(uint64_t* bar, uint32_t parity) {
   return false;
 }
 
-template <int N>
+template <int N, int kSmemWarps>
 __device__ void build_one_smem(const ProjParams& P, int slot, float2* Zs, const float2* tw, float* s_div,
                                float4* red4, float* red, float* s_misc, const unsigned short* s_bins,
                                const int* s_bptr, const float* s_fsc, const float2* next_plane, uint64_t* bar) {
   constexpr int HC = N / 2 + 1, L2 = N / 16, G = 32 / L2, RP = 2 * G;
+  constexpr int kSmemThreads = 32 * kSmemWarps;
   const Plane<N> Z{Zs};
   const int nb = P.nb, H = nb / 2 + 1;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1092,14 +1095,14 @@ __global__ void __launch_bounds__(kRiWarps * 32) rows_inverse(const float2* __re
   }
 }
 
-template <int N>
-__global__ void __launch_bounds__(kSmemThreads, 1) project_templates_smem(ProjParams P) {
+template <int N, int kSmemWarps>
+__global__ void __launch_bounds__(32 * kSmemWarps, 1) project_templates_smem(ProjParams P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* Zs = reinterpret_cast<float2*>(smem_raw);
   float2* s_tw = Zs + plane_rows(N) * plane_ld(N);
   float4* red4 = reinterpret_cast<float4*>(s_tw + kMaxFftLen / 2);
-  float* red = reinterpret_cast<float*>(red4 + kSmemWarps);
-  float* s_misc = red + kSmemWarps;                                        // [4]
+  float* red = reinterpret_cast<float*>(red4 + kSmemMaxWarps);
+  float* s_misc = red + kSmemMaxWarps;                                     // [4]
   uint64_t* bar = reinterpret_cast<uint64_t*>(s_misc + 4);
   float* s_div = reinterpret_cast<float*>(bar + 1);                         // [n_bins + 4]
   int* s_bptr = reinterpret_cast<int*>(s_div + P.n_bins + 4);              // [n_bins + 1]
@@ -1140,7 +1143,7 @@ __global__ void __launch_bounds__(kSmemThreads, 1) project_templates_smem(ProjPa
       return;
     }
     const int nxt = b + gridDim.x;
-    build_one_smem<N>(P, slot, Zs, s_tw, s_div, red4, red, s_misc, s_bins, s_bptr, s_fsc,
+    build_one_smem<N, kSmemWarps>(P, slot, Zs, s_tw, s_div, red4, red, s_misc, s_bins, s_bptr, s_fsc,
                       nxt < P.n_build ? P.planes + nxt * plane_elems : nullptr, bar);
   }
 }
@@ -1152,9 +1155,22 @@ size_t project_blocked_elems(int N) { return (size_t)4 * N * N * ((N + 1 + kBX -
 
 size_t project_smem_bytes_fast(int N, int n_bins, int nb) {
   return (size_t)plane_rows(N) * plane_ld(N) * sizeof(float2) + (kMaxFftLen / 2) * sizeof(float2) +
-         kSmemWarps * (sizeof(float4) + sizeof(float)) + 4 * sizeof(float) + sizeof(uint64_t) +
+         kSmemMaxWarps * (sizeof(float4) + sizeof(float)) + 4 * sizeof(float) + sizeof(uint64_t) +
          (size_t)(n_bins + 4) * sizeof(float) + (size_t)(n_bins + 1) * sizeof(int) +
          (size_t)N * (N / 2 + 1) * sizeof(unsigned short) + (size_t)nb * (nb / 2 + 1) * sizeof(float);
+}
+
+template <int N, int NW>
+static cudaError_t launch_tail(const ProjParams& P, int grid, size_t smem, cudaStream_t st) {
+  static size_t set_smem = 0;  // attribute set once per size, never inside a stream capture
+  if (set_smem < smem) {
+    cudaError_t e = cudaFuncSetAttribute(project_templates_smem<N, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    set_smem = smem;
+  }
+  project_templates_smem<N, NW><<<grid, 32 * NW, smem, st>>>(P);
+  return cudaGetLastError();
 }
 
 template <int N>
@@ -1172,15 +1188,9 @@ static cudaError_t launch_fast(ProjParams P, int grid, float2* planes, float2* b
   if (e0 != cudaSuccess) return e0;
   P.planes = planes;
   const size_t smem = project_smem_bytes_fast(N, P.n_bins, P.nb);
-  static size_t set_smem = 0;  // attribute set once per size, never inside a stream capture
-  if (set_smem < smem) {
-    cudaError_t e = cudaFuncSetAttribute(project_templates_smem<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e != cudaSuccess) return e;
-    set_smem = smem;
-  }
-  project_templates_smem<N><<<grid, kSmemThreads, smem, st>>>(P);
-  return cudaGetLastError();
+  // 20 warps at box 128 (templates 4% faster than with 12 or 16, measured
+  // on GB300 with 768 directions); 12 at the smaller boxes
+  return launch_tail<N, N == 128 ? 20 : 12>(P, grid, smem, st);
 }
 
 cudaError_t launch_project_templates_fast(cudaStream_t st, const float2* spectrum, const float* rot,

@@ -43,6 +43,8 @@ SIGNATURES = {
     "gisapr_score_sum_subset": [_p, _p, _p, _i, _i, _p, _p],
     "gisapr_tc_bank_bytes": [_i, _i],
     "gisapr_project_launches": [_i, _i],
+    "gisapr_projector_status": [_p, _p, _p],
+    "gisapr_set_projector_wait": [_p, C.c_longlong],
     "gisapr_set_tuning": [_p, _i, _i, _i],
     "gisapr_get_tuning": [_p, _i, _i, _p],
     "gisapr_tc_plan_work": [_p, _p, _i, _i, _i, _i, _p, _i, _p],

@@ -39,7 +39,7 @@ size_t project_smem_bytes_fast(int N, int n_bins, int nb);
 cudaError_t launch_project_templates_fast(cudaStream_t, const float2*, const float*, const int*, int,
                                           const int*, const float*, const float*, const int*, const int*,
                                           const float*, int, const float2*, float2*, int, int, int, float2*,
-                                          float2*);
+                                          float2*, int*, unsigned);
 size_t project_blocked_elems(int N);
 size_t project_slice_elems(int N, int n_build);
 cudaError_t launch_project_templates_planes(cudaStream_t, const float2*, const float*, const int*, int,
@@ -142,6 +142,8 @@ struct gisapr_context {
   std::map<int, BinTable> bins;                        // N -> radial bins
   std::map<std::pair<int, int>, CorrTables> corr;      // (n, crop) -> twiddles
   DeviceBuffer atoms, bin_counts, bin_lists, proj_scratch, prep_scratch, proj_slices, proj_blocked, vfft_scratch;
+  DeviceBuffer proj_status;        // int: set to 1 by a projector plane wait that ran out
+  unsigned proj_wait = 1u << 24;   // bound of that wait (attempts)
   int blocked_box = 0;  // box of the blocked spectrum gisapr_volume_spectrum_blocked last wrote (0: none)
   // Buffers replaced by larger ones. They are freed only with the context:
   // a CUDA graph captured before a buffer grew still names the old one, and
@@ -374,6 +376,7 @@ int gisapr_context_destroy(gisapr_ctx ctx) {
   cudaFree(ctx->proj_blocked.ptr);
   cudaFree(ctx->prep_scratch.ptr);
   cudaFree(ctx->vfft_scratch.ptr);
+  cudaFree(ctx->proj_status.ptr);
   cudaFree(ctx->tw);
   for (void* p : ctx->retired) cudaFree(p);
   cudaFree(ctx->tw3);
@@ -484,6 +487,41 @@ int gisapr_volume_spectrum_blocked(gisapr_ctx ctx, void* stream, const float* vo
   return GISAPR_OK;
 }
 
+// The projector's status word, allocated and zeroed on the context's first
+// shared-memory projector call (before any stream capture of that call).
+static int status_word(gisapr_ctx ctx) {
+  if (ctx->proj_status.ptr) return GISAPR_OK;
+  const int rc = ensure(ctx, ctx->proj_status, sizeof(int), "cudaMalloc(projector status)");
+  if (rc) return rc;
+  GISAPR_CHECK_CUDA(cudaMemset(ctx->proj_status.ptr, 0, sizeof(int)), "cudaMemset(projector status)");
+  return GISAPR_OK;
+}
+
+int gisapr_set_projector_wait(gisapr_ctx ctx, long long attempts) {
+  if (!ctx) return fail(GISAPR_ERR_ARGUMENT, "ctx is NULL");
+  ctx->proj_wait = attempts < 0 ? (1u << 24) : (unsigned)std::min<long long>(attempts, 0xffffffffLL);
+  return GISAPR_OK;
+}
+
+int gisapr_projector_status(gisapr_ctx ctx, void* stream, int* value) {
+  if (!ctx || !value) return fail(GISAPR_ERR_ARGUMENT, "ctx or value is NULL");
+  *value = 0;
+  if (!ctx->proj_status.ptr) return GISAPR_OK;
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  const cudaStream_t st = (cudaStream_t)stream;
+  int h = 0;
+  GISAPR_CHECK_CUDA(cudaMemcpyAsync(&h, ctx->proj_status.ptr, sizeof(int), cudaMemcpyDeviceToHost, st),
+                    "cudaMemcpyAsync(projector status)");
+  GISAPR_CHECK_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+  if (h != 0) {
+    GISAPR_CHECK_CUDA(cudaMemsetAsync(ctx->proj_status.ptr, 0, sizeof(int), st), "cudaMemsetAsync(projector status)");
+    GISAPR_CHECK_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+  }
+  *value = h;
+  return GISAPR_OK;
+}
+
 int gisapr_project_templates(gisapr_ctx ctx, void* stream, const float* spectrum, int box,
                              const float* rot, const int* dirs, int n_build, const int* out_slot,
                              const float* mask, const float* fsc, int newbox, float* bank) {
@@ -511,10 +549,13 @@ int gisapr_project_templates(gisapr_ctx ctx, void* stream, const float* spectrum
     if (rc) return rc;
     rc = ensure(ctx, ctx->proj_blocked, project_blocked_elems(box) * sizeof(float2), "cudaMalloc(blocked spectrum)");
     if (rc) return rc;
+    rc = status_word(ctx);
+    if (rc) return rc;
     GISAPR_CHECK_CUDA(launch_project_templates_fast((cudaStream_t)stream, (const float2*)spectrum, rot, dirs,
                                                     n_build, out_slot, mask, fsc, bt.list, bt.ptr, bt.count,
                                                     bt.n_bins, ctx->tw, (float2*)bank, grid, box, newbox,
-                                                    (float2*)ctx->proj_slices.ptr, (float2*)ctx->proj_blocked.ptr),
+                                                    (float2*)ctx->proj_slices.ptr, (float2*)ctx->proj_blocked.ptr,
+                                                    (int*)ctx->proj_status.ptr, ctx->proj_wait),
                       "project_templates");
     ctx->blocked_box = box;
     return GISAPR_OK;

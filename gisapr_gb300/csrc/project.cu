@@ -55,6 +55,8 @@ struct ProjParams {
   const int* out_slot;      // output row in bank for each build index (null => dirs[i])
   float2* scratch;          // per-CTA scratch
   size_t scratch_stride;    // complex elements per CTA
+  int* status;              // set to 1 when a plane's bulk-copy wait runs out (or null)
+  unsigned wait_limit;      // bound of that wait (attempts)
   const float2* planes;     // pass-A planes written by rows_inverse (or null): [n_build][N][plane_ld(N)]
                             // for the shared-memory path, [n_build][N][N+1] for the general kernel
   int N;
@@ -555,6 +557,7 @@ cudaError_t launch_project_templates(cudaStream_t st, const float2* spectrum, co
                                      int grid, int N, int nb) {
   if (n_build <= 0) return cudaSuccess;
   ProjParams P;
+  P.status = nullptr; P.wait_limit = 0;
   P.spectrum = spectrum; P.rot = rot; P.dirs = dirs; P.n_build = n_build; P.mask = mask;
   P.fsc = fsc; P.bin_list = bin_list; P.bin_ptr = bin_ptr; P.bin_count = bin_count;
   P.n_bins = n_bins; P.tw = tw; P.tw3 = tw3; P.bank = bank; P.out_slot = out_slot; P.scratch = scratch; P.planes = nullptr;
@@ -767,8 +770,8 @@ __device__ __forceinline__ void plane_load(float2* Zs, const float2* src, uint64
         : "memory");
 }
 
-__device__ __forceinline__ bool plane_wait(uint64_t* bar, uint32_t parity) {
-  for (unsigned i = 0; i < kPlaneWaitLimit; ++i) {
+__device__ __forceinline__ bool plane_wait(uint64_t* bar, uint32_t parity, unsigned limit) {
+  for (unsigned i = 0; i < limit; ++i) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -1131,10 +1134,17 @@ __global__ void __launch_bounds__(32 * kSmemWarps, 1) project_templates_smem(Pro
   for (int b = blockIdx.x; b < P.n_build; b += gridDim.x, phase ^= 1u) {
     const int dir = P.dirs[b];
     const int slot = P.out_slot ? P.out_slot[b] : dir;
-    const bool ok = plane_wait(bar, phase);
+    const bool ok = plane_wait(bar, phase, P.wait_limit);
     if (__syncthreads_or(!ok)) {
-      // a plane that never arrived: its template and the remaining ones of
-      // this CTA become NaN, so every score computed from them is NaN
+      // a plane that did not arrive in time: the status word reports it;
+      // the copy still in flight gets the default bound to land before the
+      // CTA's shared memory is released; this template and the remaining
+      // ones of the CTA become NaN, so every score computed from them is NaN
+      if (threadIdx.x == 0) {
+        if (P.status != nullptr) atomicExch(P.status, 1);
+        plane_wait(bar, phase, kPlaneWaitLimit);
+      }
+      __syncthreads();
       const float nan = __int_as_float(0x7fc00000);
       for (int b2 = b; b2 < P.n_build; b2 += gridDim.x) {
         float2* out = P.bank + (size_t)(P.out_slot ? P.out_slot[b2] : P.dirs[b2]) * P.nb * (P.nb / 2 + 1);
@@ -1198,10 +1208,12 @@ cudaError_t launch_project_templates_fast(cudaStream_t st, const float2* spectru
                                           const float* mask, const float* fsc, const int* bin_list,
                                           const int* bin_ptr, const float* bin_count, int n_bins,
                                           const float2* tw, float2* bank, int grid, int N, int nb,
-                                          float2* planes, float2* blocked) {
+                                          float2* planes, float2* blocked, int* status, unsigned wait_limit) {
   if (n_build <= 0) return cudaSuccess;
   if (n_build > 65535) return cudaErrorInvalidValue;
   ProjParams P;
+  P.status = status;
+  P.wait_limit = wait_limit;
   P.spectrum = spectrum; P.rot = rot; P.dirs = dirs; P.n_build = n_build; P.mask = mask;
   P.fsc = fsc; P.bin_list = bin_list; P.bin_ptr = bin_ptr; P.bin_count = bin_count;
   P.n_bins = n_bins; P.tw = tw; P.tw3 = nullptr; P.bank = bank; P.out_slot = out_slot; P.scratch = nullptr;
@@ -1233,6 +1245,7 @@ cudaError_t launch_project_templates_planes(cudaStream_t st, const float2* spect
     if (e != cudaSuccess) return e;
   }
   ProjParams P;
+  P.status = nullptr; P.wait_limit = 0;
   P.spectrum = spectrum; P.rot = rot; P.mask = mask; P.fsc = fsc; P.bin_list = bin_list; P.bin_ptr = bin_ptr;
   P.bin_count = bin_count; P.n_bins = n_bins; P.tw = tw; P.tw3 = tw3; P.bank = bank; P.scratch = scratch;
   P.scratch_stride = project_scratch_elems(N, nb); P.N = N; P.nb = nb; P.planes = planes;

@@ -392,6 +392,19 @@ class ScoringJob:
         return "".join(str(row) + "\n" for row in self.result_records())
 
 
+def projector_check(ctx_handle, stream=None) -> None:
+    """Raise if a shared-memory projector call on this native context gave
+    up waiting for a template plane (those templates are NaN); resets the
+    context's status word. Synchronizes ``stream`` (default: the current
+    stream)."""
+    st = C.c_int(0)
+    s = nat.stream_of(torch.cuda.current_device()) if stream is None else C.c_void_p(stream.cuda_stream)
+    nat.call("gisapr_projector_status", ctx_handle, s, C.byref(st))
+    if st.value != 0:
+        raise RuntimeError("projector: a template plane did not arrive within the wait bound; "
+                           "its templates are NaN")
+
+
 def idx_ptr(a: np.ndarray) -> C.c_void_p:
     """Host address of a contiguous numpy array (for the host-side ABI helpers)."""
     return C.c_void_p(a.ctypes.data)
@@ -615,9 +628,14 @@ class BatchScoringJob:
         return [(c0, min(size, n_active - c0)) for c0 in range(0, n_active, size)]
 
     def check_status(self) -> None:
-        """Raise if an on-chip barrier wait of the tensor-core kernel ran out
-        (status 1) or a scaled template value left the operand type's range
-        (status 2)."""
+        """Raise if a projector plane wait of any template lane ran out (its
+        templates are NaN), an on-chip barrier wait of the tensor-core kernel
+        ran out (status 1) or a scaled template value left the operand
+        type's range (status 2)."""
+        dev = self.job.device
+        for lane_ctx, lane_stream, _ in self.lanes:
+            ctx = lane_ctx if lane_ctx is not None else nat.Context.for_device(dev)
+            projector_check(ctx.handle, lane_stream if lane_stream is not None else self.stream)
         if self.precision == "fp32":
             return
         st = int(self.tc_status.item())

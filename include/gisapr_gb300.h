@@ -138,6 +138,23 @@ int gisapr_project_templates(gisapr_ctx ctx, void* stream, const float* spectrum
                              const float* mask, const float* fsc, int newbox, float* bank);
 
 /*
+ * Failure reporting of the shared-memory projector (boxes 32, 64, 128): each
+ * template's plane arrives in shared memory by bulk copies whose wait is
+ * bounded. When a wait runs out, the CTA sets the context's projector
+ * status word to 1, lets its copy land, writes NaN into the templates it
+ * still had to build and returns, so scores computed from them are NaN.
+ * gisapr_projector_status copies the word into *value (0 when no
+ * projector call ran), resets it to 0 and synchronizes ``stream`` (the
+ * stream the projector calls ran on). gisapr_set_projector_wait sets the
+ * bound for later calls on the context: attempts < 0 restores the default
+ * (2^24), 0 makes the wait give up at once (a way to exercise the failure
+ * path without a fault). Neither has a counterpart in the reference, whose
+ * projector has no bounded waits.
+ */
+int gisapr_projector_status(gisapr_ctx ctx, void* stream, int* value);
+int gisapr_set_projector_wait(gisapr_ctx ctx, long long attempts);
+
+/*
  * Kernel launches one gisapr_project_templates call of ``n_build``
  * templates enqueues at ``box`` (0 for n_build <= 0; -1 for an unsupported
  * box). Host only, no context; lets a caller count its launches or size a

@@ -3,7 +3,7 @@
 Run in a checkout that has the reference sources (they are read, never
 modified):
 
-    python tests/golden/make_golden.py --reference /root/reference
+    python tests/golden/make_golden.py --reference <GisAPR source root>
 
 The reference's optimized-3 tree (GisAPR-210-optimized-3.zip, whose v606
 accepts an in-memory volume) is extracted to a temporary directory and

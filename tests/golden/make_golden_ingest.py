@@ -1,6 +1,6 @@
 """Generate golden_ingest.npz by running the reference's particle preparation.
 
-    python tests/golden/make_golden_ingest.py --reference /root/reference
+    python tests/golden/make_golden_ingest.py --reference <GisAPR source root>
 
 read_star_shift_crop_and_generate_new_star_v5.py (read, never modified) is
 copied to a temporary directory and imported with stub ``starfile`` and

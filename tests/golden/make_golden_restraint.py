@@ -1,6 +1,6 @@
 """Generate golden_restraint.npz by running the reference's geometric restraint.
 
-    python tests/golden/make_golden_restraint.py --reference /root/reference
+    python tests/golden/make_golden_restraint.py --reference <GisAPR source root>
 
 The reference's func_check_boundary_for_testing_v8.py with the modules it
 imports (pdb2mrc_gpu_ver_fp32_v3.py, pdb_text.py) is copied to a temporary

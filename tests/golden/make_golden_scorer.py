@@ -1,6 +1,6 @@
 """Generate golden_scorer.npz by running the reference's search-text scorer.
 
-    python tests/golden/make_golden_scorer.py --reference /root/reference
+    python tests/golden/make_golden_scorer.py --reference <GisAPR source root>
 
 new_method_to_fit_the_2nd_Gaussian_PEAK_v4.py (read, never modified) is
 copied to a temporary directory and its run_this scores seeded synthetic

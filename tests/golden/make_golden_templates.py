@@ -2,7 +2,7 @@
 
 Run in a checkout that has the reference sources (read, never modified):
 
-    python tests/golden/make_golden_templates.py --reference /root/reference
+    python tests/golden/make_golden_templates.py --reference <GisAPR source root>
 
 The reference is imported as make_golden.py does (the optimized-3 tree with a
 stub ``mrcfile``). For each box a seeded density (synthetic.blob_density) goes

@@ -68,7 +68,8 @@ def test_cpu_device_is_rejected():
 def test_tensor_core_work_plan_on_host(native_lib):
     """gisapr_tc_plan_work is host code: every (particle, tile of 128 rows)
     appears once, tiles hold whole directions (row = direction * n_cand +
-    candidate) and the list is sorted by the tile's first direction."""
+    candidate) and the list is sorted by the tile's directions
+    (lexicographically), so tiles with the same directions are adjacent."""
     import numpy as np
     from gisapr_gb300 import _native
     lib = _native.load()
@@ -89,7 +90,10 @@ def test_tensor_core_work_plan_on_host(native_lib):
         assert lib.gisapr_tc_plan_work(vp(ptr), vp(idx), 40, n_cand, n_psi, crop, vp(work), want, C.byref(n)) == 0
         pairs = {(int(b), int(t)) for b, t in work[:want]}
         assert len(pairs) == want
-        keys = [int(idx[ptr[b] + (t // groups) * dpt]) for b, t in work[:want]]
+        keys = []
+        for b, t in work[:want]:
+            e = int(ptr[b]) + (int(t) // groups) * dpt
+            keys.append(tuple(int(v) for v in idx[e:min(e + dpt, int(ptr[b + 1]))]))
         assert keys == sorted(keys)
         if want > 1:
             assert lib.gisapr_tc_plan_work(vp(ptr), vp(idx), 40, n_cand, n_psi, crop, vp(work), want - 1,

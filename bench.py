@@ -405,6 +405,7 @@ SERVE_BOXES = ("box96_serve", "box128_5kp", "box192_serve")  # boxes 96 / 128 / 
 SERVE_POOL = 600        # unique particle images per box; jobs draw their particles from these
 SERVE_JOBS = 5          # resident jobs, particles log-uniform over 1,000-20,000
 SERVE_MAX_BATCH = 64
+SERVE_WORKERS = 3
 
 
 def _serve_stream(srv, jids, req_job, req_poses, arrive):
@@ -460,7 +461,8 @@ def run_serving(args, device):
         spec = data.spec
         cfg = JobConfig(box=spec.box, apix=spec.apix, crop=spec.crop, psi_step=spec.psi_step,
                         local_range=spec.local_range, mask_edge=spec.mask_edge, kk=spec.kk)
-        fp = job_footprint_bytes(cfg.box, cfg.new_box, npart, 3, len(data.model_rot), SERVE_MAX_BATCH, "fp16x3")
+        fp = job_footprint_bytes(cfg.box, cfg.new_box, npart, 3, len(data.model_rot), SERVE_MAX_BATCH, "fp16x3",
+                                 contexts=SERVE_WORKERS + 1)  # workers' contexts + a batch's second template lane
         jobs[f"job{k}"] = (cfg, data, spec, fp)
     t_gen = time.perf_counter() - t_gen
     jids = sorted(jobs)
@@ -480,9 +482,9 @@ def run_serving(args, device):
     n_req = args.serve_requests
     out = {"jobs": [f"{jid}: box {jobs[jid][0].box}, {len(jobs[jid][1].records.rot)} particles, "
                     f"{jobs[jid][3] / 1e9:.1f} GB footprint" for jid in jids],
-           "precision": "fp16x3", "max_batch": SERVE_MAX_BATCH, "workers": 3, "drivers": 4,
+           "precision": "fp16x3", "max_batch": SERVE_MAX_BATCH, "workers": SERVE_WORKERS, "drivers": 4,
            "synthetic_data_s": t_gen}
-    with ScoringServer(device, hbm_cap_bytes=150e9, max_batch=SERVE_MAX_BATCH, n_workers=3,
+    with ScoringServer(device, hbm_cap_bytes=150e9, max_batch=SERVE_MAX_BATCH, n_workers=SERVE_WORKERS,
                        precision="fp16x3") as srv:
         for jid in jids:
             srv.register(jid, factory(jid), jobs[jid][3])
@@ -540,7 +542,7 @@ def run_serving(args, device):
     # footprint, so every job fits alone but not all at once
     fps = sorted((jobs[j][3] for j in jids), reverse=True)
     cap = fps[0] + fps[-1]
-    with ScoringServer(device, hbm_cap_bytes=cap, max_batch=SERVE_MAX_BATCH, n_workers=3,
+    with ScoringServer(device, hbm_cap_bytes=cap, max_batch=SERVE_MAX_BATCH, n_workers=SERVE_WORKERS,
                        precision="fp16x3") as srv:
         t0 = time.perf_counter()
         futs = []

@@ -173,7 +173,11 @@ class IntegratedProjector:
         self.packed_fsc = packed_fsc.to(self.device, torch.float32).contiguous()
         self.batch_size = max(1, int(projection_batch_size))
         self._rot_cache = None
-        self.spectrum = None
+        # cuFFT spectrum (boxes 96, 192) per native context: the template
+        # lanes of a batch run the transform and the projector of different
+        # candidates at the same time on their own contexts and streams, so
+        # each context writes and samples its own buffer
+        self._spectra = {}
         # power-of-two boxes transform the density straight into the blocked
         # copy the slice gather reads (gisapr_volume_spectrum_blocked);
         # False keeps the cuFFT spectrum + blocked copy of volume_spectrum
@@ -188,14 +192,21 @@ class IntegratedProjector:
             self._rot_cache = (key, t.reshape(-1, 9).to(self.device))
         return self._rot_cache[1]
 
+    @property
+    def spectrum(self) -> Optional[torch.Tensor]:
+        """The last cuFFT spectrum written on this thread's current context."""
+        return self._spectra.get(nat.Context.for_device(self.device).handle.value)
+
     def volume_spectrum(self, volume: Optional[torch.Tensor]) -> torch.Tensor:
         n = self.original_box
-        if self.spectrum is None:
-            self.spectrum = torch.empty((2 * n, 2 * n, n + 1), dtype=torch.complex64, device=self.device)
-        nat.call("gisapr_volume_spectrum", nat.Context.for_device(self.device).handle,
-                 nat.stream_of(self.device), nat.ptr(volume), n, nat.ptr(self.spectrum))
+        ctx = nat.Context.for_device(self.device).handle
+        spec = self._spectra.get(ctx.value)
+        if spec is None:
+            spec = torch.empty((2 * n, 2 * n, n + 1), dtype=torch.complex64, device=self.device)
+            self._spectra[ctx.value] = spec
+        nat.call("gisapr_volume_spectrum", ctx, nat.stream_of(self.device), nat.ptr(volume), n, nat.ptr(spec))
         self._from_blocked = False
-        return self.spectrum
+        return spec
 
     def volume_spectrum_blocked(self, volume: torch.Tensor) -> None:
         """The density's half-volume spectrum, straight into the context's

@@ -77,9 +77,12 @@ def projector_scratch_bytes(box: int, new_box: int, n_dirs: int, sm_count: int =
 
 
 def job_footprint_bytes(box: int, new_box: int, n_particles: int, n_psi: int, n_dirs: int, max_batch: int,
-                        precision: str = "fp32", local_dirs: int = 64) -> int:
+                        precision: str = "fp32", local_dirs: int = 64, contexts: int = 2) -> int:
     """Upper bound of a job's device memory: resident particle spectra and
-    tables, the per-candidate volume and spectrum buffers, the batch's
+    tables, the per-candidate volume buffers, the padded FFT input and the
+    volume spectrum of every native context that runs the job (``contexts``:
+    the server's workers plus the extra template lanes of a batch; at boxes
+    96 and 192 the projector keeps one spectrum per context), the batch's
     template banks (every model direction counted as needed), its per-map
     outputs (``local_dirs`` directions per particle at most) and the
     projector scratch of a library context (counted once for every job,
@@ -87,7 +90,7 @@ def job_footprint_bytes(box: int, new_box: int, n_particles: int, n_psi: int, n_
     h = new_box // 2 + 1
     spectra = n_particles * n_psi * new_box * h * 8
     tables = n_particles * (new_box * h * 4 + 64) + n_dirs * 64 + 8 * new_box * h * 4
-    volume = (2 * box) ** 3 * 4 + (2 * box) ** 2 * (box + 1) * 8 + box ** 3 * 4 * 2
+    volume = max(1, int(contexts)) * ((2 * box) ** 3 * 4 + (2 * box) ** 2 * (box + 1) * 8) + box ** 3 * 4 * 2
     banks = max_batch * n_dirs * new_box * h * 8
     if precision != "fp32":
         banks += min(max_batch, 128) * n_dirs * new_box * h * 8

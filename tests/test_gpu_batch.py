@@ -65,3 +65,25 @@ def test_batch_mixes_moving_chains_of_different_sizes():
     got = batch.score_batch(poses)
     want = np.asarray([jobs[m].score(p) for m, p in zip(model_of, poses)])
     np.testing.assert_array_equal(got, want)
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_batch_lanes_equal_single_candidates_box96(use_graph):
+    """Box 96 runs the cuFFT volume transform: the batch's two template
+    lanes transform and project different candidates at the same time, each
+    into its own context's spectrum, so every candidate's score and peaks
+    equal the per-candidate path's bit for bit."""
+    spec = syn.WORKLOADS["box96_tiny"]
+    data = syn.make_job(spec, seed=5, n_particles=24)
+    job = ScoringJob(_cfg(spec), data.model.pdb_text, model_angles_from_lists(data.model_rot, data.model_tilt),
+                     records_from_job(data), data.images, fsc_values=data.fsc, device=DEV)
+    poses = list(syn.candidate_poses(12, 21, 5.0, 3.0))
+    single, single_peaks = [], []
+    for p in poses:
+        single.append(job.score(p))
+        single_peaks.append(job.particle_results()["peak"])
+    batch = BatchScoringJob(job, len(poses), use_graph=use_graph, lanes=2)
+    for _ in range(2):
+        got = batch.score_batch(poses)
+        np.testing.assert_array_equal(got, np.asarray(single))
+        np.testing.assert_array_equal(batch.peak.cpu().numpy(), np.stack(single_peaks))

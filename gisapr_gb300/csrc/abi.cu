@@ -81,8 +81,8 @@ size_t correlate_tc_smem_bytes(int n, int crop, int split, int sa, int sb);
 bool correlate_tc_rings(int n, int crop, int split, int want_sa, int want_sb, int* sa, int* sb);
 long long correlate_tc_bank_halves(int n_slot, int n);
 int correlate_tc_plan(const int*, const int*, int, int, int, int, int*, int);
-cudaError_t launch_bank_to_operands(cudaStream_t, const float2*, long long, int, int, int, int, const float*, void*,
-                                    int*);
+cudaError_t launch_bank_to_operands(cudaStream_t, const float2*, long long, int, int, int, int, int, const float*,
+                                    void*, int*);
 int correlate_tc_max_cand();
 cudaError_t launch_correlate_tc(cudaStream_t, const void*, int, const float2*, const int*, const int*, const int*,
                                 int, int, int, int, int, int, int, const float*, const float*, unsigned,
@@ -806,7 +806,7 @@ int gisapr_correlate_tc_batch_ex(gisapr_ctx ctx, void* stream, const float* bank
   const cudaStream_t st = (cudaStream_t)stream;
   const int bf16 = (precision == GISAPR_TC_BF16 || precision == GISAPR_TC_BF16X3) ? 1 : 0;
   const int split = (precision == GISAPR_TC_FP16X3 || precision == GISAPR_TC_BF16X3) ? 1 : 0;
-  GISAPR_CHECK_CUDA(launch_bank_to_operands(st, (const float2*)bank, bank_stride, n_cand, n_slot, n, bf16,
+  GISAPR_CHECK_CUDA(launch_bank_to_operands(st, (const float2*)bank, bank_stride, n_cand, n_slot, n, bf16, split,
                                             col_scale_t, tbank, status),
                     "bank_to_operands");
   const int grid = std::min(n_work, ctx->sm_count);

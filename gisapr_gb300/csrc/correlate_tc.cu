@@ -775,13 +775,15 @@ __global__ void __launch_bounds__(kTcThreads, 1) correlate_tc(TcParams P) {
 // stored at position c ^ (cand & 7) (the 128-byte swizzle of the
 // shared-memory tile, whose direction blocks start on multiples of 8 rows).
 // One block per (slot, candidate); every candidate writes whole 128-byte
-// rows. A value that leaves the operand type's range sets *status to 2.
+// rows. The lo halves are written for the split forms only (the single
+// forms never read them). A value that leaves the operand type's range sets
+// *status to 2.
 __host__ __device__ inline int bank_fp16_ld(int n) { return n + n / 8 + 1; }
 
 template <bool BF>
 __global__ void bank_to_operands(const float2* __restrict__ bank, long long bank_stride, int n, int n_cand,
                                  int cb, const float* __restrict__ t_scale, unsigned char* __restrict__ out,
-                                 int* status) {
+                                 int split, int* status) {
   // [cb][ld]: columns [c0, c0 + cb) of the template, column-major with a
   // spare slot after every 8 rows, so the 16 row blocks a warp reads at once
   // fall on distinct banks
@@ -816,8 +818,9 @@ __global__ void bank_to_operands(const float2* __restrict__ bank, long long bank
       const size_t row = (((size_t)slot * H + col) * nq + qq) * 2;  // part 0 row block
       const int pos = c ^ (cand & 7);
       *reinterpret_cast<uint4*>(out + ((row * n_cand + cand) * 8 + pos) * 16) = make_uint4(h[0], h[1], h[2], h[3]);
-      *reinterpret_cast<uint4*>(out + (((row + 1) * n_cand + cand) * 8 + pos) * 16) =
-          make_uint4(l[0], l[1], l[2], l[3]);
+      if (split)
+        *reinterpret_cast<uint4*>(out + (((row + 1) * n_cand + cand) * 8 + pos) * 16) =
+            make_uint4(l[0], l[1], l[2], l[3]);
     }
   }
   if (bad && status != nullptr) atomicExch(status, 2);
@@ -942,7 +945,8 @@ int correlate_tc_plan(const int* local_ptr, const int* local_idx, int n_particle
 }
 
 cudaError_t launch_bank_to_operands(cudaStream_t st, const float2* bank, long long bank_stride, int n_cand,
-                                    int n_slot, int n, int bf16, const float* t_scale, void* out, int* status) {
+                                    int n_slot, int n, int bf16, int split, const float* t_scale, void* out,
+                                    int* status) {
   if (n_cand <= 0 || n_slot <= 0) return cudaSuccess;
   // columns per pass of a block: 16 (18.6 KB of shared memory at n = 128)
   // keeps about ten blocks resident per SM, so loads of some blocks overlap
@@ -963,10 +967,10 @@ cudaError_t launch_bank_to_operands(cudaStream_t st, const float2* bank, long lo
   }
   if (bf16)
     bank_to_operands<true><<<dim3(n_slot, n_cand), 256, smem, st>>>(bank, bank_stride, n, n_cand, cb, t_scale,
-                                                                     (unsigned char*)out, status);
+                                                                     (unsigned char*)out, split, status);
   else
     bank_to_operands<false><<<dim3(n_slot, n_cand), 256, smem, st>>>(bank, bank_stride, n, n_cand, cb, t_scale,
-                                                                      (unsigned char*)out, status);
+                                                                      (unsigned char*)out, split, status);
   return cudaGetLastError();
 }
 

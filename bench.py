@@ -74,6 +74,8 @@ def parse_args():
     ap.add_argument("--precision-particles", type=int, default=4000,
                     help="particles of the box-256 precision comparison (0: skip it; 20000 is the full "
                          "configuration, about three minutes of synthetic-data generation)")
+    ap.add_argument("--precision-fp64", type=int, default=100,
+                    help="particles of the precision comparison also evaluated in FP64 (torch float64 on the GPU)")
     ap.add_argument("--serve-requests", type=int, default=40,
                     help="requests in the serving stream (0: skip the serving measurement)")
     ap.add_argument("--precisions", default="fp32,fp16x3,fp16",
@@ -360,12 +362,47 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def fp64_maxima(bank, stack, ptr, idx, n_part, crop):
+    """FP64 maxima of the crop-window maps of the first ``n_part`` particles
+    (torch float64 on the GPU): raw(y, x) = sum_{r,c} w_c Re[T P e^{2 pi i
+    (r y + c x)/n}] on the stored (pre-shifted) arrays, w_c = 1 for c in
+    {0, n/2} else 2 (the closed form of the reference's crop-window irfft2,
+    v606:1437-1449), score = 1024 max raw, first maximum in row-major crop
+    order. Returns per particle (scores [d, n_psi], y, x) or None."""
+    import torch
+    n, h = stack.shape[-2], stack.shape[-1]
+    dev = stack.device
+    off = torch.arange(crop, device=dev, dtype=torch.float64) - crop // 2
+    ey = torch.exp(2j * math.pi * torch.outer(torch.arange(n, device=dev, dtype=torch.float64), off) / n)
+    w = torch.full((h,), 2.0, dtype=torch.float64, device=dev)
+    w[0] = 1.0
+    w[n // 2] = 1.0
+    ex = w[:, None] * torch.exp(2j * math.pi * torch.outer(torch.arange(h, device=dev, dtype=torch.float64), off) / n)
+    out = []
+    for i in range(n_part):
+        a, b = int(ptr[i]), int(ptr[i + 1])
+        if b <= a:
+            out.append(None)
+            continue
+        t = bank[idx[a:b]].to(torch.complex128)                     # [d, n, h]
+        pp = stack[i].to(torch.complex128)                           # [n_psi, n, h]
+        q = t[:, None] * pp[None]                                    # [d, n_psi, n, h]
+        z = torch.einsum("ry,abrc->abyc", ey, q)
+        raw = torch.einsum("abyc,cx->abyx", z, ex).real.reshape(b - a, pp.shape[0], -1)
+        k = torch.argmax(raw, dim=-1)
+        best = torch.gather(raw, -1, k[..., None])[..., 0] * 1024.0
+        out.append((best.cpu().numpy(), (k // crop).cpu().numpy(), (k % crop).cpu().numpy()))
+    return out
+
+
 def run_precision(args, device):
     """Box-256 precision configuration (crop 14, psi step 3.75, local 6 deg)
-    on a small particle set: the tensor-core forms against the plain FP32
-    batched path, per candidate score and per particle argmax (direction,
-    psi, shift). The FP64 comparison of the same forms is in the test suite
-    (tests/test_gpu_tc.py)."""
+    on a particle set: every tensor-core form against the plain FP32 batched
+    path (all particles) and against an FP64 evaluation of the same
+    contraction on the same templates and particle spectra (the first
+    ``args.precision_fp64`` particles): per candidate score and per particle
+    argmax (direction, psi, shift), identical or tied within 1e-5 of the
+    FP64 maxima."""
     import numpy as np
     from gisapr_gb300 import synthetic as syn
     from gisapr_gb300.engine import BatchScoringJob, JobConfig, ScoringJob
@@ -378,26 +415,60 @@ def run_precision(args, device):
     job = ScoringJob(cfg, data.model.pdb_text, model_angles_from_lists(data.model_rot, data.model_tilt),
                      job_records(data), data.images, fsc_values=data.fsc, device=device)
     poses = list(syn.candidate_poses(8, args.seed + 78, 5.0, 3.0))
-    runs = {}
-    for prec in ("fp32", "fp16x3", "fp16"):
+    n64 = min(n_part, args.precision_fp64)
+    ptr = job.local_ptr.cpu().numpy()
+    idx = job.local_idx.cpu().numpy()
+    n_psi = job.n_psi
+    forms = ("fp32", "fp16x3", "bf16x3", "fp16", "bf16")
+    runs, ref64 = {}, None
+    for prec in forms:
         bj = BatchScoringJob(job, len(poses), use_graph=False, precision=prec)
         scores = bj.score_active(poses)
         runs[prec] = (scores, bj.score_buf.cpu().numpy(),
                       np.stack([t.cpu().numpy() for t in (bj.best_entry, bj.best_psi, bj.peak_y, bj.peak_x)], -1),
-                      bj.stage_ms(poses)["correlate"])
+                      bj.stage_ms(poses)["correlate"], bj.peak.cpu().numpy())
+        if prec == "fp32" and n64 > 0:
+            # the same float32 templates and spectra feed every form
+            ref64 = [fp64_maxima(bj.banks[c], job.stack, ptr, idx, n64, cfg.crop) for c in range(len(poses))]
         del bj
-    ref_scores, ref_maps, ref_arg, _ = runs["fp32"]
+    ref_scores, ref_maps, ref_arg, _, _ = runs["fp32"]
     out = {"workload": f"box256_20kp shapes, {n_part} particles, {len(poses)} candidates",
            "box": spec.box, "crop": spec.crop, "directions": len(data.model_rot),
-           "maps_per_candidate": job.nnz * job.n_psi}
-    for prec in ("fp16x3", "fp16"):
-        sc, maps, arg, ms = runs[prec]
-        valid = ref_arg[..., 0] >= 0
-        agree = np.all(arg == ref_arg, axis=-1)[valid]
-        out[prec] = {"score_max_rel_err_vs_fp32": float(np.max(np.abs(sc / ref_scores - 1.0))),
-                     "map_max_err_rel_to_scale": float(np.max(np.abs(maps - ref_maps)) / np.max(np.abs(ref_maps))),
-                     "argmax_agreement_vs_fp32": float(np.mean(agree)),
-                     "correlate_ms": ms, "plain_correlate_ms": runs["fp32"][3]}
+           "maps_per_candidate": job.nnz * job.n_psi,
+           "fp64": f"torch float64 on the GPU, first {n64} particles, same templates and particle spectra"}
+    for prec in forms:
+        sc, maps, arg, ms, peak = runs[prec]
+        entry = {"correlate_ms": ms, "plain_correlate_ms": runs["fp32"][3]}
+        if prec != "fp32":
+            valid = ref_arg[..., 0] >= 0
+            agree = np.all(arg == ref_arg, axis=-1)[valid]
+            entry.update({"score_max_rel_err_vs_fp32": float(np.max(np.abs(sc / ref_scores - 1.0))),
+                          "map_max_err_rel_to_scale": float(np.max(np.abs(maps - ref_maps)) / np.max(np.abs(ref_maps))),
+                          "argmax_agreement_vs_fp32": float(np.mean(agree))})
+        if ref64 is not None:
+            worst, hits, total = 0.0, 0, 0
+            for c in range(len(poses)):
+                want = got = 0.0
+                for i in range(n64):
+                    r = ref64[c][i]
+                    if r is None:
+                        continue
+                    s64, y64, x64 = r
+                    k = int(np.argmax(s64.reshape(-1)))
+                    want += math.exp(float(s64.reshape(-1)[k]) / 1024.0)
+                    got += math.exp(float(peak[c][i]) / 1024.0)
+                    mine = int(arg[c, i, 0] - ptr[i]) * n_psi + int(arg[c, i, 1])
+                    hit = mine == k and int(arg[c, i, 2]) == int(y64.reshape(-1)[k]) and \
+                        int(arg[c, i, 3]) == int(x64.reshape(-1)[k])
+                    if not hit:  # a tie within 1e-5 of the FP64 maxima
+                        hit = abs(float(s64.reshape(-1)[mine]) - float(s64.reshape(-1)[k])) <= \
+                            1e-5 * abs(float(s64.reshape(-1)[k]))
+                    hits += int(hit)
+                    total += 1
+                worst = max(worst, abs(got / want - 1.0))
+            entry.update({"score_max_rel_err_vs_fp64": worst,
+                          "argmax_agreement_vs_fp64": hits / max(1, total)})
+        out[prec] = entry
     return out
 
 

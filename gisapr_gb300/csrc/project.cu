@@ -1051,16 +1051,26 @@ __host__ __device__ constexpr int plane_out_ld() { return flat_plane<N>() ? N + 
 template <int N>
 __host__ __device__ constexpr int ri_cols() { return kRiWarps * pass_a_cols<N>(); }
 
+// Eight CTAs per SM (64 registers, 21 KB of shared memory): the gather is
+// bound by the latency of its scattered loads, and resident warps hide it
+// (measured on GB300 at box 128: 7 CTAs per SM 0.615 ms for the gather and
+// tail of 768 templates, 8 CTAs 0.597 ms, 10 CTAs at 48 registers 0.644 ms;
+// giving the L1 more of the SM's memory at the cost of resident CTAs was
+// slower still).
 template <int N>
-__global__ void __launch_bounds__(kRiWarps * 32) rows_inverse(const float2* __restrict__ spectrum,
+__global__ void __launch_bounds__(kRiWarps * 32, 8) rows_inverse(const float2* __restrict__ spectrum,
                                                               const float* __restrict__ rot,
                                                               const int* __restrict__ dirs,
                                                               const float2* __restrict__ tw_g,
                                                               float2* __restrict__ planes) {
   constexpr int m = 2 * N, W = N + 1, CPR = pass_a_cols<N>(), CC = ri_cols<N>(), LINE = plane_ld(N);
+  constexpr int OUTC = CC + 1;
+  static_assert(N * OUTC <= kRiWarps * 2 * CPR * LINE, "the output tile fits the staging lines");
   __shared__ float2 s_tw[kMaxFftLen / 2];
+  // staging lines of the gather and the FFT; once every warp has its
+  // outputs in registers, the same memory holds the CTA's N x CC output tile
   __shared__ float2 s_line[kRiWarps][2 * CPR][LINE];
-  __shared__ float2 s_out[N][CC + 1];
+  float2(*s_out)[OUTC] = reinterpret_cast<float2(*)[OUTC]>(&s_line[0][0][0]);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int b = blockIdx.y, c_cta = blockIdx.x * CC, cw = c_cta + warp * CPR;
   const int nc = max(0, min(CPR, W - cw));
@@ -1080,13 +1090,30 @@ __global__ void __launch_bounds__(kRiWarps * 32) rows_inverse(const float2* __re
     L[2 * cl + (r & 1)][k + (k >> 3)] = slice_value<N>(spectrum, R, r, cw + cl);
   }
   __syncthreads();
+  constexpr int RES = CPR * N / 32;  // outputs of a lane (8 at every box)
+  float2 res[RES];
   if (nc > 0) {
     warp_fft<N, 1>(StageLines<N>{&L[0][0]}, 2 * nc, s_tw);
-    for (int idx = lane; idx < nc * N; idx += 32) {
-      const int cl = idx / N, k = idx - cl * N;
-      const int u = k < N / 2 ? k : k - N;
-      const int kk = k + (k >> 3);
-      s_out[(k + N / 2) & (N - 1)][warp * CPR + cl] = cadd(L[2 * cl][kk], cmul(tw_pos(s_tw, u, m), L[2 * cl + 1][kk]));
+#pragma unroll
+    for (int i = 0; i < RES; ++i) {
+      const int idx = lane + 32 * i;
+      if (idx < nc * N) {
+        const int cl = idx / N, k = idx - cl * N;
+        const int u = k < N / 2 ? k : k - N;
+        const int kk = k + (k >> 3);
+        res[i] = cadd(L[2 * cl][kk], cmul(tw_pos(s_tw, u, m), L[2 * cl + 1][kk]));
+      }
+    }
+  }
+  __syncthreads();  // every warp has read its lines
+  if (nc > 0) {
+#pragma unroll
+    for (int i = 0; i < RES; ++i) {
+      const int idx = lane + 32 * i;
+      if (idx < nc * N) {
+        const int cl = idx / N, k = idx - cl * N;
+        s_out[(k + N / 2) & (N - 1)][warp * CPR + cl] = res[i];
+      }
     }
   }
   __syncthreads();

@@ -43,12 +43,16 @@ __device__ __forceinline__ void stage_pair(const StageLines<N>& L, int q, int y,
 // x pass: CTA = one z plane and a band of rows; each warp transforms
 // vf_lines/2 rows (two lines per row). Output A1[z][kx][y], kx in [0, N].
 template <int N>
-__global__ void __launch_bounds__(kVfWarps * 32) vfft_x(const float* __restrict__ vol, float2* __restrict__ a1,
-                                                         const float2* __restrict__ tw_g) {
+__global__ void __launch_bounds__(kVfWarps * 32, 8) vfft_x(const float* __restrict__ vol, float2* __restrict__ a1,
+                                                            const float2* __restrict__ tw_g) {
   constexpr int G = vf_lines<N>(), RPW = G / 2, RY = kVfWarps * RPW, m = 2 * N, W = N + 1;
+  constexpr int OUTC = RY + 1, RES = (RPW * W + 31) / 32;
+  static_assert(W * OUTC <= kVfWarps * G * plane_ld(N), "the output tile fits the staging lines");
   __shared__ float2 s_tw[kMaxFftLen / 2];
+  // staging lines; once every warp holds its outputs in registers, the same
+  // memory holds the CTA's output tile
   __shared__ float2 s_line[kVfWarps][G * plane_ld(N)];
-  __shared__ float2 s_out[W][RY + 1];
+  float2(*s_out)[OUTC] = reinterpret_cast<float2(*)[OUTC]>(&s_line[0][0]);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int z = blockIdx.y, y0 = blockIdx.x * RY;
   for (int t = threadIdx.x; t < kMaxFftLen / 2; t += blockDim.x) s_tw[t] = tw_g[t];
@@ -65,9 +69,23 @@ __global__ void __launch_bounds__(kVfWarps * 32) vfft_x(const float* __restrict_
   }
   __syncwarp();
   warp_fft<N, -1>(L, G, s_tw);
-  for (int idx = lane; idx < RPW * W; idx += 32) {
-    const int q = idx / W, k = idx - q * W;
-    s_out[k][warp * RPW + q] = L.at(2 * q + (k & 1), k >> 1);
+  float2 res[RES];
+#pragma unroll
+  for (int i = 0; i < RES; ++i) {
+    const int idx = lane + 32 * i;
+    if (idx < RPW * W) {
+      const int q = idx / W, k = idx - q * W;
+      res[i] = L.at(2 * q + (k & 1), k >> 1);
+    }
+  }
+  __syncthreads();  // every warp has read its lines
+#pragma unroll
+  for (int i = 0; i < RES; ++i) {
+    const int idx = lane + 32 * i;
+    if (idx < RPW * W) {
+      const int q = idx / W, k = idx - q * W;
+      s_out[k][warp * RPW + q] = res[i];
+    }
   }
   __syncthreads();
   for (int idx = threadIdx.x; idx < W * RY; idx += blockDim.x) {
@@ -79,12 +97,17 @@ __global__ void __launch_bounds__(kVfWarps * 32) vfft_x(const float* __restrict_
 // y pass: CTA = one kx and a band of z; lines along y. Output
 // A2[ky][kx][z], ky in [0, 2N) (unshifted).
 template <int N>
-__global__ void __launch_bounds__(kVfWarps * 32) vfft_y(const float2* __restrict__ a1, float2* __restrict__ a2,
-                                                         const float2* __restrict__ tw_g) {
+__global__ void __launch_bounds__(kVfWarps * 32, 8) vfft_y(const float2* __restrict__ a1, float2* __restrict__ a2,
+                                                            const float2* __restrict__ tw_g) {
   constexpr int G = vf_lines<N>(), RPW = G / 2, RZ = kVfWarps * RPW, m = 2 * N, W = N + 1;
+  constexpr int OUTC = RZ + 1, RES = (RPW * m + 31) / 32;
+  constexpr bool kAlias = m * OUTC <= kVfWarps * G * plane_ld(N);  // all boxes but 256
   __shared__ float2 s_tw[kMaxFftLen / 2];
+  // staging lines; once every warp holds its outputs in registers, the same
+  // memory holds the CTA's output tile (a tile of its own where it does not fit)
   __shared__ float2 s_line[kVfWarps][G * plane_ld(N)];
-  __shared__ float2 s_out[m][RZ + 1];
+  __shared__ float2 s_tile[kAlias ? 1 : m][OUTC];
+  float2(*s_out)[OUTC] = kAlias ? reinterpret_cast<float2(*)[OUTC]>(&s_line[0][0]) : s_tile;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int kx = blockIdx.x, z0 = blockIdx.y * RZ;
   for (int t = threadIdx.x; t < kMaxFftLen / 2; t += blockDim.x) s_tw[t] = tw_g[t];
@@ -96,9 +119,19 @@ __global__ void __launch_bounds__(kVfWarps * 32) vfft_y(const float2* __restrict
   }
   __syncwarp();
   warp_fft<N, -1>(L, G, s_tw);
-  for (int idx = lane; idx < RPW * m; idx += 32) {
+  float2 res[RES];
+#pragma unroll
+  for (int i = 0; i < RES; ++i) {
+    const int idx = lane + 32 * i;
     const int q = idx / m, k = idx - q * m;
-    s_out[k][warp * RPW + q] = L.at(2 * q + (k & 1), k >> 1);
+    res[i] = L.at(2 * q + (k & 1), k >> 1);
+  }
+  __syncthreads();  // every warp has read its lines
+#pragma unroll
+  for (int i = 0; i < RES; ++i) {
+    const int idx = lane + 32 * i;
+    const int q = idx / m, k = idx - q * m;
+    s_out[k][warp * RPW + q] = res[i];
   }
   __syncthreads();
   for (int idx = threadIdx.x; idx < m * RZ; idx += blockDim.x) {

@@ -764,8 +764,7 @@ class BatchScoringJob:
         self.subset.copy_(torch.from_numpy(mask))
 
     def set_poses(self, poses) -> None:
-        for c, p in enumerate(poses):
-            self.poses_host[c].copy_(self.models[self.model_of[c]].pose_tensor(p))
+        self.poses_host[:len(poses)].copy_(MovedChainDensity.pose_tensors(poses))
         self.poses_dev.copy_(self.poses_host, non_blocking=True)
 
     def score_active(self, poses, stream=None, subsets=None) -> np.ndarray:
@@ -779,8 +778,7 @@ class BatchScoringJob:
         if subsets is not None:
             self.set_subsets(subsets)
         st = stream if stream is not None else self.stream
-        for c, p in enumerate(poses):
-            self.poses_host[c].copy_(self.models[self.model_of[c]].pose_tensor(p))
+        self.poses_host[:k].copy_(MovedChainDensity.pose_tensors(poses))
         with torch.cuda.stream(st):
             self.poses_dev[:k].copy_(self.poses_host[:k], non_blocking=True)
             self.enqueue(n_active=k)

@@ -163,6 +163,18 @@ def rotation_matrix(pose) -> np.ndarray:
     return Rotation.from_rotvec(np.deg2rad(pose[:3])).as_matrix()
 
 
+def rotation_matrices(poses) -> np.ndarray:
+    """rotation_matrix of every row of a (k, 6) pose array in one call,
+    element for element the same matrices."""
+    from scipy.spatial.transform import Rotation
+    poses = np.asarray(poses, dtype=np.float64)
+    if poses.ndim != 2 or poses.shape[1] != 6 or not np.all(np.isfinite(poses)):
+        raise ValueError("Poses must be a (k, 6) array of finite rotation/translation values")
+    if len(poses) == 0:
+        return np.zeros((0, 3, 3))
+    return Rotation.from_rotvec(np.deg2rad(poses[:, :3])).as_matrix().reshape(-1, 3, 3)
+
+
 def transform_coordinates(coords, pose, pivot=None) -> np.ndarray:
     coords = np.asarray(coords)
     if coords.ndim != 2 or coords.shape[1] != 3 or not len(coords):

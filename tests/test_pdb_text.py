@@ -36,3 +36,21 @@ def test_reader_matches_reference(fx, tmp_path):
             assert p.elements.tolist() == want["elements"], case
             assert p.chains.tolist() == want["chains"], case
             assert p.atom_line_indices.tolist() == want["lines"], case
+
+
+def test_rotation_matrices_equal_the_per_pose_matrices():
+    """The vectorized rotation of a batch of poses gives, element for
+    element, the matrices of the per-pose call (the batch engine copies
+    them to the device as the pose of every slot)."""
+    import numpy as np
+    from gisapr_gb300.pdb_text import rotation_matrices, rotation_matrix
+    rng = np.random.default_rng(11)
+    poses = np.concatenate([rng.uniform(-180, 180, (40, 3)), rng.uniform(-5, 5, (40, 3))], axis=1)
+    poses[0, :3] = 0.0
+    got = rotation_matrices(poses)
+    for p, m in zip(poses, got):
+        assert np.array_equal(m, rotation_matrix(p))
+    assert rotation_matrices(np.zeros((0, 6))).shape == (0, 3, 3)
+    import pytest
+    with pytest.raises(ValueError):
+        rotation_matrices(np.full((2, 6), np.nan))

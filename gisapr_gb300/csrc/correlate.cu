@@ -198,63 +198,54 @@ __global__ void __launch_bounds__(kThreads) correlate_plain(CorrParams P) {
   }
 }
 
-// One warp per particle: first maximum over (local direction, psi), the
-// population mean and sigma of all its scores (FP64 sums), and the z-score.
-// A particle the candidate does not score (subset) gets the record of a
-// particle without directions.
+// One thread per particle: first maximum over (local direction, psi), the
+// population mean and sigma of all its scores (FP64 sums in entry order),
+// and the z-score. A particle has a few dozen scores at most, so a thread
+// walks them itself (one warp per particle ran 32 times as many warps, most
+// of their time in shuffle trees). A particle the candidate does not score
+// (subset) gets the record of a particle without directions.
 __global__ void particle_results(const int* __restrict__ local_ptr, const float* __restrict__ score,
                                  const int* __restrict__ ys, const int* __restrict__ xs, int n_particles,
                                  int n_psi, const unsigned char* __restrict__ subset, int* __restrict__ best_entry,
                                  int* __restrict__ best_psi, float* __restrict__ peak, int* __restrict__ peak_y,
                                  int* __restrict__ peak_x, float* __restrict__ zscore) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (warp >= n_particles) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_particles) return;
   {  // candidate blockIdx.y: its scores follow the previous candidates'
     const int nnz = local_ptr[n_particles];
     const size_t so = (size_t)blockIdx.y * nnz * n_psi, po = (size_t)blockIdx.y * n_particles;
     score += so; ys += so; xs += so;
     best_entry += po; best_psi += po; peak += po; peak_y += po; peak_x += po; zscore += po;
   }
-  const bool scored = subset == nullptr || subset[(size_t)blockIdx.y * n_particles + warp] != 0;
-  const int e0 = local_ptr[warp], cnt = scored ? (local_ptr[warp + 1] - e0) * n_psi : 0;
+  const bool scored = subset == nullptr || subset[(size_t)blockIdx.y * n_particles + i] != 0;
+  const int e0 = local_ptr[i], cnt = scored ? (local_ptr[i + 1] - e0) * n_psi : 0;
   if (cnt <= 0) {
-    if (lane == 0) {
-      best_entry[warp] = -1; best_psi[warp] = -1; peak[warp] = 0.f;
-      peak_y[warp] = 0; peak_x[warp] = 0; zscore[warp] = 0.f;
-    }
+    best_entry[i] = -1; best_psi[i] = -1; peak[i] = 0.f;
+    peak_y[i] = 0; peak_x[i] = 0; zscore[i] = 0.f;
     return;
   }
   const float* s = score + (size_t)e0 * n_psi;
   float best = -INFINITY;
-  int bi = cnt;
+  int bi = 0;
   double sum = 0.0;
-  for (int e = lane; e < cnt; e += 32) {
+  for (int e = 0; e < cnt; ++e) {
     const float v = s[e];
     sum += (double)v;
     if (v > best) { best = v; bi = e; }
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    const float ov = __shfl_xor_sync(0xffffffffu, best, o);
-    const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-    if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
-  }
-  sum = warp_sum_d(sum);
   const double mean = sum / cnt;
   double var = 0.0;
-  for (int e = lane; e < cnt; e += 32) {
+  for (int e = 0; e < cnt; ++e) {
     const double dv = (double)s[e] - mean;
     var += dv * dv;
   }
-  var = warp_sum_d(var);
-  if (lane == 0) {
-    const double sd = sqrt(var / cnt);
-    best_entry[warp] = e0 + bi / n_psi;
-    best_psi[warp] = bi % n_psi;
-    peak[warp] = best;
-    peak_y[warp] = ys[(size_t)e0 * n_psi + bi];
-    peak_x[warp] = xs[(size_t)e0 * n_psi + bi];
-    zscore[warp] = (float)(((double)best - mean) / sd);
-  }
+  const double sd = sqrt(var / cnt);
+  best_entry[i] = e0 + bi / n_psi;
+  best_psi[i] = bi % n_psi;
+  peak[i] = best;
+  peak_y[i] = ys[(size_t)e0 * n_psi + bi];
+  peak_x[i] = xs[(size_t)e0 * n_psi + bi];
+  zscore[i] = (float)(((double)best - mean) / sd);
 }
 
 // sum over particles with at least one direction of exp(peak / 1024), FP64,
@@ -365,8 +356,8 @@ cudaError_t launch_particle_results(cudaStream_t st, const int* local_ptr, const
                                     int* best_entry, int* best_psi, float* peak, int* peak_y,
                                     int* peak_x, float* zscore, int n_cand, const unsigned char* subset) {
   if (n_particles <= 0 || n_cand <= 0) return cudaSuccess;
-  const int threads = 256, warps = threads / 32;
-  particle_results<<<dim3((n_particles + warps - 1) / warps, n_cand), threads, 0, st>>>(
+  const int threads = 128;
+  particle_results<<<dim3((n_particles + threads - 1) / threads, n_cand), threads, 0, st>>>(
       local_ptr, score, ys, xs, n_particles, n_psi, subset, best_entry, best_psi, peak, peak_y, peak_x, zscore);
   return cudaGetLastError();
 }

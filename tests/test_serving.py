@@ -115,6 +115,16 @@ def test_footprint_estimate_counts_spectra_and_banks():
     assert job_footprint_bytes(128, 128, 10000, 3, 768, 64) > base
 
 
+def test_footprint_counts_one_spectrum_per_context():
+    """Every native context that runs a job (the server's workers and a
+    batch's extra template lanes) holds its own padded FFT input and volume
+    spectrum of the job's box."""
+    per_context = (2 * 96) ** 3 * 4 + (2 * 96) ** 2 * 97 * 8
+    one = job_footprint_bytes(96, 96, 2000, 3, 768, 64, contexts=1)
+    assert job_footprint_bytes(96, 96, 2000, 3, 768, 64, contexts=4) - one == 3 * per_context
+    assert job_footprint_bytes(96, 96, 2000, 3, 768, 64) - one == per_context  # default: two template lanes
+
+
 def test_footprint_counts_projector_scratch():
     from gisapr_gb300.serving import CONTEXT_GROWTH_BOUND as G, projector_scratch_bytes
     # a context's buffers grow by doubling and keep their predecessors: the

@@ -126,3 +126,13 @@ def test_projector_launch_counts_on_host(native_lib):
     assert ScoringJob.projector_launches(256, 8192) == 5
     with pytest.raises(ValueError):
         ScoringJob.projector_launches(80, 1)
+
+
+def test_projector_status_calls_check_their_arguments(native_lib):
+    """The projector's status query and wait bound reject a NULL context or
+    output pointer on the host."""
+    from gisapr_gb300 import _native
+    lib = _native.load()
+    v = C.c_int(7)
+    assert lib.gisapr_projector_status(None, None, C.byref(v)) == 1
+    assert lib.gisapr_set_projector_wait(None, C.c_longlong(0)) == 1

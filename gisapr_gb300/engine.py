@@ -144,6 +144,10 @@ class ScoringJob:
         # as a CUDA graph on the second call and replayed after that
         self.use_graph = True
         self._graphs: Dict[int, tuple] = {}
+        # score() and score_volume() write the job's device buffers (density,
+        # bank, maps, records, total): calls from several host threads take
+        # turns, as the reference's worker serialises requests under a lock
+        self._call_lock = threading.RLock()
         self._warm: Dict[int, int] = {}
         self.total_host = torch.zeros(1, dtype=torch.float64).pin_memory()
         torch.cuda.synchronize(dev)
@@ -308,7 +312,12 @@ class ScoringJob:
 
     def score(self, pose) -> float:
         """sum_i exp(rawCC_i / 1024) of one pose (degrees, Angstrom)."""
-        self.pose_host.copy_(self.density.pose_tensor(pose))
+        t = self.density.pose_tensor(pose)
+        with self._call_lock:
+            return self._score(t)
+
+    def _score(self, pose_tensor: torch.Tensor) -> float:
+        self.pose_host.copy_(pose_tensor)
         self.pose_dev.copy_(self.pose_host, non_blocking=True)
         g = self._score_graph()
         if g is not None:
@@ -353,10 +362,11 @@ class ScoringJob:
         if not torch.is_tensor(volume):
             volume = torch.from_numpy(np.ascontiguousarray(volume, dtype=np.float32))
         volume = volume.to(self.device, torch.float32)
-        self.enqueue_volume(volume)
-        self.total_host.copy_(self.total, non_blocking=True)
-        torch.cuda.current_stream(self.device).synchronize()
-        return float(self.total_host[0])
+        with self._call_lock:
+            self.enqueue_volume(volume)
+            self.total_host.copy_(self.total, non_blocking=True)
+            torch.cuda.current_stream(self.device).synchronize()
+            return float(self.total_host[0])
 
     # ------------------------------------------------------------------
     def particle_results(self) -> Dict[str, np.ndarray]:
@@ -775,17 +785,21 @@ class BatchScoringJob:
         k = len(poses)
         if not 0 < k <= self.n_cand:
             raise ValueError(f"expected 1..{self.n_cand} poses, got {k}")
-        if subsets is not None:
-            self.set_subsets(subsets)
-        st = stream if stream is not None else self.stream
-        self.poses_host[:k].copy_(MovedChainDensity.pose_tensors(poses))
-        with torch.cuda.stream(st):
-            self.poses_dev[:k].copy_(self.poses_host[:k], non_blocking=True)
-            self.enqueue(n_active=k)
-            self.totals_host[:k].copy_(self.totals[:k], non_blocking=True)
-        st.synchronize()
-        self.check_status()
-        return self.totals_host[:k].numpy().copy()
+        t = MovedChainDensity.pose_tensors(poses)
+        # the batch shares the job's density buffer and spectra with the
+        # job's own score(): calls on one job take turns
+        with self.job._call_lock:
+            if subsets is not None:
+                self.set_subsets(subsets)
+            st = stream if stream is not None else self.stream
+            self.poses_host[:k].copy_(t)
+            with torch.cuda.stream(st):
+                self.poses_dev[:k].copy_(self.poses_host[:k], non_blocking=True)
+                self.enqueue(n_active=k)
+                self.totals_host[:k].copy_(self.totals[:k], non_blocking=True)
+            st.synchronize()
+            self.check_status()
+            return self.totals_host[:k].numpy().copy()
 
     def slot_results(self, n_slots: Optional[int] = None) -> List[Dict[str, np.ndarray]]:
         """Per-particle arrays of each of the first n_slots slots of the last batch."""
@@ -805,12 +819,13 @@ class BatchScoringJob:
         (``subsets``: set_subsets first when given)."""
         if len(poses) != self.n_cand:
             raise ValueError(f"expected {self.n_cand} poses, got {len(poses)}")
-        if subsets is not None:
-            self.set_subsets(subsets)
-        self._ensure_graph()
-        self.set_poses(poses)
-        self.run()
-        self.totals_host.copy_(self.totals, non_blocking=True)
-        torch.cuda.current_stream(self.job.device).synchronize()
-        self.check_status()
-        return self.totals_host.numpy().copy()
+        with self.job._call_lock:  # shared buffers with the job's score(), as in score_active
+            if subsets is not None:
+                self.set_subsets(subsets)
+            self._ensure_graph()
+            self.set_poses(poses)
+            self.run()
+            self.totals_host.copy_(self.totals, non_blocking=True)
+            torch.cuda.current_stream(self.job.device).synchronize()
+            self.check_status()
+            return self.totals_host.numpy().copy()

@@ -326,7 +326,13 @@ class ScoringJob:
             self.enqueue(self.pose_dev)
         self.total_host.copy_(self.total, non_blocking=True)
         torch.cuda.current_stream(self.device).synchronize()
+        self._check_projector()
         return float(self.total_host[0])
+
+    def _check_projector(self) -> None:
+        """Raise if this call's projector gave up waiting for a template
+        plane (the stream is idle here: one 4-byte read)."""
+        projector_check(nat.Context.for_device(self.device).handle, torch.cuda.current_stream(self.device))
 
     def _score_graph(self):
         """The captured launch sequence of score() for this host thread, or
@@ -366,6 +372,7 @@ class ScoringJob:
             self.enqueue_volume(volume)
             self.total_host.copy_(self.total, non_blocking=True)
             torch.cuda.current_stream(self.device).synchronize()
+            self._check_projector()
             return float(self.total_host[0])
 
     # ------------------------------------------------------------------

@@ -67,3 +67,28 @@ def test_projector_wait_bound_reports_and_recovers(golden32):
         assert _status(ctx) == 0
         projector_check(ctx.handle)
     np.testing.assert_array_equal(again, base)
+
+
+def test_scoring_job_raises_when_the_projector_gives_up(golden32):
+    """ScoringJob.score reads the status word after each call: a projector
+    that gave up raises instead of returning a score over NaN templates, and
+    the next call with the default bound returns the earlier score bitwise."""
+    from gisapr_gb300.engine import JobConfig, ScoringJob
+    from gisapr_gb300 import synthetic as syn
+    from tests.helpers import records_from_golden
+    g = golden32
+    spec = syn.WORKLOADS["box32_tiny"]
+    cfg = JobConfig(box=32, apix=3.0, crop=spec.crop, psi_step=spec.psi_step, local_range=spec.local_range,
+                    mask_edge=spec.mask_edge, kk=spec.kk)
+    job = ScoringJob(cfg, str(g["pdb_text"]), model_angles_from_lists(g["model_rot"], g["model_tilt"]),
+                     records_from_golden(g), g["images"], fsc_values=g["fsc"], device=DEV)
+    job.use_graph = False
+    base = job.score(g["pose"])
+    ctx = nat.Context.for_device(DEV)
+    nat.call("gisapr_set_projector_wait", ctx.handle, 0)
+    try:
+        with pytest.raises(RuntimeError, match="projector"):
+            job.score(g["pose"])
+    finally:
+        nat.call("gisapr_set_projector_wait", ctx.handle, -1)
+    assert job.score(g["pose"]) == base

@@ -255,7 +255,8 @@ def load_peaks():
 
 
 def profiled_traffic(kernel: str, workload: str):
-    """DRAM bytes per launch of ``kernel`` from the committed ncu summary."""
+    """DRAM bytes per launch of ``kernel`` from the committed ncu summary, at
+    the workload's own particle count (a run with another count has none)."""
     p = ROOT / "profiles" / "traffic.json"
     if not p.exists():
         return None
@@ -764,9 +765,10 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
     corr_s = stage_ms["correlate"] / 1e3
     dominant = max(stage_ms, key=stage_ms.get)
     achieved = flops / corr_s / 1e12
+    traffic = profiled_traffic("correlate_plain", args.workload) if not args.particles else None
     roofline = {
         "kernel": "correlate_plain", "bound": "tensor", "achieved": achieved, "peak": bf16_peak,
-        "unit": "TFLOP/s", "frac": achieved / bf16_peak, "traffic": profiled_traffic("correlate_plain", args.workload),
+        "unit": "TFLOP/s", "frac": achieved / bf16_peak, "traffic": traffic,
         "peak_source": f"{peak_kind} bf16 dense (MEASURED_PEAKS.json)" if peak_kind == "measured" else "fallback",
         "algorithmic": f"{flops:.4g} flop per launch = {maps} maps x (6K + 2.5 n^2 log2 n^2), n={cfg.new_box}",
         "note": "plain FP32 correlation runs on CUDA cores; its fraction is against the bf16 tensor peak",

@@ -1056,7 +1056,8 @@ __host__ __device__ constexpr int ri_cols() { return kRiWarps * pass_a_cols<N>()
 // (measured on GB300 at box 128: 7 CTAs per SM 0.615 ms for the gather and
 // tail of 768 templates, 8 CTAs 0.597 ms, 9 CTAs at 56 registers the same,
 // 10 CTAs at 48 registers 0.644 ms; giving the L1 more of the SM's memory at
-// the cost of resident CTAs was slower still).
+// the cost of resident CTAs was slower still). Streaming (evict-first) stores
+// of the planes, to keep the blocked spectrum in L2, measured the same.
 template <int N>
 __global__ void __launch_bounds__(kRiWarps * 32, 8) rows_inverse(const float2* __restrict__ spectrum,
                                                               const float* __restrict__ rot,

@@ -4,7 +4,7 @@ particle subset: every tensor-core form and the plain FP32 form against an
 FP64 evaluation of the same contraction (the oracle's closed form of the
 reference's crop-window irfft2, on the job's own float32 templates and
 particle spectra), so the comparison isolates the contraction's
-arithmetic. Bars (the benchmark spec): candidate score within 1e-4 relative and the
+arithmetic. Bars: candidate score within 1e-4 relative and the
 per-particle argmax (direction, psi, y, x) identical or tied within 1e-5 on
 at least 99.9% of particles."""
 import numpy as np

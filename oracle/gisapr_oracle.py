@@ -1,6 +1,6 @@
 """CPU oracle for GisAPR's candidate-scoring path -- TEST INFRASTRUCTURE ONLY.
 
-This module is the checker, never the product. Only ``tests/``,
+This module checks the product and is never part of it. Only ``tests/``,
 ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` may import
 it. The ``gisapr_gb300`` package never imports it and has no CPU fallback.
 

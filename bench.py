@@ -88,50 +88,105 @@ def parse_args():
 # ---------------------------------------------------------------------------
 
 class ClockSampler:
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    """nvidia-smi samples of SM clock and throttle reasons every INTERVAL_MS
+    while the run's timed regions execute. ``start`` returns once sampling
+    is live; ``begin``/``end`` bracket each timed region (called after a
+    device synchronize on both sides); ``stop`` keeps the samples whose
+    timestamps fall inside a region. A region shorter than the interval may
+    hold none: if no region holds any, the first sample within one interval
+    after each region stands in for it."""
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    REASONS = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+    INTERVAL_MS = 50
 
-    def __init__(self, gpu_index: int):
+    def __init__(self, gpu_index: int, exe: str = "nvidia-smi"):
         self.gpu = gpu_index
+        self.exe = exe
         self.proc = None
         self.path = None
+        self.windows = []  # (t0, t1) host wall-clock seconds of each timed region
+        self._t0 = None
 
-    def start(self):
+    def start(self, wait_s: float = 5.0):
         fd, self.path = tempfile.mkstemp(suffix=".csv")
         os.close(fd)
         try:
-            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
-                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            with open(self.path, "w") as out:
+                self.proc = subprocess.Popen([self.exe, "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                              "--format=csv,noheader,nounits", "-lms", str(self.INTERVAL_MS)],
+                                             stdout=out, stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
+            return
+        import atexit
+        atexit.register(self._terminate)
+        deadline = time.time() + wait_s
+        while time.time() < deadline and self.proc.poll() is None and os.path.getsize(self.path) == 0:
+            time.sleep(0.01)
+
+    def begin(self):
+        self._t0 = time.time()
+
+    def end(self):
+        if self._t0 is not None:
+            self.windows.append((self._t0, time.time()))
+        self._t0 = None
+
+    def _terminate(self):
+        if self.proc is not None and self.proc.poll() is None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    @staticmethod
+    def _when(stamp: str):
+        import datetime
+        for fmt in ("%Y/%m/%d %H:%M:%S.%f", "%Y/%m/%d %H:%M:%S"):
+            try:
+                return datetime.datetime.strptime(stamp, fmt).timestamp()
+            except ValueError:
+                pass
+        return None
+
+    def _samples(self):
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 10:
+                continue
+            try:
+                sm, smax = float(parts[2]), float(parts[3])
+            except ValueError:
+                continue
+            active = {nm for nm, v in zip(self.REASONS, parts[6:10]) if v.lower() == "active"}
+            rows.append((self._when(parts[0]), sm, smax, active))
+        return rows
 
     def stop(self):
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=5)
-        except subprocess.TimeoutExpired:
-            self.proc.kill()
-        sm, smax, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in open(self.path):
-            parts = [p.strip() for p in line.split(",")]
-            if len(parts) < 9:
-                continue
-            try:
-                sm.append(float(parts[1]))
-                smax.append(float(parts[2]))
-            except ValueError:
-                continue
-            for nm, v in zip(names, parts[5:9]):
-                if v.lower() == "active":
-                    reasons.add(nm)
+        self._terminate()
+        rows = self._samples()
         os.unlink(self.path)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+        dt = self.INTERVAL_MS / 1e3
+        if rows and all(r[0] is not None for r in rows) and self.windows:
+            inside = [r for r in rows if any(t0 <= r[0] <= t1 for t0, t1 in self.windows)]
+            span = "samples inside the timed regions"
+            if not inside:
+                inside = [r for r in rows if any(t1 < r[0] <= t1 + dt for _, t1 in self.windows)]
+                span = "no sample inside the timed regions: the first sample within one interval after each"
+        else:
+            inside, span = rows, "timestamps unavailable: every sample of the run"
+        sm = [r[1] for r in inside]
+        reasons = set().union(*(r[3] for r in inside)) if inside else set()
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(r[2] for r in inside) if inside else None,
+                "reasons": sorted(reasons), "samples": len(sm), "interval_ms": self.INTERVAL_MS,
+                "regions": len(self.windows), "span": span}
 
 
 # ---------------------------------------------------------------------------
@@ -163,10 +218,11 @@ def job_records(job):
                            float(r.defocus_angle[i])) for i in range(len(r.rot))]
 
 
-def run_batched(job, dens, gen, precision, n_batch, K, W, device, barrier, tc_chunk=128, lanes=2):
+def run_batched(job, dens, gen, precision, n_batch, K, W, device, barrier, tc_chunk=128, lanes=2, clocks=None):
     """Time K graph-replayed generations of n_batch candidates (device events on
     the batch stream), then K end-to-end generations (poses from the host,
-    scores and per-particle peaks back)."""
+    scores and per-particle peaks back). ``clocks`` (a running ClockSampler)
+    gets both timed regions."""
     import torch
     from gisapr_gb300.engine import BatchScoringJob
     model_of = [i % len(dens) for i in range(n_batch)]
@@ -176,6 +232,8 @@ def run_batched(job, dens, gen, precision, n_batch, K, W, device, barrier, tc_ch
         bj.score_batch(gen[k])
     barrier()
     torch.cuda.synchronize(device)
+    if clocks is not None:
+        clocks.begin()
     b0 = torch.cuda.Event(enable_timing=True)
     b1 = torch.cuda.Event(enable_timing=True)
     b_steps = []
@@ -189,6 +247,8 @@ def run_batched(job, dens, gen, precision, n_batch, K, W, device, barrier, tc_ch
             bj.run()
         b1.record()
     torch.cuda.synchronize(device)
+    if clocks is not None:
+        clocks.end()
     barrier()
     bj.check_status()
     b_elapsed = b0.elapsed_time(b1) / 1e3
@@ -197,12 +257,16 @@ def run_batched(job, dens, gen, precision, n_batch, K, W, device, barrier, tc_ch
     bpeaks_host = torch.empty(tuple(bj.peak.shape), dtype=torch.float32).pin_memory()
     e2 = torch.cuda.Event(enable_timing=True)
     e3 = torch.cuda.Event(enable_timing=True)
+    if clocks is not None:
+        clocks.begin()
     e2.record()
     for k in range(K):
         bj.score_batch(gen[W + k])
         bpeaks_host.copy_(bj.peak, non_blocking=True)
     e3.record()
     torch.cuda.synchronize(device)
+    if clocks is not None:
+        clocks.end()
     b_e2e = e2.elapsed_time(e3) / 1e3
     stages = bj.stage_ms(gen[W])
     extra = {}
@@ -675,6 +739,7 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
     barrier()
     torch.cuda.synchronize(device)
     clocks.start()
+    clocks.begin()
     start = torch.cuda.Event(enable_timing=True)
     end = torch.cuda.Event(enable_timing=True)
     start.record()
@@ -685,8 +750,8 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
         job.enqueue(pose_dev[W + k], stage_events=stage_events)
     end.record()
     torch.cuda.synchronize(device)
+    clocks.end()
     barrier()
-    clk = clocks.stop()
     elapsed = start.elapsed_time(end) / 1e3
     step_ev.append(end)
     lat = sorted(step_ev[i].elapsed_time(step_ev[i + 1]) for i in range(K))
@@ -699,6 +764,7 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
         job.score(poses[0])
     barrier()
     torch.cuda.synchronize(device)
+    clocks.begin()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record()
@@ -708,6 +774,7 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
         peaks_host.copy_(job.peak, non_blocking=True)
     e1.record()
     torch.cuda.synchronize(device)
+    clocks.end()
     barrier()
     e2e_elapsed = e0.elapsed_time(e1) / 1e3
 
@@ -735,8 +802,9 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
         for precision in args.precisions.split(","):
             batched[precision] = run_batched(job, dens, gen, precision, args.batch, K, W, device, barrier,
                                              tc_chunk=tuned.tc_chunk if tuned else 128,
-                                             lanes=tuned.template_lanes if tuned else 2)
+                                             lanes=tuned.template_lanes if tuned else 2, clocks=clocks)
             batched[precision]["autotune"] = autotune
+    clk = clocks.stop()  # samples inside the timed regions above (plain, end to end, batched)
     tl = [elapsed, e2e_elapsed]
     for b in batched.values():
         tl += [b["elapsed_s"], b["e2e_elapsed_s"]]

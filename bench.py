@@ -93,8 +93,8 @@ class ClockSampler:
     is live; ``begin``/``end`` bracket each timed region (called after a
     device synchronize on both sides); ``stop`` keeps the samples whose
     timestamps fall inside a region. A region shorter than the interval may
-    hold none: if no region holds any, the first sample within one interval
-    after each region stands in for it."""
+    hold none: if no region holds any, the samples within two intervals
+    after each region stand in for it."""
     FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -177,8 +177,8 @@ class ClockSampler:
             inside = [r for r in rows if any(t0 <= r[0] <= t1 for t0, t1 in self.windows)]
             span = "samples inside the timed regions"
             if not inside:
-                inside = [r for r in rows if any(t1 < r[0] <= t1 + dt for _, t1 in self.windows)]
-                span = "no sample inside the timed regions: the first sample within one interval after each"
+                inside = [r for r in rows if any(t1 < r[0] <= t1 + 2 * dt for _, t1 in self.windows)]
+                span = "no sample inside the timed regions: the samples within two intervals after each"
         else:
             inside, span = rows, "timestamps unavailable: every sample of the run"
         sm = [r[1] for r in inside]

@@ -419,7 +419,7 @@ def run_reference(args):
                                   "templates": int(info["n_templates"]), "particles": n_p,
                                   "note": f"each step runs {len(sample)} of the {n_p} particles; the candidate "
                                           f"rate extrapolates the per-particle time to all {n_p}"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": int(threads), "kind": kind,
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": int(threads), "kind": kind, **host_cpu(),
                          "sample": f"{what}; per step one pose: density, {int(info['n_templates'])} templates "
                                    f"and {len(sample)} of {n_p} particles, particle time scaled to all {n_p}"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -892,6 +892,27 @@ def run_gb300(args, rank: int, world: int, local_rank: int):
     print(json.dumps(line), flush=True)
 
 
+def host_cpu() -> dict:
+    """The host's CPU model (lscpu, else /proc/cpuinfo, else the machine
+    type) and its logical core count, stated beside every CPU timing."""
+    import platform
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        model = next((ln.split(":", 1)[1].strip() for ln in out.splitlines()
+                      if ln.lower().startswith("model name:")), None)
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if not model:
+        try:
+            with open("/proc/cpuinfo") as fh:
+                model = next((ln.split(":", 1)[1].strip() for ln in fh
+                              if ln.lower().startswith(("model name", "hardware"))), None)
+        except OSError:
+            pass
+    return {"cpu_model": model or platform.machine(), "nproc": os.cpu_count()}
+
+
 def run_cpu_baseline(spec, data, pose, sample: int) -> dict:
     """The reference's own CPU path on this job (one pose, 100 particles;
     about 10 s of CPU work), or the numpy port when baseline/_ref is absent."""
@@ -908,9 +929,10 @@ def run_cpu_baseline(spec, data, pose, sample: int) -> dict:
         return {"value": 1.0 / sec, "unit": UNIT, "cores": runner.threads, "kind": "reference",
                 "sample": f"GisAPR's own CPU torch path from baseline/_ref, one pose: density, "
                           f"{int(r['n_templates'])} templates, {len(idx)} of {n_p} particles "
-                          f"(particle time scaled to all {n_p}; {wall:.1f} s of CPU work)"}
+                          f"(particle time scaled to all {n_p}; {wall:.1f} s of CPU work)", **host_cpu()}
     cb = cpu_baseline(spec, data, pose, sample)
     return {"value": 1.0 / cb["seconds_per_candidate"], "unit": UNIT, "cores": int(cb["threads"]), "kind": "port",
+            **host_cpu(),
             "sample": f"numpy port of the reference's CPU path (baseline/_ref absent), one pose: full "
                       f"moving-chain splat and 3-D FFT, {int(cb['sample_templates'])} templates timed "
                       f"(extrapolated to the {int(cb['n_templates'])} needed), {int(cb['sample_particles'])} of "

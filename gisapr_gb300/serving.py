@@ -191,9 +191,14 @@ class ScoringServer:
             self._lock.notify_all()
 
     def retire(self, job_id: str) -> None:
-        """Free the job's memory once its queued requests are done."""
+        """Free the job's memory once its queued requests are done. A job
+        not yet admitted keeps its place in the admission order while it
+        has queued requests (they still run) and is dropped once it has
+        none; new requests for a retiring job are refused."""
         with self._lock:
-            j = self._jobs[job_id]
+            j = self._jobs.get(job_id)
+            if j is None:
+                raise ValueError(f"job {job_id!r} is not registered")
             j.retiring = True
             self._maybe_free_locked(j)
             self._lock.notify_all()
@@ -280,7 +285,7 @@ class ScoringServer:
     def _admit_locked(self) -> None:
         for jid in self._order:
             j = self._jobs[jid]
-            if j.admitted or j.retiring:
+            if j.admitted:
                 continue
             if self._in_use + j.footprint > self.cap:
                 break  # admission in registration order
@@ -289,14 +294,18 @@ class ScoringServer:
             self._peak_in_use = max(self._peak_in_use, self._in_use)
 
     def _maybe_free_locked(self, j: _Job) -> None:
-        if j.retiring and j.admitted and not j.pending and not j.busy:
+        """Drop a retiring job with no queued or running work (releasing its
+        memory if it was admitted) and admit the jobs waiting behind it."""
+        if self._jobs.get(j.job_id) is not j or not j.retiring or j.pending or j.busy:
+            return
+        if j.admitted:
             j.job = None
             j.batch = None
             j.admitted = False
             self._in_use -= j.footprint
-            self._order.remove(j.job_id)
-            del self._jobs[j.job_id]
-            self._admit_locked()
+        self._order.remove(j.job_id)
+        del self._jobs[j.job_id]
+        self._admit_locked()
 
     def _next_locked(self) -> Optional[_Job]:
         best = None

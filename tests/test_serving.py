@@ -198,3 +198,29 @@ def test_deferred_admissions_and_peak_memory_are_counted():
         srv.retire("a")
         srv.submit("b", poses_of(2, 2)).result(timeout=30)
         assert srv.stats().peak_in_use == 70
+
+
+def test_retiring_a_deferred_job_still_serves_its_queued_requests():
+    """A job retired before admission keeps its place while it has queued
+    requests: they run once memory frees up, then the job is dropped and
+    its id can be registered again; a deferred job retired with nothing
+    queued is dropped at once."""
+    with FakeServer(hbm_cap_bytes=100, max_batch=8, n_workers=1) as srv:
+        srv.register("a", lambda: 1.0, 70)
+        srv.register("b", lambda: 2.0, 50)   # deferred
+        srv.register("c", lambda: 3.0, 40)   # deferred behind b
+        fb = srv.submit("b", poses_of(5, 3))
+        srv.retire("b")
+        with pytest.raises(ValueError):
+            srv.submit("b", poses_of(6, 1))  # retiring: no new requests
+        srv.retire("c")                      # nothing queued: dropped now
+        assert srv.memory_in_use() == 70
+        srv.register("c", lambda: 4.0, 40)   # the id is free again
+        srv.submit("a", poses_of(1, 2)).result(timeout=30)
+        srv.retire("a")
+        np.testing.assert_array_equal(fb.result(timeout=30), poses_of(5, 3).sum(axis=1) * 2.0)
+        srv.drain(timeout=30)
+        assert srv.is_admitted("c") and srv.memory_in_use() == 40
+        assert srv.built == ["a", "b"]
+        with pytest.raises(ValueError):
+            srv.retire("b")                  # already gone

@@ -269,11 +269,19 @@ class ScoringServer:
             self._t0 = None
 
     def close(self) -> None:
+        """Stop accepting requests, let the workers finish what admitted jobs
+        have queued, then fail the requests of jobs never admitted."""
         with self._lock:
             self._closed = True
             self._lock.notify_all()
         for w in self._workers:
             w.join()
+        with self._lock:
+            for j in self._jobs.values():
+                while j.pending:
+                    r = j.pending.popleft()
+                    if not r.future.done():
+                        r.future.set_exception(RuntimeError(f"server closed before job {j.job_id!r} was admitted"))
 
     def __enter__(self):
         return self

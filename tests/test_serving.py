@@ -224,3 +224,15 @@ def test_retiring_a_deferred_job_still_serves_its_queued_requests():
         assert srv.built == ["a", "b"]
         with pytest.raises(ValueError):
             srv.retire("b")                  # already gone
+
+
+def test_close_fails_requests_of_jobs_never_admitted():
+    srv = FakeServer(hbm_cap_bytes=100, max_batch=8, n_workers=1)
+    srv.register("a", lambda: 1.0, 70)
+    srv.register("b", lambda: 2.0, 50)   # never admitted: a is not retired
+    fa = srv.submit("a", poses_of(1, 2))
+    fb = srv.submit("b", poses_of(2, 2))
+    srv.close()
+    np.testing.assert_array_equal(fa.result(timeout=30), poses_of(1, 2).sum(axis=1))
+    with pytest.raises(RuntimeError, match="closed"):
+        fb.result(timeout=30)

@@ -1,7 +1,7 @@
 """Launch-shape autotuner for batched scoring.
 
-Two choices decide the correlation's speed for a given box, crop, psi count
-and particle set, and the best value depends on the GPU:
+Four launch choices decide a batch's speed for a given box, crop, psi count
+and particle set, and the best values depend on the GPU:
 
 * the thread-block cluster size of the plain FP32 correlation (CTAs that
   split one particle's packed columns; each holds its columns of every psi
@@ -99,12 +99,27 @@ class Autotuner:
         except (OSError, ValueError):
             return {}
 
-    def _save(self, data: dict) -> None:
+    def _save(self, key: str, entry: dict) -> None:
+        """Add one entry to the cache file. Under an exclusive lock on a
+        side file it re-reads the cache, so entries that other processes
+        (replicas tuning at the same time) wrote are kept, and replaces it
+        through a temporary file of this process."""
+        import fcntl
+        import tempfile
         try:
             self.cache_path.parent.mkdir(parents=True, exist_ok=True)
-            tmp = self.cache_path.with_suffix(".tmp")
-            tmp.write_text(json.dumps(data, indent=1, sort_keys=True))
-            os.replace(tmp, self.cache_path)
+            with open(str(self.cache_path) + ".lock", "w") as lock:
+                fcntl.flock(lock, fcntl.LOCK_EX)
+                data = self._load()
+                data[key] = entry
+                fd, tmp = tempfile.mkstemp(dir=self.cache_path.parent, prefix=self.cache_path.name, suffix=".tmp")
+                try:
+                    with os.fdopen(fd, "w") as fh:
+                        fh.write(json.dumps(data, indent=1, sort_keys=True))
+                    os.replace(tmp, self.cache_path)
+                except OSError:
+                    os.unlink(tmp)
+                    raise
         except OSError:
             pass  # a read-only home only loses the cache
 
@@ -184,7 +199,6 @@ class Autotuner:
         r = TuneResult(key=key, size=nb, corr_cluster=best_k, tc_chunk=best_c, times_ms=times,
                        tc_a_stages=best_ring[0], tc_b_stages=best_ring[1], dirs_per_tile=dpt,
                        template_lanes=best_l)
-        cache[key] = asdict(r)
-        self._save(cache)
+        self._save(key, asdict(r))
         r.apply()
         return r

@@ -31,9 +31,13 @@ def read_mrc(path, mmap: bool = True) -> np.ndarray:
     if len(raw) < 1024:
         raise ValueError(f"{path} is not an MRC file (short header)")
     endian, nx, ny, nz, mode, nsymbt = _header(raw)
+    if min(nx, ny, nz) <= 0 or nsymbt < 0:
+        raise ValueError(f"{path}: invalid MRC header (size {nx} x {ny} x {nz}, extended header {nsymbt} bytes)")
     dtype = np.dtype(_MODES[mode]).newbyteorder(endian)
     offset = 1024 + nsymbt
     count = nx * ny * nz
+    if path.stat().st_size < offset + count * dtype.itemsize:
+        raise ValueError(f"{path} is truncated: the header announces {nx} x {ny} x {nz} values")
     if mmap:
         data = np.memmap(path, dtype=dtype, mode="r", offset=offset, shape=(count,))
     else:

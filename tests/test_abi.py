@@ -136,3 +136,29 @@ def test_projector_status_calls_check_their_arguments(native_lib):
     v = C.c_int(7)
     assert lib.gisapr_projector_status(None, None, C.byref(v)) == 1
     assert lib.gisapr_set_projector_wait(None, C.c_longlong(0)) == 1
+
+
+def _native_signatures():
+    from gisapr_gb300 import _native
+    return _native.SIGNATURES
+
+
+_NO_STATUS = ("gisapr_abi_version", "gisapr_tc_bank_bytes", "gisapr_project_launches", "gisapr_context_destroy")
+
+
+@pytest.mark.parametrize("name", [n for n in _native_signatures() if n not in _NO_STATUS])
+def test_every_entry_point_rejects_null_pointers_without_gpu(native_lib, name):
+    """Every status-returning entry point, called with every pointer NULL
+    (sizes 4, scalars 1), returns the argument error and a message before
+    it touches the device."""
+    from gisapr_gb300 import _native
+    args = []
+    for t in _native.SIGNATURES[name]:
+        if t is C.c_void_p or (isinstance(t, type) and issubclass(t, C._Pointer)):
+            args.append(None)
+        elif t in (C.c_double, C.c_float):
+            args.append(t(1.0))
+        else:
+            args.append(t(4))
+    assert getattr(native_lib, name)(*args) == _native.ERR_ARGUMENT
+    assert native_lib.gisapr_last_error()
